@@ -1,0 +1,137 @@
+"""Pin the CPU oracle (oracle/oracle.cc) to the reference's own known-answer
+vectors (source/lib/tests/*.cc, source/tests/pt/test_tabulate_fusion_se_a.py)
+and to fixtures produced by the reference's CPU library (ref_water.npz).
+CPU only."""
+
+import numpy as np
+import pytest
+
+
+def _sec_sel(sec):
+    return [sec[i + 1] - sec[i] for i in range(len(sec) - 1)]
+
+
+def _fixture_env(O, fx, dtype=np.float64):
+    """copy_coord + format + env mat of the reference's 6-atom fixture
+    (13 A box), as test_env_mat_a.cc / test_prod_force_a.cc SetUp do."""
+    posi = np.array(fx["posi"], dtype)
+    atype = np.array(fx["atype"], np.int32)
+    box = np.array(fx["box"], dtype)
+    sel = _sec_sel(fx["sec_a"])
+    ec, et, emap = O.copy_coord(posi, atype, box, fx["rc"])
+    nloc = len(atype)
+    nnei = sum(sel)
+    avg = np.zeros((2, nnei * 4), dtype)
+    std = np.ones((2, nnei * 4), dtype)
+    em, emd, rij, nl = O.prod_env_mat_a_ext(ec, et, nloc, avg, std, fx["rc"], fx["rc_smth"], sel)
+    return dict(nloc=nloc, nall=len(et), nnei=nnei, em=em, emd=emd, rij=rij, nl=nl,
+                ec=ec, et=et, emap=emap, sel=sel)
+
+
+@pytest.mark.parametrize("name", ["TestEnvMatA", "TestEnvMatAShortSel"])
+def test_env_mat_golden(oracle, golden_lib, name):
+    fx = golden_lib[name]
+    r = _fixture_env(oracle, fx)
+    np.testing.assert_allclose(r["em"], np.array(fx["expected_env"]), atol=1e-5)
+
+
+@pytest.mark.parametrize("name", ["TestFormatNlist", "TestFormatNlistShortSel"])
+def test_format_nlist_golden(oracle, golden_lib, name):
+    fx = golden_lib[name]
+    posi = np.array(fx["posi"])
+    atype = np.array(fx["atype"], np.int32)
+    ec, et, emap = oracle.copy_coord(posi, atype, np.array(fx["box"]), fx["rc"])
+    nl = oracle.format_nlist(ec, et, len(atype), fx["rc"], _sec_sel(fx["sec_a"]))
+    np.testing.assert_array_equal(nl.reshape(-1), np.array(fx["expect_nlist_cpy"]))
+
+
+def test_prod_force_golden(oracle, golden_lib):
+    fx = golden_lib["TestProdForceA"]
+    r = _fixture_env(oracle, fx)
+    nd = r["nloc"] * r["nnei"] * 4
+    net = 10 - np.arange(nd) * 0.01
+    nf = fx["nframes"]
+    f = oracle.prod_force_a(np.tile(net, nf), np.tile(r["emd"], nf), np.tile(r["nl"], nf),
+                            r["nloc"], r["nall"], r["nnei"], nf)
+    exp = np.tile(np.array(fx["expected_force"]), nf)
+    np.testing.assert_allclose(f.reshape(-1), exp, atol=1e-5)
+
+
+def test_prod_virial_golden(oracle, golden_lib):
+    fx = golden_lib["TestProdVirialA"]
+    r = _fixture_env(oracle, fx)
+    nd = r["nloc"] * r["nnei"] * 4
+    net = 10 - np.arange(nd) * 0.01
+    v, av = oracle.prod_virial_a(net, r["emd"], r["rij"], r["nl"], r["nloc"], r["nall"], r["nnei"])
+    np.testing.assert_allclose(v, np.array(fx["expected_virial"]), atol=1e-5)
+    np.testing.assert_allclose(av, np.array(fx["expected_atom_virial"]), atol=1e-5)
+
+
+def test_prod_force_grad_golden(oracle, golden_lib):
+    fx = golden_lib["TestProdForceGradA"]
+    r = _fixture_env(oracle, fx)
+    nf = fx["nframes"]
+    grad = 10 - np.arange(r["nloc"] * 3) * 0.1
+    g = oracle.prod_force_grad_a(np.tile(grad, nf), np.tile(r["emd"], nf), np.tile(r["nl"], nf),
+                                 r["nloc"], r["nnei"], nf)
+    np.testing.assert_allclose(g, np.tile(np.array(fx["expected_grad_net"]), nf), atol=1e-5)
+
+
+def test_prod_virial_grad_golden(oracle, golden_lib):
+    fx = golden_lib["TestProdVirialGradA"]
+    r = _fixture_env(oracle, fx)
+    grad = 10 - np.arange(9) * 1.0
+    g = oracle.prod_virial_grad_a(grad, r["emd"], r["rij"], r["nl"], r["nloc"], r["nnei"])
+    np.testing.assert_allclose(g, np.array(fx["expected_grad_net"]), atol=1e-5)
+
+
+def test_tabulate_lib_golden(oracle, golden_lib):
+    fx = golden_lib["TestTabulateSeA"]
+    nloc, nnei, M = fx["nloc"], fx["nnei"], fx["last_layer_size"]
+    table = np.array(fx["table"]).reshape(-1, 6 * M)
+    info = np.array(fx["info"])
+    em_x = np.array(fx["em_x"]).reshape(nloc * nnei, 1)
+    em = np.array(fx["em"]).reshape(nloc, nnei, 4)
+    out = oracle.tabulate_fusion_se_a(table, info, em_x, em, M)
+    np.testing.assert_allclose(out.reshape(-1), fx["expected_xyz_scatter"], atol=1e-5)
+    gx, gm = oracle.tabulate_fusion_se_a_grad(table, info, em_x, em, np.ones((nloc, 4, M)))
+    np.testing.assert_allclose(gx.reshape(-1), fx["expected_dy_dem_x"], atol=1e-5)
+    np.testing.assert_allclose(gm.reshape(-1), fx["expected_dy_dem"], atol=1e-5)
+
+
+@pytest.mark.parametrize("dtype,prec", [(np.float64, 1e-10), (np.float32, 1e-5)])
+def test_tabulate_pt_golden(oracle, golden_pt, dtype, prec):
+    g = golden_pt
+    M = 8
+    table = np.array(g["table_tensor"]["values"], dtype).reshape(-1, 6 * M)
+    info = np.array(g["table_info_tensor"]["values"], dtype)
+    em_x = np.array(g["em_x_tensor"]["values"], dtype).reshape(-1, 1)
+    em = np.array(g["em_tensor"]["values"], dtype).reshape(4, 4, 4)
+    out = oracle.tabulate_fusion_se_a(table, info, em_x, em, M)
+    exp = np.array(g["expected_descriptor_tensor"]["values"], dtype).reshape(4, 4, M)
+    np.testing.assert_allclose(out, exp, atol=prec, rtol=prec)
+    gx, gm = oracle.tabulate_fusion_se_a_grad(table, info, em_x, em, np.ones((4, 4, M), dtype))
+    np.testing.assert_allclose(gx.reshape(-1), np.array(g["expected_dy_dem_x"]["values"], dtype),
+                               atol=prec, rtol=prec)
+    np.testing.assert_allclose(gm.reshape(-1), np.array(g["expected_dy_dem"]["values"], dtype),
+                               atol=prec, rtol=prec)
+
+
+@pytest.mark.parametrize("tag", ["w192", "w24", "w1536"])
+@pytest.mark.parametrize("sfx,dtype", [("f64", np.float64), ("f32", np.float32)])
+def test_env_mat_vs_reference_run(oracle, golden_water, tag, sfx, dtype):
+    """Bit-exact against the reference library's own output on seeded water."""
+    g = golden_water
+    sel = list(g["sel"])
+    nnei = sum(sel)
+    em, emd, rij, nl, ec, et, emap = oracle.prod_env_mat_a_pbc(
+        g[f"{tag}_coord"].astype(dtype), g[f"{tag}_atype"], g[f"{tag}_box"].astype(dtype),
+        g["avg"].astype(dtype), g["std"].astype(dtype), float(g["rcut"]), float(g["rcut_smth"]),
+        sel, return_ext=True)
+    np.testing.assert_array_equal(nl, g[f"{tag}_{sfx}_nlist"].astype(np.int32))
+    np.testing.assert_array_equal(emap, g[f"{tag}_{sfx}_mapping"].astype(np.int32))
+    assert len(et) == int(g[f"{tag}_{sfx}_nall"])
+    keep = 24 * nnei
+    np.testing.assert_array_equal(em[: keep * 4], g[f"{tag}_{sfx}_em"])
+    np.testing.assert_array_equal(emd[: keep * 12], g[f"{tag}_{sfx}_em_deriv"])
+    np.testing.assert_array_equal(rij[: keep * 3], g[f"{tag}_{sfx}_rij"])

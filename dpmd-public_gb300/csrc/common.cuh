@@ -1,0 +1,165 @@
+// Shared device/host helpers for the GB300 (sm_103a) se_e2_a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/gbdp.h"
+
+namespace gbdp {
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------------ error state --
+// The last error message is thread-local; entry points return a status code
+// and never throw across the C ABI.
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* where);
+
+#define GBDP_CHECK_LAUNCH(where)                                        \
+  do {                                                                  \
+    cudaError_t _e = cudaGetLastError();                                \
+    if (_e != cudaSuccess) return ::gbdp::cuda_status(_e, where);       \
+  } while (0)
+
+#define GBDP_REQUIRE(cond, ...)                \
+  do {                                         \
+    if (!(cond)) {                             \
+      ::gbdp::set_error(__VA_ARGS__);          \
+      return GBDP_ERR_INVALID;                 \
+    }                                          \
+  } while (0)
+
+// ------------------------------------------------------------ warp helpers --
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Device-side error word: kernels record the first problem they hit and
+// return; the host reads the word after the stream is synchronised.
+__device__ __forceinline__ void raise_status(int* status, int code) {
+  if (status) atomicCAS(status, 0, code);
+}
+
+// ------------------------------------------------------- table addressing --
+// locate_xx of the reference (source/lib/src/tabulate.cc:19-42): the row of a
+// normalised s value and its offset inside that row, two uniform strides,
+// clamped outside [lower, max).
+template <typename T>
+struct TableInfo {
+  T lower, upper, max, stride0, stride1;
+  int first_stride;  // int((upper - lower) / stride0)
+  int last_row;      // first_stride + int((max - upper) / stride1) - 1
+};
+
+__device__ __forceinline__ float fmul_x(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double fmul_x(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fadd_x(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double fadd_x(double a, double b) { return __dadd_rn(a, b); }
+
+// The row offset is formed as in the reference (multiply, round, add, round;
+// no fused multiply-add) so that every x lands in the same row.
+template <typename T>
+__device__ __forceinline__ int locate_row(const TableInfo<T>& ti, T& xx) {
+  int idx;
+  if (xx < ti.lower) {
+    idx = 0;
+    xx = T(0);
+  } else if (xx < ti.upper) {
+    idx = (int)((xx - ti.lower) / ti.stride0);
+    xx -= fadd_x(fmul_x((T)idx, ti.stride0), ti.lower);
+  } else if (xx < ti.max) {
+    idx = ti.first_stride + (int)((xx - ti.upper) / ti.stride1);
+    xx -= fadd_x(fmul_x((T)(idx - ti.first_stride), ti.stride1), ti.upper);
+  } else {
+    idx = ti.last_row;
+    xx = T(0);
+  }
+  return idx;
+}
+
+template <typename T>
+TableInfo<T> make_table_info(const T* info) {
+  TableInfo<T> ti;
+  ti.lower = info[0];
+  ti.upper = info[1];
+  ti.max = info[2];
+  ti.stride0 = info[3];
+  ti.stride1 = info[4];
+  ti.first_stride = int((ti.upper - ti.lower) / ti.stride0);
+  ti.last_row = ti.first_stride + int((ti.max - ti.upper) / ti.stride1) - 1;
+  return ti;
+}
+
+// Horner forms of the fifth-order row polynomial and its derivative, in the
+// reference's evaluation order (tabulate.cc:119-128, :214-219).
+template <typename T>
+__device__ __forceinline__ T poly5(const T* a, T x) {
+  return a[0] + (a[1] + (a[2] + (a[3] + (a[4] + a[5] * x) * x) * x) * x) * x;
+}
+template <typename T>
+__device__ __forceinline__ T dpoly5(const T* a, T x) {
+  return a[1] + (T(2) * a[2] + (T(3) * a[3] + (T(4) * a[4] + T(5) * a[5] * x) * x) * x) * x;
+}
+
+// --------------------------------------------------- bulk async copy (TMA) --
+// cp.async.bulk global -> shared completing on an mbarrier.  Both addresses
+// must be 16-byte aligned and the size a multiple of 16.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, "
+      "1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after `limit` polls and reports it through `status`.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase, int* status,
+                                                  long limit = (1l << 26)) {
+  for (long it = 0; it < limit; ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  raise_status(status, GBDP_STATUS_TIMEOUT);
+  return false;
+}
+
+}  // namespace gbdp

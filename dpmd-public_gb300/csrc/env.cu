@@ -1,0 +1,830 @@
+// Periodic neighbour build + environment matrix for se_e2_a (sm_103a).
+//
+// Pipeline per packed batch of frames (one launch each, all stream-ordered,
+// no host synchronisation, capturable in a CUDA graph):
+//   k_localize   wrap local atoms into the box, write them as the first
+//                extended atoms, bin them into the reference's cells;
+//   k_cell_scan  one CTA per frame: cell offsets, ghost offsets, nall;
+//   k_cell_bucket / k_cell_rank  atoms of each cell in ascending index order;
+//   k_ghost_fill one warp per extended cell: ghost images in copy_coord order
+//                and a cell-ordered packed copy of every extended atom;
+//   k_nlist_env  one warp per centre atom: candidates from the stencil of
+//                cells, per-type rank by (float r^2, index), env matrix row
+//                and its derivative, normalised by davg/dstd.
+#include <algorithm>
+#include <cstring>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gbdp {
+namespace {
+
+constexpr int kMaxTypes = 16;
+constexpr int kEnvWarps = 4;  // warps (centre atoms) per CTA in k_nlist_env
+
+struct SecInfo {
+  int ntypes;
+  int nnei;
+  int sec[kMaxTypes + 1];
+};
+
+struct __align__(32) D4 {
+  double x, y, z, w;
+};
+
+template <typename T>
+struct XsOf;
+template <>
+struct XsOf<float> {
+  using type = float4;
+};
+template <>
+struct XsOf<double> {
+  using type = D4;
+};
+
+__device__ __forceinline__ int pack_idx_type(int idx, int type) {
+  return (int)(((unsigned)(type & 0xff) << 24) | (unsigned)idx);
+}
+
+__device__ __forceinline__ float4 make_xs(float x, float y, float z, int packed) {
+  return make_float4(x, y, z, __int_as_float(packed));
+}
+__device__ __forceinline__ D4 make_xs(double x, double y, double z, int packed) {
+  D4 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  r.w = (double)packed;
+  return r;
+}
+__device__ __forceinline__ int xs_packed(const float4& v) { return __float_as_int(v.w); }
+__device__ __forceinline__ int xs_packed(const D4& v) { return (int)v.w; }
+
+// Exact (non-contracted) arithmetic helpers, so that the wrap into the box
+// and the float r^2 sort key round exactly like the reference's CPU code.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fmod1(float a) { return fmodf(a, 1.0f); }
+__device__ __forceinline__ double fmod1(double a) { return fmod(a, 1.0); }
+
+template <typename T>
+__device__ __forceinline__ const T* box_of(const gbdp_nbr_frame& g);
+template <>
+__device__ __forceinline__ const float* box_of<float>(const gbdp_nbr_frame& g) {
+  return g.boxf;
+}
+template <>
+__device__ __forceinline__ const double* box_of<double>(const gbdp_nbr_frame& g) {
+  return g.box;
+}
+template <typename T>
+__device__ __forceinline__ const T* rec_of(const gbdp_nbr_frame& g);
+template <>
+__device__ __forceinline__ const float* rec_of<float>(const gbdp_nbr_frame& g) {
+  return g.recf;
+}
+template <>
+__device__ __forceinline__ const double* rec_of<double>(const gbdp_nbr_frame& g) {
+  return g.rec;
+}
+
+__device__ __forceinline__ int floordiv(int a, int b) {
+  int q = a / b;
+  return (a % b != 0 && (a < 0)) ? q - 1 : q;
+}
+
+__device__ __forceinline__ int find_frame_atom(const gbdp_nbr_frame* fr, int nframes, int i) {
+  int lo = 0, hi = nframes - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].atom_off <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int find_frame_cell(const gbdp_nbr_frame* fr, int nframes, int e) {
+  int lo = 0, hi = nframes - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].ext_cell_off <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// ----------------------------------------------------------- k_localize --
+// source/lib/src/coord.cc:13-28 (normalize_coord_cpu) and the cell index of
+// source/lib/src/neighbor_list.cc:86-111 (build_clist).
+template <typename T>
+__global__ void k_localize(const gbdp_nbr_frame* __restrict__ fr, int nframes, int nloc_total,
+                           const T* __restrict__ coord, const int* __restrict__ atype,
+                           T* __restrict__ ext_coord, int* __restrict__ ext_type,
+                           int* __restrict__ ext_map, int* __restrict__ atom_frame,
+                           int* __restrict__ atom_cell, int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nloc_total) return;
+  const int f = find_frame_atom(fr, nframes, i);
+  const gbdp_nbr_frame& g = fr[f];
+  const int il = i - g.atom_off;
+  const T* box = box_of<T>(g);
+  const T* rec = rec_of<T>(g);
+  T p[3] = {coord[3 * (size_t)i], coord[3 * (size_t)i + 1], coord[3 * (size_t)i + 2]};
+  T ri[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T v = add_rn(add_rn(mul_rn(p[0], rec[d * 3 + 0]), mul_rn(p[1], rec[d * 3 + 1])),
+                 mul_rn(p[2], rec[d * 3 + 2]));
+    v = fmod1(v);
+    if (v < T(0)) v = add_rn(v, T(1));
+    ri[d] = v;
+  }
+  T q[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    q[d] = add_rn(add_rn(mul_rn(ri[0], box[0 * 3 + d]), mul_rn(ri[1], box[1 * 3 + d])),
+                  mul_rn(ri[2], box[2 * 3 + d]));
+  const size_t e = (size_t)g.ext_off + il;
+  ext_coord[3 * e + 0] = q[0];
+  ext_coord[3 * e + 1] = q[1];
+  ext_coord[3 * e + 2] = q[2];
+  ext_type[e] = atype[i];
+  ext_map[e] = il;
+  // cell from the wrapped coordinate, in double (SimulationRegion<double>)
+  double pd[3] = {(double)q[0], (double)q[1], (double)q[2]};
+  int ci[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double in = __dadd_rn(__dadd_rn(__dmul_rn(pd[0], g.rec[d * 3 + 0]),
+                                    __dmul_rn(pd[1], g.rec[d * 3 + 1])),
+                          __dmul_rn(pd[2], g.rec[d * 3 + 2]));
+    double cs = 1. / g.ncell[d];
+    int k = (int)(in / cs);
+    if (in < 0.) --k;
+    k = max(0, min(k, g.ncell[d] - 1));
+    ci[d] = k;
+  }
+  const int c = g.cell_off + (ci[0] * g.ncell[1] + ci[1]) * g.ncell[2] + ci[2];
+  atom_frame[i] = f;
+  atom_cell[i] = c;
+  atomicAdd(&cell_count[c], 1);
+}
+
+// Block-wide exclusive scan (blockDim.x multiple of 32, <= 1024).
+__device__ int block_excl_scan(int v, int* warp_tot, int& total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(kFull, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) warp_tot[lane] = t;
+  }
+  __syncthreads();
+  const int off = w > 0 ? warp_tot[w - 1] : 0;
+  total = warp_tot[nw - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+__device__ __forceinline__ void ext_cell_source(const gbdp_nbr_frame& g, int e, int* ii,
+                                                int* sh, int& src, bool& local) {
+  const int n1 = g.ncell[1] + 2 * g.ngcell[1], n2 = g.ncell[2] + 2 * g.ngcell[2];
+  int e0 = e / (n1 * n2), r = e - e0 * n1 * n2;
+  int e1 = r / n2, e2 = r - e1 * n2;
+  ii[0] = e0 - g.ngcell[0];
+  ii[1] = e1 - g.ngcell[1];
+  ii[2] = e2 - g.ngcell[2];
+  local = true;
+  int jj[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    // compute_pbc_shift of neighbor_list.cc:727-743 in closed form
+    sh[d] = -floordiv(ii[d], g.ncell[d]);
+    jj[d] = ii[d] + sh[d] * g.ncell[d];
+    local = local && ii[d] >= 0 && ii[d] < g.ncell[d];
+  }
+  src = g.cell_off + (jj[0] * g.ncell[1] + jj[1]) * g.ncell[2] + jj[2];
+}
+
+// ---------------------------------------------------------- k_cell_scan --
+__global__ void k_cell_scan(const gbdp_nbr_frame* __restrict__ fr,
+                            const int* __restrict__ cell_count, int* __restrict__ cell_start,
+                            int* __restrict__ ext_start, int* __restrict__ ext_cnt,
+                            int* __restrict__ ghost_start, int* __restrict__ ext_nall,
+                            int* __restrict__ status) {
+  __shared__ int warp_tot[32];
+  const gbdp_nbr_frame& g = fr[blockIdx.x];
+  const int ncl = g.ncell[0] * g.ncell[1] * g.ncell[2];
+  int carry = 0;
+  for (int base = 0; base < ncl; base += blockDim.x) {
+    int c = base + threadIdx.x;
+    int v = c < ncl ? cell_count[g.cell_off + c] : 0;
+    int tot;
+    int ex = block_excl_scan(v, warp_tot, tot);
+    if (c < ncl) cell_start[g.cell_off + c] = g.atom_off + carry + ex;
+    carry += tot;
+  }
+  const int ne = (g.ncell[0] + 2 * g.ngcell[0]) * (g.ncell[1] + 2 * g.ngcell[1]) *
+                 (g.ncell[2] + 2 * g.ngcell[2]);
+  int carry_all = 0, carry_ghost = 0;
+  for (int base = 0; base < ne; base += blockDim.x) {
+    int e = base + threadIdx.x;
+    int cnt = 0, gcnt = 0;
+    if (e < ne) {
+      int ii[3], sh[3], src;
+      bool local;
+      ext_cell_source(g, e, ii, sh, src, local);
+      cnt = cell_count[src];
+      gcnt = local ? 0 : cnt;
+    }
+    int tot_all, tot_ghost;
+    int ex_all = block_excl_scan(cnt, warp_tot, tot_all);
+    int ex_ghost = block_excl_scan(gcnt, warp_tot, tot_ghost);
+    if (e < ne) {
+      ext_start[g.ext_cell_off + e] = g.ext_off + carry_all + ex_all;
+      ext_cnt[g.ext_cell_off + e] = cnt;
+      ghost_start[g.ext_cell_off + e] = g.nloc + carry_ghost + ex_ghost;
+    }
+    carry_all += tot_all;
+    carry_ghost += tot_ghost;
+  }
+  if (threadIdx.x == 0) {
+    const int nall = g.nloc + carry_ghost;
+    ext_nall[blockIdx.x] = nall;
+    if (nall > g.ext_cap) raise_status(status, GBDP_STATUS_EXT_OVERFLOW);
+  }
+}
+
+// ------------------------------------------- k_cell_bucket / k_cell_rank --
+__global__ void k_cell_bucket(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
+                              const int* __restrict__ atom_frame,
+                              const int* __restrict__ atom_cell,
+                              const int* __restrict__ cell_start, int* __restrict__ cell_fill,
+                              int* __restrict__ bucket) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nloc_total) return;
+  const int c = atom_cell[i];
+  const int slot = atomicAdd(&cell_fill[c], 1);
+  bucket[cell_start[c] + slot] = i - fr[atom_frame[i]].atom_off;
+}
+
+// Ascending local index inside each cell: the order build_clist pushes them.
+__global__ void k_cell_rank(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
+                            const int* __restrict__ atom_frame,
+                            const int* __restrict__ atom_cell,
+                            const int* __restrict__ cell_start,
+                            const int* __restrict__ cell_count, const int* __restrict__ bucket,
+                            int* __restrict__ cell_atoms) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nloc_total) return;
+  const int c = atom_cell[i];
+  const int il = i - fr[atom_frame[i]].atom_off;
+  const int s = cell_start[c], n = cell_count[c];
+  int rank = 0;
+  for (int k = 0; k < n; ++k) rank += bucket[s + k] < il;
+  cell_atoms[s + rank] = il;
+}
+
+// --------------------------------------------------------- k_ghost_fill --
+// source/lib/src/neighbor_list.cc:796-845: for each extended cell in
+// lexicographic order that is not local, the atoms of its periodic source
+// cell shifted by the image vector (double arithmetic, rounded to T).
+template <typename T>
+__global__ void k_ghost_fill(const gbdp_nbr_frame* __restrict__ fr, int nframes,
+                             int next_cell_total, const int* __restrict__ cell_start,
+                             const int* __restrict__ cell_count,
+                             const int* __restrict__ cell_atoms,
+                             const int* __restrict__ ext_start,
+                             const int* __restrict__ ghost_start, T* __restrict__ ext_coord,
+                             int* __restrict__ ext_type, int* __restrict__ ext_map,
+                             typename XsOf<T>::type* __restrict__ xs) {
+  const int ew = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (ew >= next_cell_total) return;
+  const int f = find_frame_cell(fr, nframes, ew);
+  const gbdp_nbr_frame& g = fr[f];
+  const int e = ew - g.ext_cell_off;
+  int ii[3], sh[3], src;
+  bool local;
+  ext_cell_source(g, e, ii, sh, src, local);
+  double sv[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    sv[d] = __dadd_rn(__dadd_rn(__dmul_rn((double)sh[0], g.box[0 * 3 + d]),
+                                __dmul_rn((double)sh[1], g.box[1 * 3 + d])),
+                      __dmul_rn((double)sh[2], g.box[2 * 3 + d]));
+  const int n = cell_count[src], s = cell_start[src];
+  const int xs0 = ext_start[ew], g0 = ghost_start[ew];
+  const int xs_end = g.ext_off + g.ext_cap;
+  for (int k = lane; k < n; k += 32) {
+    // slots past the frame's reservation are never written (k_cell_scan has
+    // already raised GBDP_STATUS_EXT_OVERFLOW for that case)
+    if (xs0 + k >= xs_end || (!local && g0 + k >= g.ext_cap)) break;
+    const int p = cell_atoms[s + k];
+    const size_t ep = (size_t)g.ext_off + p;
+    T x = ext_coord[3 * ep], y = ext_coord[3 * ep + 1], z = ext_coord[3 * ep + 2];
+    const int t = ext_type[ep];
+    int idx = p;
+    if (!local) {
+      idx = g0 + k;
+      x = (T)__dsub_rn((double)x, sv[0]);
+      y = (T)__dsub_rn((double)y, sv[1]);
+      z = (T)__dsub_rn((double)z, sv[2]);
+      const size_t eg = (size_t)g.ext_off + idx;
+      ext_coord[3 * eg] = x;
+      ext_coord[3 * eg + 1] = y;
+      ext_coord[3 * eg + 2] = z;
+      ext_type[eg] = t;
+      ext_map[eg] = p;
+    }
+    xs[xs0 + k] = make_xs(x, y, z, pack_idx_type(idx, t));
+  }
+}
+
+// --------------------------------------------------------- k_nlist_env --
+// Candidate test and key: source/lib/src/neighbor_list.cc:893-903
+// (r^2 < rc^2 in the coordinate type) and source/lib/src/fmt_nlist.cc:114-143
+// (float r^2 <= float rc^2, order by (type, float r^2, index), first sel[t]
+// of each type).  Env row: source/lib/src/env_mat.cc:122-226 with
+// source/lib/include/switcher.h:60-83; normalisation prod_env_mat.cc:84-100.
+template <typename T>
+__device__ __forceinline__ void spline5(T& vv, T& dd, T xx, T rmin, T rmax) {
+  if (xx < rmin) {
+    dd = T(0);
+    vv = T(1);
+  } else if (xx < rmax) {
+    T uu = (xx - rmin) / (rmax - rmin);
+    T du = T(1) / (rmax - rmin);
+    vv = uu * uu * uu * (T(-6) * uu * uu + T(15) * uu - T(10)) + T(1);
+    dd = (T(3) * uu * uu * (T(-6) * uu * uu + T(15) * uu - T(10)) +
+          uu * uu * uu * (T(-12) * uu + T(15))) *
+         du;
+  } else {
+    dd = T(0);
+    vv = T(0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ bool cand_test(const typename XsOf<T>::type& r, T xi, T yi, T zi,
+                                          float rc2f, float& key);
+
+template <>
+__device__ __forceinline__ bool cand_test<float>(const float4& r, float xi, float yi, float zi,
+                                                 float rc2f, float& key) {
+  float dx = __fsub_rn(r.x, xi), dy = __fsub_rn(r.y, yi), dz = __fsub_rn(r.z, zi);
+  float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  key = r2;
+  return r2 < rc2f;
+}
+
+template <>
+__device__ __forceinline__ bool cand_test<double>(const D4& r, double xi, double yi, double zi,
+                                                  float rc2f, float& key) {
+  double dx = __dsub_rn(xi, r.x), dy = __dsub_rn(yi, r.y), dz = __dsub_rn(zi, r.z);
+  double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  float fx = __fsub_rn((float)r.x, (float)xi), fy = __fsub_rn((float)r.y, (float)yi),
+        fz = __fsub_rn((float)r.z, (float)zi);
+  float r2f = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+  key = r2f;
+  return r2 < (double)rc2f && r2f <= rc2f;
+}
+
+template <typename T>
+__device__ __forceinline__ void store4(T* p, T a, T b, T c, T d);
+template <>
+__device__ __forceinline__ void store4<float>(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+template <>
+__device__ __forceinline__ void store4<double>(double* p, double a, double b, double c,
+                                               double d) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kEnvWarps * 32)
+    k_nlist_env(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
+                const int* __restrict__ atom_frame, const int* __restrict__ atom_cell,
+                const int* __restrict__ ext_start, const int* __restrict__ ext_cnt,
+                const typename XsOf<T>::type* __restrict__ xs, const T* __restrict__ ext_coord,
+                const int* __restrict__ ext_map, const int* __restrict__ atype,
+                const T* __restrict__ avg, const T* __restrict__ stdv, SecInfo si, float rc2f,
+                T rmin, T rmax, int max_cand, T* __restrict__ em, T* __restrict__ em_deriv,
+                T* __restrict__ rij, int* __restrict__ nlist, int* __restrict__ nlist_ext,
+                int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kEnvWarps + warp;
+  if (i >= nloc_total) return;
+  const int nnei = si.nnei;
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + (size_t)warp * max_cand;
+  int* row = reinterpret_cast<int*>(smem + (size_t)kEnvWarps * max_cand * 8) +
+             (size_t)warp * ((nnei + 3) & ~3);
+  unsigned char* ctype = smem + (size_t)kEnvWarps * max_cand * 8 +
+                         (size_t)kEnvWarps * ((nnei + 3) & ~3) * 4 + (size_t)warp * max_cand;
+
+  const gbdp_nbr_frame& g = fr[atom_frame[i]];
+  const int il = i - g.atom_off;
+  const size_t eoff = g.ext_off;
+  const T xi = ext_coord[3 * (eoff + il)], yi = ext_coord[3 * (eoff + il) + 1],
+          zi = ext_coord[3 * (eoff + il) + 2];
+  const int ti = atype[i];
+  const int c = atom_cell[i] - g.cell_off;
+  const int c0 = c / (g.ncell[1] * g.ncell[2]);
+  const int c1 = (c / g.ncell[2]) % g.ncell[1];
+  const int c2 = c % g.ncell[2];
+  const int n1 = g.ncell[1] + 2 * g.ngcell[1], n2 = g.ncell[2] + 2 * g.ngcell[2];
+
+  // ---- gather candidates from the stencil of extended cells
+  int ncand = 0;
+  for (int d0 = -g.stencil[0]; d0 <= g.stencil[0]; ++d0)
+    for (int d1 = -g.stencil[1]; d1 <= g.stencil[1]; ++d1)
+      for (int d2 = -g.stencil[2]; d2 <= g.stencil[2]; ++d2) {
+        const int e = g.ext_cell_off + ((c0 + g.ngcell[0] + d0) * n1 + (c1 + g.ngcell[1] + d1)) * n2 +
+                      (c2 + g.ngcell[2] + d2);
+        const int st = ext_start[e], cnt = ext_cnt[e];
+        for (int b = 0; b < cnt; b += 32) {
+          bool ok = false;
+          uint64_t key = 0;
+          int t = 0;
+          if (b + lane < cnt) {
+            const auto r = xs[st + b + lane];
+            const int pk = xs_packed(r);
+            const int idx = pk & 0xffffff;
+            t = (int)((unsigned)pk >> 24);
+            float k2;
+            ok = cand_test<T>(r, xi, yi, zi, rc2f, k2) && idx != il && t != 0xff &&
+                 t < si.ntypes;
+            key = ((uint64_t)__float_as_uint(k2) << 32) | (uint32_t)idx;
+          }
+          const unsigned m = __ballot_sync(kFull, ok);
+          const int pos = ncand + __popc(m & ((1u << lane) - 1u));
+          if (ok && pos < max_cand) {
+            keys[pos] = key;
+            ctype[pos] = (unsigned char)t;
+          }
+          ncand += __popc(m);
+        }
+      }
+  if (ncand > max_cand) {
+    if (lane == 0) raise_status(status, GBDP_STATUS_CAND_OVERFLOW);
+    ncand = max_cand;
+  }
+  for (int s = lane; s < nnei; s += 32) row[s] = -1;
+  __syncwarp();
+  // ---- rank inside each type: position = number of same-type candidates
+  //      with a smaller (r^2, index) key
+  for (int cidx = lane; cidx < ncand; cidx += 32) {
+    const uint64_t k = keys[cidx];
+    const int t = ctype[cidx];
+    int rank = 0;
+    for (int d = 0; d < ncand; ++d) rank += (ctype[d] == t) & (keys[d] < k);
+    const int sel_t = si.sec[t + 1] - si.sec[t];
+    if (rank < sel_t) row[si.sec[t] + rank] = (int)(uint32_t)(k & 0xffffffffu);
+  }
+  __syncwarp();
+
+  // ---- env matrix rows
+  const int nem = nnei * 4;
+  const T* av = avg + (size_t)max(ti, 0) * nem;
+  const T* sd = stdv + (size_t)max(ti, 0) * nem;
+  for (int s = lane; s < nnei; s += 32) {
+    const int j = row[s];
+    T e[4] = {T(0), T(0), T(0), T(0)};
+    T dv[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) dv[q] = T(0);
+    T rr[3] = {T(0), T(0), T(0)};
+    if (j >= 0) {
+      rr[0] = ext_coord[3 * (eoff + j)] - xi;
+      rr[1] = ext_coord[3 * (eoff + j) + 1] - yi;
+      rr[2] = ext_coord[3 * (eoff + j) + 2] - zi;
+      const T nr2 = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
+      const T inr = T(1) / sqrt(nr2);
+      const T nr = nr2 * inr;
+      const T inr2 = inr * inr;
+      const T inr4 = inr2 * inr2;
+      const T inr3 = inr4 * nr;
+      T sw, dsw;
+      spline5<T>(sw, dsw, nr, rmin, rmax);
+      e[0] = T(1) / nr;
+      e[1] = rr[0] / nr2;
+      e[2] = rr[1] / nr2;
+      e[3] = rr[2] / nr2;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dv[d] = rr[d] * inr3 * sw - e[0] * dsw * rr[d] * inr;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          T t = T(2) * rr[a] * rr[d] * inr4;
+          if (a == d) t -= inr2;
+          dv[3 + a * 3 + d] = t * sw - e[1 + a] * dsw * rr[d] * inr;
+        }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) e[q] *= sw;
+    }
+    const size_t o = ((size_t)i * nnei + s);
+    T out[4];
+    if (ti >= 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) out[q] = (e[q] - av[s * 4 + q]) / sd[s * 4 + q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) out[q] = T(0);
+    }
+    store4<T>(em + o * 4, out[0], out[1], out[2], out[3]);
+    if (em_deriv) {
+      T* dp = em_deriv + o * 12;
+#pragma unroll
+      for (int q = 0; q < 12; q += 4) {
+        if (ti >= 0)
+          store4<T>(dp + q, dv[q] / sd[s * 4 + q / 3], dv[q + 1] / sd[s * 4 + (q + 1) / 3],
+                    dv[q + 2] / sd[s * 4 + (q + 2) / 3], dv[q + 3] / sd[s * 4 + (q + 3) / 3]);
+        else
+          store4<T>(dp + q, T(0), T(0), T(0), T(0));
+      }
+    }
+    if (rij) {
+      rij[o * 3] = rr[0];
+      rij[o * 3 + 1] = rr[1];
+      rij[o * 3 + 2] = rr[2];
+    }
+    nlist[o] = j >= 0 ? ext_map[eoff + j] : -1;
+    if (nlist_ext) nlist_ext[o] = j;
+  }
+}
+
+// ------------------------------------------------------------ host side --
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct EnvWs {
+  int* status;
+  int* atom_frame;
+  int* atom_cell;
+  int* cell_count;
+  int* cell_fill;
+  int* cell_start;
+  int* bucket;
+  int* cell_atoms;
+  int* ext_start;
+  int* ext_cnt;
+  int* ghost_start;
+  void* xs;
+  size_t bytes;
+};
+
+EnvWs carve(const gbdp_nbr_plan& p, void* base, int fp64) {
+  EnvWs w;
+  char* b = static_cast<char*>(base);
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    char* r = b ? b + off : nullptr;
+    off += align256(n);
+    return r;
+  };
+  w.status = reinterpret_cast<int*>(take(256));
+  w.atom_frame = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.atom_cell = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.cell_count = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
+  w.cell_fill = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
+  w.cell_start = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
+  w.bucket = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.cell_atoms = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.ext_start = reinterpret_cast<int*>(take(sizeof(int) * p.next_cell_total));
+  w.ext_cnt = reinterpret_cast<int*>(take(sizeof(int) * p.next_cell_total));
+  w.ghost_start = reinterpret_cast<int*>(take(sizeof(int) * p.next_cell_total));
+  w.xs = take((fp64 ? 32 : 16) * (size_t)p.ext_total);
+  w.bytes = off;
+  return w;
+}
+
+template <typename T>
+int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
+               int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
+               const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
+               const gbdp_nbr_frame* frames, float rcut_smth, const int* sel, int ntypes,
+               void* workspace, size_t ws_bytes, cudaStream_t stream) {
+  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a: null plan/frames/workspace");
+  GBDP_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, "prod_env_mat_a: ntypes %d out of [1,%d]",
+               ntypes, kMaxTypes);
+  GBDP_REQUIRE(em && nlist && ext_coord && ext_type && ext_map && ext_nall && coord && atype &&
+                   avg && stdv && sel,
+               "prod_env_mat_a: null required pointer");
+  GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && (!em_deriv || ((uintptr_t)em_deriv & 15) == 0),
+               "prod_env_mat_a: em / em_deriv must be 16-byte aligned");
+  const int fp64 = sizeof(T) == 8;
+  EnvWs w = carve(*plan, workspace, fp64);
+  GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_env_mat_a: workspace %zu < %zu bytes", ws_bytes,
+               w.bytes);
+  SecInfo si;
+  si.ntypes = ntypes;
+  si.sec[0] = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    GBDP_REQUIRE(sel[t] >= 0, "prod_env_mat_a: negative sel");
+    si.sec[t + 1] = si.sec[t] + sel[t];
+  }
+  si.nnei = si.sec[ntypes];
+  GBDP_REQUIRE(si.nnei > 0, "prod_env_mat_a: sum(sel) must be positive");
+  const int nl = plan->nloc_total;
+  if (nl == 0) return GBDP_OK;
+  cudaMemsetAsync(w.status, 0, 256, stream);
+  cudaMemsetAsync(w.cell_count, 0, sizeof(int) * plan->ncell_total, stream);
+  cudaMemsetAsync(w.cell_fill, 0, sizeof(int) * plan->ncell_total, stream);
+  const int tb = 256;
+  k_localize<T><<<(nl + tb - 1) / tb, tb, 0, stream>>>(frames, plan->nframes, nl, coord, atype,
+                                                       ext_coord, ext_type, ext_map,
+                                                       w.atom_frame, w.atom_cell, w.cell_count);
+  k_cell_scan<<<plan->nframes, 1024, 0, stream>>>(frames, w.cell_count, w.cell_start,
+                                                  w.ext_start, w.ext_cnt, w.ghost_start,
+                                                  ext_nall, w.status);
+  k_cell_bucket<<<(nl + tb - 1) / tb, tb, 0, stream>>>(nl, frames, w.atom_frame, w.atom_cell,
+                                                       w.cell_start, w.cell_fill, w.bucket);
+  k_cell_rank<<<(nl + tb - 1) / tb, tb, 0, stream>>>(nl, frames, w.atom_frame, w.atom_cell,
+                                                     w.cell_start, w.cell_count, w.bucket,
+                                                     w.cell_atoms);
+  const int nec = plan->next_cell_total;
+  k_ghost_fill<T><<<(nec * 32 + tb - 1) / tb, tb, 0, stream>>>(
+      frames, plan->nframes, nec, w.cell_start, w.cell_count, w.cell_atoms, w.ext_start,
+      w.ghost_start, ext_coord, ext_type, ext_map,
+      static_cast<typename XsOf<T>::type*>(w.xs));
+  const int mc = plan->max_cand;
+  const size_t smem = (size_t)kEnvWarps * mc * 9 + (size_t)kEnvWarps * ((si.nnei + 3) & ~3) * 4;
+  GBDP_REQUIRE(smem <= 200 * 1024, "prod_env_mat_a: max_cand %d needs too much shared memory",
+               mc);
+  auto kern = k_nlist_env<T>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+  const float rc = plan->rcut;
+  kern<<<(nl + kEnvWarps - 1) / kEnvWarps, kEnvWarps * 32, smem, stream>>>(
+      nl, frames, w.atom_frame, w.atom_cell, w.ext_start, w.ext_cnt,
+      static_cast<const typename XsOf<T>::type*>(w.xs), ext_coord, ext_map, atype, avg, stdv, si,
+      rc * rc, (T)rcut_smth, (T)rc, mc, em, em_deriv, rij, nlist, nlist_ext, w.status);
+  GBDP_CHECK_LAUNCH("prod_env_mat_a");
+  return GBDP_OK;
+}
+
+// reference cell geometry (mirrors the oracle's cell_geom, which follows
+// source/lib/src/neighbor_list.cc:745-775 and SimulationRegion_Impl.h:364-372)
+void rec_box_d(double* r, const double* b) {
+  double v = b[0] * (b[4] * b[8] - b[7] * b[5]) - b[1] * (b[3] * b[8] - b[6] * b[5]) +
+             b[2] * (b[3] * b[7] - b[6] * b[4]);
+  double vi = 1. / std::fabs(v);
+  r[0] = (b[4] * b[8] - b[7] * b[5]) * vi;
+  r[4] = (b[0] * b[8] - b[6] * b[2]) * vi;
+  r[8] = (b[0] * b[4] - b[3] * b[1]) * vi;
+  r[1] = (-b[3] * b[8] + b[6] * b[5]) * vi;
+  r[2] = (b[3] * b[7] - b[6] * b[4]) * vi;
+  r[3] = (-b[1] * b[8] + b[7] * b[2]) * vi;
+  r[5] = (-b[0] * b[7] + b[6] * b[1]) * vi;
+  r[6] = (b[1] * b[5] - b[4] * b[2]) * vi;
+  r[7] = (-b[0] * b[5] + b[3] * b[2]) * vi;
+}
+void rec_box_f(float* r, const float* b) {
+  float v = b[0] * (b[4] * b[8] - b[7] * b[5]) - b[1] * (b[3] * b[8] - b[6] * b[5]) +
+            b[2] * (b[3] * b[7] - b[6] * b[4]);
+  float vi = 1.f / std::fabs(v);
+  r[0] = (b[4] * b[8] - b[7] * b[5]) * vi;
+  r[4] = (b[0] * b[8] - b[6] * b[2]) * vi;
+  r[8] = (b[0] * b[4] - b[3] * b[1]) * vi;
+  r[1] = (-b[3] * b[8] + b[6] * b[5]) * vi;
+  r[2] = (b[3] * b[7] - b[6] * b[4]) * vi;
+  r[3] = (-b[1] * b[8] + b[7] * b[2]) * vi;
+  r[5] = (-b[0] * b[7] + b[6] * b[1]) * vi;
+  r[6] = (b[1] * b[5] - b[4] * b[2]) * vi;
+  r[7] = (-b[0] * b[5] + b[3] * b[2]) * vi;
+}
+
+}  // namespace
+}  // namespace gbdp
+
+using namespace gbdp;
+
+extern "C" int gbdp_nbr_plan_make(gbdp_nbr_plan* plan, gbdp_nbr_frame* frames, int nframes,
+                                  const int* nloc, const double* boxes, float rcut,
+                                  int max_cand) {
+  GBDP_REQUIRE(plan && frames && nloc && boxes, "nbr_plan_make: null argument");
+  GBDP_REQUIRE(nframes >= 1, "nbr_plan_make: nframes must be >= 1");
+  GBDP_REQUIRE(rcut > 0.f, "nbr_plan_make: rcut must be positive");
+  long atom_off = 0, cell_off = 0, ecell_off = 0, ext_off = 0;
+  for (int f = 0; f < nframes; ++f) {
+    gbdp_nbr_frame& g = frames[f];
+    std::memset(&g, 0, sizeof(g));
+    const double* b = boxes + 9 * (size_t)f;
+    std::copy(b, b + 9, g.box);
+    for (int k = 0; k < 9; ++k) g.boxf[k] = (float)b[k];
+    double vol = std::fabs(b[0] * (b[4] * b[8] - b[7] * b[5]) - b[1] * (b[3] * b[8] - b[6] * b[5]) +
+                           b[2] * (b[3] * b[7] - b[6] * b[4]));
+    GBDP_REQUIRE(vol > 0, "nbr_plan_make: frame %d has a zero-volume box", f);
+    rec_box_d(g.rec, g.box);
+    rec_box_f(g.recf, g.boxf);
+    const int pa[3] = {3, 6, 0}, pb[3] = {6, 0, 3};
+    long mult = 1;
+    for (int d = 0; d < 3; ++d) {
+      const double* u = g.box + pa[d];
+      const double* v = g.box + pb[d];
+      double t0 = u[1] * v[2] - u[2] * v[1], t1 = u[2] * v[0] - u[0] * v[2],
+             t2 = u[0] * v[1] - u[1] * v[0];
+      double face = vol * (1. / std::sqrt(t0 * t0 + t1 * t1 + t2 * t2));
+      int nc = (int)(face / (double)rcut);
+      if (nc == 0) nc = 1;
+      double cs = face / nc;
+      g.ncell[d] = nc;
+      g.ngcell[d] = (int)((double)rcut / cs) + 1;
+      // every extended atom within rcut of a local atom lies within ngcell
+      // cells of it (cell >= rcut, or ngcell covers rcut / cell)
+      g.stencil[d] = g.ngcell[d];
+      // a local cell index l is imaged by every extended index in
+      // [-ngcell, nc + ngcell) congruent to it: at most ceil((nc+2ng)/nc)
+      mult *= (nc + 2 * g.ngcell[d] + nc - 1) / nc;
+    }
+    g.nloc = nloc[f];
+    GBDP_REQUIRE(g.nloc >= 0, "nbr_plan_make: negative nloc");
+    g.atom_off = (int)atom_off;
+    g.cell_off = (int)cell_off;
+    g.ext_cell_off = (int)ecell_off;
+    g.ext_off = (int)ext_off;
+    long cap = (long)g.nloc * mult;
+    GBDP_REQUIRE(cap < (1l << 24), "nbr_plan_make: frame %d needs %ld extended slots (max 2^24)",
+                 f, cap);
+    g.ext_cap = (int)cap;
+    atom_off += g.nloc;
+    cell_off += (long)g.ncell[0] * g.ncell[1] * g.ncell[2];
+    ecell_off += (long)(g.ncell[0] + 2 * g.ngcell[0]) * (g.ncell[1] + 2 * g.ngcell[1]) *
+                 (g.ncell[2] + 2 * g.ngcell[2]);
+    ext_off += cap;
+    GBDP_REQUIRE(ext_off < (1l << 31) && ecell_off < (1l << 31),
+                 "nbr_plan_make: batch too large for 32-bit offsets");
+  }
+  plan->nframes = nframes;
+  plan->nloc_total = (int)atom_off;
+  plan->ncell_total = (int)cell_off;
+  plan->next_cell_total = (int)ecell_off;
+  plan->ext_total = (int)ext_off;
+  plan->max_cand = max_cand > 0 ? max_cand : 512;
+  plan->rcut = rcut;
+  plan->pad0 = 0;
+  return GBDP_OK;
+}
+
+extern "C" size_t gbdp_env_workspace_bytes(const gbdp_nbr_plan* plan, int fp64) {
+  if (!plan) return 0;
+  return carve(*plan, nullptr, fp64).bytes;
+}
+
+extern "C" int gbdp_env_status(const void* workspace, gbdp_stream stream) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, workspace, sizeof(int), cudaMemcpyDeviceToHost,
+                                  (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "env_status");
+  return h;
+}
+
+extern "C" int gbdp_prod_env_mat_a_f32(float* em, float* em_deriv, float* rij, int* nlist,
+                                       int* nlist_ext, float* ext_coord, int* ext_type,
+                                       int* ext_map, int* ext_nall, const float* coord,
+                                       const int* atype, const float* avg, const float* std,
+                                       const gbdp_nbr_plan* plan,
+                                       const gbdp_nbr_frame* frames_dev, float rcut_smth,
+                                       const int* sel, int ntypes, void* workspace,
+                                       size_t workspace_bytes, gbdp_stream stream) {
+  return env_launch<float>(em, em_deriv, rij, nlist, nlist_ext, ext_coord, ext_type, ext_map,
+                           ext_nall, coord, atype, avg, std, plan, frames_dev, rcut_smth, sel,
+                           ntypes, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij, int* nlist,
+                                       int* nlist_ext, double* ext_coord, int* ext_type,
+                                       int* ext_map, int* ext_nall, const double* coord,
+                                       const int* atype, const double* avg, const double* std,
+                                       const gbdp_nbr_plan* plan,
+                                       const gbdp_nbr_frame* frames_dev, float rcut_smth,
+                                       const int* sel, int ntypes, void* workspace,
+                                       size_t workspace_bytes, gbdp_stream stream) {
+  return env_launch<double>(em, em_deriv, rij, nlist, nlist_ext, ext_coord, ext_type, ext_map,
+                            ext_nall, coord, atype, avg, std, plan, frames_dev, rcut_smth, sel,
+                            ntypes, workspace, workspace_bytes, (cudaStream_t)stream);
+}

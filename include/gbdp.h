@@ -1,0 +1,238 @@
+/*
+ * gbdp.h - C ABI of the GB300 (sm_103a) se_e2_a descriptor library
+ * (libgbdp.so).
+ *
+ * Plain pointers and sizes only.  Every device buffer (inputs, outputs and
+ * workspace) is allocated by the caller; the library never calls cudaMalloc,
+ * never synchronises the device and launches only on the stream it is given.
+ * Return value: GBDP_OK (0), a positive GBDP_STATUS_* for a capacity problem
+ * the caller can fix by retrying with more room, or a negative error code;
+ * gbdp_last_error() then describes it.  No C++ exception crosses this ABI.
+ *
+ * Layouts follow the reference operator contract (DeePMD-kit, OutisLi fork):
+ *   em          [nloc, nnei, 4]        (TF ProdEnvMatA "descrpt")
+ *   em_deriv    [nloc, nnei, 4, 3]     ("descrpt_deriv")
+ *   rij         [nloc, nnei, 3]
+ *   nlist       [nloc, nnei] int32, -1 = empty slot, per-type sections
+ *   table       [nspline, 6 * last_layer_size], coefficient-minor
+ * with nnei = sum(sel).  Reference paths are relative to the reference
+ * project root.
+ */
+#ifndef GBDP_H_
+#define GBDP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gbdp_stream; /* == cudaStream_t */
+
+#if defined(__GNUC__)
+#define GBDP_API __attribute__((visibility("default")))
+#else
+#define GBDP_API
+#endif
+
+enum {
+  GBDP_OK = 0,
+  GBDP_STATUS_CAND_OVERFLOW = 1, /* a centre had more candidates than max_cand */
+  GBDP_STATUS_EXT_OVERFLOW = 2,  /* more ghost atoms than the plan reserved  */
+  GBDP_STATUS_TIMEOUT = 3,       /* a bounded device-side wait gave up       */
+  GBDP_STATUS_BAD_INDEX = 4,     /* an input index was out of range          */
+  GBDP_ERR_INVALID = -1,
+  GBDP_ERR_CUDA = -2
+};
+
+/* Thread-local description of the last failure (empty string if none). */
+GBDP_API const char* gbdp_last_error(void);
+/* Library version, major * 10000 + minor * 100 + patch. */
+GBDP_API int gbdp_version(void);
+
+/* ------------------------------------------------------------------------
+ * Tabulated embedding + G^T.R contraction (compressed se_e2_a).
+ * Replaces deepmd::tabulate_fusion_se_a_gpu / _grad_gpu / _grad_grad_gpu
+ * (source/lib/include/tabulate.h:151-190; kernels
+ * source/lib/src/gpu/tabulate.cu:196-503) as bound by the torch op
+ * deepmd::tabulate_fusion_se_a (source/op/pt/tabulate_multi_device.cc:605-830,
+ * :1498-1552).  table_info is a HOST array of 6 values
+ * [lower, upper, max, stride0, stride1, check_freq], as the reference reads
+ * it on the host (tabulate.cu:997-999).  em_x is [nloc, nnei], em
+ * [nloc, nnei, 4], out / dy / dz_dy [nloc, 4, last_layer_size].
+ * is_sorted != 0 enables the reference's trailing-padding fold.
+ * ---------------------------------------------------------------------- */
+GBDP_API int gbdp_tabulate_fusion_se_a_f32(float* out, const float* table, const float* table_info,
+                                  const float* em_x, const float* em, int nloc, int nnei,
+                                  int last_layer_size, int is_sorted, gbdp_stream stream);
+GBDP_API int gbdp_tabulate_fusion_se_a_f64(double* out, const double* table, const double* table_info,
+                                  const double* em_x, const double* em, int nloc, int nnei,
+                                  int last_layer_size, int is_sorted, gbdp_stream stream);
+GBDP_API int gbdp_tabulate_fusion_se_a_grad_f32(float* dy_dem_x, float* dy_dem, const float* table,
+                                       const float* table_info, const float* em_x,
+                                       const float* em, const float* dy, int nloc, int nnei,
+                                       int last_layer_size, int is_sorted, gbdp_stream stream);
+GBDP_API int gbdp_tabulate_fusion_se_a_grad_f64(double* dy_dem_x, double* dy_dem, const double* table,
+                                       const double* table_info, const double* em_x,
+                                       const double* em, const double* dy, int nloc, int nnei,
+                                       int last_layer_size, int is_sorted, gbdp_stream stream);
+GBDP_API int gbdp_tabulate_fusion_se_a_grad_grad_f32(float* dz_dy, const float* table,
+                                            const float* table_info, const float* em_x,
+                                            const float* em, const float* dz_dy_dem_x,
+                                            const float* dz_dy_dem, int nloc, int nnei,
+                                            int last_layer_size, int is_sorted,
+                                            gbdp_stream stream);
+GBDP_API int gbdp_tabulate_fusion_se_a_grad_grad_f64(double* dz_dy, const double* table,
+                                            const double* table_info, const double* em_x,
+                                            const double* em, const double* dz_dy_dem_x,
+                                            const double* dz_dy_dem, int nloc, int nnei,
+                                            int last_layer_size, int is_sorted,
+                                            gbdp_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Neighbour plan for a packed batch of periodic frames.
+ *
+ * Frame f owns local atoms [atom_off, atom_off + nloc) of the packed
+ * coordinate arrays and extended-atom slots [ext_off, ext_off + ext_cap).
+ * Within a frame, extended atoms are numbered exactly as the reference's
+ * copy_coord orders them (source/lib/src/neighbor_list.cc:745-845): local
+ * atoms first, then the ghost images cell by cell.  The cell geometry is the
+ * reference's (ncell = floor(face distance / rcut), ngcell = int(rcut / cell)
+ * + 1).  gbdp_nbr_plan_make fills the plan and the frame table on the host;
+ * the caller copies the frame table (plan->nframes structs, plain bytes) to
+ * device memory and passes that copy to the device entry points.
+ * ---------------------------------------------------------------------- */
+typedef struct gbdp_nbr_frame {
+  double box[9];   /* rows are the cell vectors                          */
+  double rec[9];   /* reciprocal (fractional = rec * phys), double       */
+  float boxf[9];   /* the same in float, for float coordinates           */
+  float recf[9];
+  int ncell[3];    /* local cells per dimension                          */
+  int ngcell[3];   /* ghost cell layers per dimension                    */
+  int stencil[3];  /* neighbour-cell half width per dimension            */
+  int nloc;        /* local atoms                                        */
+  int atom_off;    /* first local atom in the packed arrays              */
+  int cell_off;    /* first local cell                                   */
+  int ext_cell_off;/* first extended cell                                */
+  int ext_off;     /* first extended-atom slot                           */
+  int ext_cap;     /* extended-atom slots reserved (upper bound of nall) */
+  int pad0;
+} gbdp_nbr_frame;
+
+typedef struct gbdp_nbr_plan {
+  int nframes;
+  int nloc_total;
+  int ncell_total;     /* local cells, all frames    */
+  int next_cell_total; /* extended cells, all frames */
+  int ext_total;       /* extended-atom slots        */
+  int max_cand;        /* candidates per centre kept on chip */
+  float rcut;
+  int pad0;
+} gbdp_nbr_plan;
+
+/* Fill plan and frames[nframes] from per-frame atom counts and HOST boxes
+ * (nframes x 9, row vectors).  max_cand <= 0 selects the default (512). */
+GBDP_API int gbdp_nbr_plan_make(gbdp_nbr_plan* plan, gbdp_nbr_frame* frames, int nframes,
+                       const int* nloc, const double* boxes, float rcut, int max_cand);
+
+/* Device workspace bytes for gbdp_prod_env_mat_a_* with this plan. */
+GBDP_API size_t gbdp_env_workspace_bytes(const gbdp_nbr_plan* plan, int fp64);
+
+/* ------------------------------------------------------------------------
+ * Environment matrix with the internal periodic neighbour build.
+ * Replaces deepmd::prod_env_mat_a_gpu (source/lib/include/prod_env_mat.h:47-65)
+ * together with the TF ProdEnvMatA op's internal-PBC mode
+ * (source/op/tf/prod_env_mat_multi_device.cc:11-28, :417-438 nei_mode 1:
+ * normalize_coord, copy_coord, build_nlist, format_nlist, env mat, map).
+ *
+ * Inputs (device, packed over frames): coord [nloc_total, 3], atype
+ * [nloc_total] (type < 0 atoms are never neighbours), avg / std
+ * [ntypes, nnei * 4].  sel is a HOST array of ntypes section sizes.
+ * Outputs (device): em, nlist (frame-local indices of LOCAL atoms, the TF
+ * op's mapped form), and optionally (NULL to skip) em_deriv, rij and
+ * nlist_ext (frame-local extended indices).  ext_coord [ext_total, 3],
+ * ext_type, ext_map [ext_total] receive the extended system (slots past a
+ * frame's nall are left untouched); ext_nall [nframes] its atom count.
+ * Neighbour order within a type section is (float r^2, extended index)
+ * ascending, bit-exact against format_nlist_cpu (source/lib/src/fmt_nlist.cc:
+ * 98-143).  A GBDP_STATUS_* code is also written to the first int of the
+ * workspace; read it with gbdp_env_status after the stream has run.
+ * ---------------------------------------------------------------------- */
+GBDP_API int gbdp_prod_env_mat_a_f32(float* em, float* em_deriv, float* rij, int* nlist, int* nlist_ext,
+                            float* ext_coord, int* ext_type, int* ext_map, int* ext_nall,
+                            const float* coord, const int* atype, const float* avg,
+                            const float* std, const gbdp_nbr_plan* plan,
+                            const gbdp_nbr_frame* frames_dev, float rcut_smth, const int* sel,
+                            int ntypes, void* workspace, size_t workspace_bytes,
+                            gbdp_stream stream);
+GBDP_API int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij, int* nlist,
+                            int* nlist_ext, double* ext_coord, int* ext_type, int* ext_map,
+                            int* ext_nall, const double* coord, const int* atype,
+                            const double* avg, const double* std, const gbdp_nbr_plan* plan,
+                            const gbdp_nbr_frame* frames_dev, float rcut_smth, const int* sel,
+                            int ntypes, void* workspace, size_t workspace_bytes,
+                            gbdp_stream stream);
+
+/* Synchronise `stream` and return the device status word of an env-mat
+ * workspace (GBDP_OK or a GBDP_STATUS_* code). */
+GBDP_API int gbdp_env_status(const void* workspace, gbdp_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Force and virial from the derivative of the energy wrt the env matrix.
+ * Replace deepmd::prod_force_a_gpu (source/lib/include/prod_force.h:72-80,
+ * kernels source/lib/src/gpu/prod_force.cu:4-131) and
+ * deepmd::prod_virial_a_gpu (source/lib/include/prod_virial.h:30-38,
+ * source/lib/src/gpu/prod_virial.cu:4-135), bound by the TF ops ProdForceSeA
+ * (source/op/tf/prod_force_multi_device.cc:6-14) and ProdVirialSeA
+ * (source/op/tf/prod_virial_multi_device.cc:5-15).
+ * net_deriv [nframes, nloc, nnei*4], env_deriv [nframes, nloc, nnei*4, 3],
+ * rij [nframes, nloc, nnei, 3], nlist [nframes, nloc, nnei] (indices in
+ * [0, nall)), force [nframes, nall, 3], virial [nframes, 9], atom_virial
+ * [nframes, nall, 9].  deterministic != 0 gathers through a reverse
+ * neighbour list (bitwise reproducible); 0 scatters with atomics.
+ * ---------------------------------------------------------------------- */
+GBDP_API size_t gbdp_prod_workspace_bytes(int nframes, int nloc, int nall, int nnei, int deterministic);
+GBDP_API int gbdp_prod_force_a_f32(float* force, const float* net_deriv, const float* env_deriv,
+                          const int* nlist, int nloc, int nall, int nnei, int nframes,
+                          int deterministic, void* workspace, size_t workspace_bytes,
+                          gbdp_stream stream);
+GBDP_API int gbdp_prod_force_a_f64(double* force, const double* net_deriv, const double* env_deriv,
+                          const int* nlist, int nloc, int nall, int nnei, int nframes,
+                          int deterministic, void* workspace, size_t workspace_bytes,
+                          gbdp_stream stream);
+GBDP_API int gbdp_prod_virial_a_f32(float* virial, float* atom_virial, const float* net_deriv,
+                           const float* env_deriv, const float* rij, const int* nlist,
+                           int nloc, int nall, int nnei, int nframes, int deterministic,
+                           void* workspace, size_t workspace_bytes, gbdp_stream stream);
+GBDP_API int gbdp_prod_virial_a_f64(double* virial, double* atom_virial, const double* net_deriv,
+                           const double* env_deriv, const double* rij, const int* nlist,
+                           int nloc, int nall, int nnei, int nframes, int deterministic,
+                           void* workspace, size_t workspace_bytes, gbdp_stream stream);
+
+/* Backward of the two ops wrt net_deriv (second order of the env-mat
+ * derivative).  Replace deepmd::prod_force_grad_a_gpu
+ * (source/lib/include/prod_force_grad.h, source/lib/src/gpu/
+ * prod_force_grad.cu:10-145) and deepmd::prod_virial_grad_a_gpu
+ * (source/lib/include/prod_virial_grad.h, source/lib/src/gpu/
+ * prod_virial_grad.cu:14-130).  grad [nframes, nloc, 3] (force) or
+ * [nframes, 9] (virial); grad_net [nframes, nloc, nnei*4].  For the force
+ * version, neighbour indices >= nloc are folded with j % nloc as the
+ * reference does (prod_force_grad.cc:54-57). */
+GBDP_API int gbdp_prod_force_grad_a_f32(float* grad_net, const float* grad, const float* env_deriv,
+                               const int* nlist, int nloc, int nnei, int nframes,
+                               gbdp_stream stream);
+GBDP_API int gbdp_prod_force_grad_a_f64(double* grad_net, const double* grad, const double* env_deriv,
+                               const int* nlist, int nloc, int nnei, int nframes,
+                               gbdp_stream stream);
+GBDP_API int gbdp_prod_virial_grad_a_f32(float* grad_net, const float* grad, const float* env_deriv,
+                                const float* rij, const int* nlist, int nloc, int nnei,
+                                int nframes, gbdp_stream stream);
+GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, const double* env_deriv,
+                                const double* rij, const int* nlist, int nloc, int nnei,
+                                int nframes, gbdp_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDP_H_ */

@@ -1,0 +1,94 @@
+"""The C-ABI library loads and exports every entry point include/gbdp.h
+declares; host-only planning matches the reference cell geometry.  CPU only
+(no compute call needs a GPU here)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "gbdp.h")).read()
+    return sorted(set(re.findall(r"GBDP_API\s+[\w\s\*]+?\b(gbdp_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(gb):
+    lib = gb._lib.load()
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    # the ctypes signature table covers exactly the header
+    assert sorted(gb._lib.declared_symbols()) == names
+
+
+def test_version_and_error_string(gb):
+    lib = gb._lib.load()
+    assert lib.gbdp_version() >= 100
+    assert isinstance(lib.gbdp_last_error(), bytes)
+
+
+def test_invalid_arguments_are_reported_not_raised(gb):
+    lib = gb._lib.load()
+    info = (ctypes.c_float * 6)(0, 1, 2, 0.1, 0.1, -1)
+    rc = lib.gbdp_tabulate_fusion_se_a_f32(None, None, info, None, None, 4, 4, 0, 1, None)
+    assert rc == gb._lib.GBDP_OK - 1
+    assert b"last_layer_size" in lib.gbdp_last_error()
+    # zero-sized work is a no-op that needs no device
+    rc = lib.gbdp_tabulate_fusion_se_a_f32(None, None, info, None, None, 0, 4, 8, 1, None)
+    assert rc == 0
+
+
+def _plan(gb, nloc, boxes, rcut=6.0):
+    L = gb._lib
+    plan = L.NbrPlan()
+    nf = len(nloc)
+    frames = (L.NbrFrame * nf)()
+    nl = np.asarray(nloc, np.int32)
+    bx = np.ascontiguousarray(np.asarray(boxes, np.float64).reshape(nf, 9))
+    rc = L.load().gbdp_nbr_plan_make(ctypes.byref(plan), frames, nf,
+                                     nl.ctypes.data_as(ctypes.c_void_p),
+                                     bx.ctypes.data_as(ctypes.c_void_p), ctypes.c_float(rcut), 0)
+    return rc, plan, frames
+
+
+def test_plan_geometry_and_ghost_bound(gb, oracle):
+    water = __import__("dpmd_public_gb300.water", fromlist=["x"])
+    cases = [(4, 12.42, 1), (2, 6.2, 3), (8, 24.84, 5), (16, 49.68, 9)]
+    frames_in = [water.water_frame(n, L, s) for n, L, s in cases]
+    rc, plan, frames = _plan(gb, [len(t) for _, t, _ in frames_in], [b for _, _, b in frames_in])
+    assert rc == 0
+    off = 0
+    for f, (c, t, b) in enumerate(frames_in):
+        fr = frames[f]
+        L = b[0]
+        nc = max(1, int(L / 6.0))
+        assert list(fr.ncell) == [nc] * 3
+        assert list(fr.ngcell) == [int(6.0 / (L / nc)) + 1] * 3
+        assert fr.atom_off == off
+        off += len(t)
+        ec, et, em = oracle.copy_coord(c, t, b, 6.0)
+        assert len(et) <= fr.ext_cap  # the reserved bound holds
+    assert plan.nloc_total == off
+    assert plan.ext_total == sum(frames[f].ext_cap for f in range(len(cases)))
+
+
+def test_plan_rejects_bad_input(gb):
+    rc, _, _ = _plan(gb, [10], np.zeros(9))
+    assert rc < 0
+    assert b"zero-volume" in gb._lib.load().gbdp_last_error()
+
+
+def test_workspace_sizes(gb):
+    L = gb._lib
+    rc, plan, frames = _plan(gb, [192], np.diag([12.42] * 3))
+    w32 = L.load().gbdp_env_workspace_bytes(ctypes.byref(plan), 0)
+    w64 = L.load().gbdp_env_workspace_bytes(ctypes.byref(plan), 1)
+    assert 0 < w32 < w64
+    assert L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 0) > 0
+    assert (L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 1)
+            > L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 0))

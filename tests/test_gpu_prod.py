@@ -1,0 +1,119 @@
+"""GPU parity of prod_force_se_a / prod_virial_se_a (atomic and deterministic
+scatter) and of their backward kernels, against the CPU oracle and the
+reference's golden vectors.  Deterministic mode must also be bitwise
+reproducible run to run."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _ops(gb):
+    gb.load_library()
+
+
+def _env(oracle, fx):
+    posi = np.array(fx["posi"])
+    atype = np.array(fx["atype"], np.int32)
+    sec = fx["sec_a"]
+    sel = [sec[i + 1] - sec[i] for i in range(len(sec) - 1)]
+    ec, et, emap = oracle.copy_coord(posi, atype, np.array(fx["box"]), fx["rc"])
+    nloc, nnei = len(atype), sum(sel)
+    em, emd, rij, nl = oracle.prod_env_mat_a_ext(ec, et, nloc, np.zeros((2, nnei * 4)),
+                                                 np.ones((2, nnei * 4)), fx["rc"], fx["rc_smth"], sel)
+    return nloc, len(et), nnei, emd, rij, nl
+
+
+@pytest.mark.parametrize("det", [False, True])
+def test_golden_force_virial(gb, oracle, golden_lib, det):
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    fx = golden_lib["TestProdForceA"]
+    nloc, nall, nnei, emd, rij, nl = _env(oracle, fx)
+    net = 10 - np.arange(nloc * nnei * 4) * 0.01
+    natoms = torch.tensor([nloc, nall, 2, 4], dtype=torch.int32)
+    T = lambda a: torch.tensor(np.tile(a, (2, 1)) if a.ndim == 1 else a, device=DEV)
+    f = ops.prod_force_se_a_impl(T(net), T(emd), T(nl.astype(np.int32)), natoms, nnei, 0, det)
+    exp = np.array(fx["expected_force"])
+    np.testing.assert_allclose(f.cpu().numpy(), np.tile(exp, (2, 1)), atol=1e-5)
+    fv = golden_lib["TestProdVirialA"]
+    v, av = ops.prod_virial_se_a_impl(T(net), T(emd), T(rij), T(nl.astype(np.int32)), natoms, nnei, 0, det)
+    np.testing.assert_allclose(v[0].cpu().numpy(), fv["expected_virial"], atol=1e-5)
+    np.testing.assert_allclose(av[0].cpu().numpy(), fv["expected_atom_virial"], atol=1e-5)
+
+
+def test_golden_grads(gb, oracle, golden_lib):
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    fx = golden_lib["TestProdForceGradA"]
+    nloc, nall, nnei, emd, rij, nl = _env(oracle, fx)
+    grad = 10 - np.arange(nloc * 3) * 0.1
+    T = lambda a: torch.tensor(a, device=DEV)
+    g = ops.prod_force_grad_impl(T(np.tile(grad, 2)), T(np.tile(emd, 2)), T(np.tile(nl, 2).astype(np.int32)),
+                                 nloc, nnei, 2)
+    np.testing.assert_allclose(g.cpu().numpy().reshape(-1), np.tile(fx["expected_grad_net"], 2), atol=1e-5)
+    fv = golden_lib["TestProdVirialGradA"]
+    gv = ops.prod_virial_grad_impl(T(10 - np.arange(9) * 1.0), T(emd), T(rij), T(nl.astype(np.int32)),
+                                   nloc, nnei, 1)
+    np.testing.assert_allclose(gv.cpu().numpy().reshape(-1), fv["expected_grad_net"], atol=1e-5)
+
+
+def _water_case(gb, oracle, dtype, n=4, L=12.42, seed=4):
+    water = __import__("dpmd_public_gb300.water", fromlist=["x"])
+    c, t, b = water.water_frame(n, L, seed)
+    sel = [46, 92]
+    nnei = sum(sel)
+    npd = np.float64 if dtype == torch.float64 else np.float32
+    avg = np.zeros((2, nnei * 4), npd)
+    std = np.ones((2, nnei * 4), npd)
+    em, emd, rij, nl = oracle.prod_env_mat_a_pbc(c.astype(npd), t, b.astype(npd), avg, std, 6.0, 0.5, sel)
+    rng = np.random.default_rng(seed)
+    net = rng.normal(0, 1, em.shape).astype(npd)
+    return len(t), nnei, net, emd, rij, nl
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("det", [False, True])
+def test_water_vs_oracle(gb, oracle, dtype, det):
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    nloc, nnei, net, emd, rij, nl = _water_case(gb, oracle, dtype)
+    natoms = torch.tensor([nloc, nloc, 0, 0], dtype=torch.int32)
+    T = lambda a: torch.tensor(a.reshape(1, -1), device=DEV)
+    f = ops.prod_force_se_a_impl(T(net), T(emd), T(nl), natoms, nnei, 0, det)
+    v, av = ops.prod_virial_se_a_impl(T(net), T(emd), T(rij), T(nl), natoms, nnei, 0, det)
+    fo = oracle.prod_force_a(net, emd, nl, nloc, nloc, nnei)
+    vo, avo = oracle.prod_virial_a(net, emd, rij, nl, nloc, nloc, nnei)
+    tol = dict(atol=1e-10, rtol=1e-10) if dtype == torch.float64 else dict(atol=2e-3, rtol=1e-4)
+    np.testing.assert_allclose(f.cpu().numpy(), fo, **tol)
+    np.testing.assert_allclose(av.cpu().numpy().reshape(-1), avo, **tol)
+    vtol = dict(atol=1e-9, rtol=1e-10) if dtype == torch.float64 else dict(atol=5e-2, rtol=1e-4)
+    np.testing.assert_allclose(v.cpu().numpy().reshape(-1), vo, **vtol)
+
+
+def test_deterministic_is_bitwise_reproducible(gb, oracle):
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    nloc, nnei, net, emd, rij, nl = _water_case(gb, oracle, torch.float32, n=8, L=24.84, seed=6)
+    natoms = torch.tensor([nloc, nloc, 0, 0], dtype=torch.int32)
+    T = lambda a: torch.tensor(a.reshape(1, -1), device=DEV)
+    runs = [ops.prod_force_se_a_impl(T(net), T(emd), T(nl), natoms, nnei, 0, True) for _ in range(3)]
+    vir = [ops.prod_virial_se_a_impl(T(net), T(emd), T(rij), T(nl), natoms, nnei, 0, True)[0] for _ in range(3)]
+    for a in runs[1:]:
+        assert torch.equal(a, runs[0])
+    for a in vir[1:]:
+        assert torch.equal(a, vir[0])
+
+
+def test_force_autograd_second_order(gb, oracle):
+    """torch.ops.deepmd.prod_force_se_a is differentiable wrt net_deriv
+    (prod_force_grad), as a force-loss training step needs."""
+    nloc, nnei, net, emd, rij, nl = _water_case(gb, oracle, torch.float64, n=2, L=6.2, seed=9)
+    natoms = torch.tensor([nloc, nloc, 0, 0], dtype=torch.int32)
+    netT = torch.tensor(net.reshape(1, -1), device=DEV, requires_grad=True)
+    f = torch.ops.deepmd.prod_force_se_a(netT, torch.tensor(emd.reshape(1, -1), device=DEV),
+                                         torch.tensor(nl.reshape(1, -1), device=DEV), natoms, nnei, 0)
+    w = torch.linspace(-1, 1, f.numel(), dtype=f.dtype, device=DEV).reshape(f.shape)
+    (f * w).sum().backward()
+    go = oracle.prod_force_grad_a(w.cpu().numpy().reshape(-1), emd, nl, nloc, nnei)
+    np.testing.assert_allclose(netT.grad.cpu().numpy().reshape(-1), go, atol=1e-10)

@@ -363,10 +363,13 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const T* em,
              const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,
              const T* stdv, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
-             float rcut_smth, float rcut, int nloc, int M, int A, cudaStream_t st) {
+             float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st) {
   TabSet<T> ts;
   int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side);
   if (rc) return rc;
+  GBDP_REQUIRE(force && vir_acc && nframes >= 1, "se_a descriptor bwd: null output / nframes");
+  cudaMemsetAsync(force, 0, sizeof(T) * 3 * (size_t)nloc, st);
+  cudaMemsetAsync(vir_acc, 0, sizeof(double) * 9 * (size_t)nframes, st);
   GBDP_REQUIRE(M >= 1 && M <= 128, "se_a descriptor: neuron[-1] %d not in [1,128]", M);
   GBDP_REQUIRE(A == 16, "se_a descriptor: axis_neuron %d (this build supports 16)", A);
   if (nloc == 0) return GBDP_OK;
@@ -416,12 +419,12 @@ using namespace gbdp;
       const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,          \
       const T* std, const int* atom_frame, const int* frame_atom_off,                          \
       const int* frame_ext_off, const T* const* tables, const T* table_infos, int ntypes,      \
-      const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,                \
+      const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
     return desc_bwd<T>(force, virial_acc, X, dE_dD, em, nlist_ext, ext_coord, ext_map, atype,  \
                        std, atom_frame, frame_atom_off, frame_ext_off, tables, table_infos,    \
-                       ntypes, sel, type_one_side, rcut_smth, rcut, nloc, last_layer_size,     \
-                       axis_neuron, (cudaStream_t)stream);                                     \
+                       ntypes, sel, type_one_side, rcut_smth, rcut, nloc, nframes,             \
+                       last_layer_size, axis_neuron, (cudaStream_t)stream);                    \
   }
 
 GBDP_FUSED_ENTRY(float, f32)

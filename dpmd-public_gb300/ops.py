@@ -164,7 +164,13 @@ class NeighborPlan:
     def __init__(self, nloc_per_frame, boxes, rcut: float, device, dtype=torch.float32,
                  max_cand: int = 0):
         nl = np.ascontiguousarray(np.asarray(nloc_per_frame, dtype=np.int32).reshape(-1))
-        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(len(nl), 9))
+        bx = np.asarray(boxes, dtype=np.float64).reshape(len(nl), 9)
+        if dtype == torch.float32:
+            # float coordinates come with a float box: the reference builds
+            # its cell grid and ghost shifts from that box converted to
+            # double (source/lib/src/coord.cc:42-47)
+            bx = bx.astype(np.float32).astype(np.float64)
+        bx = np.ascontiguousarray(bx)
         self.nframes = len(nl)
         self.nloc = nl
         self.boxes = bx

@@ -1,0 +1,294 @@
+"""se_e2_a energy / force / virial on GB300, three forms over one model:
+
+* ``fused``      the chosen form: periodic neighbour build + env matrix
+                 (libgbdp), fused tabulated descriptor forward (libgbdp),
+                 per-type fitting nets (cuBLAS GEMMs, forward and input
+                 gradient), fused descriptor backward with the force / virial
+                 scatter (libgbdp).  Packed ragged batches, static buffers,
+                 capturable in a CUDA graph.
+* ``ops``        the compressed model through the reference's operator
+                 contract: prod_env_mat_a -> torch.ops.deepmd.
+                 tabulate_fusion_se_a per section -> fitting -> autograd to
+                 dE/d(env) -> prod_force_se_a / prod_virial_se_a
+                 (the sequence of deepmd/tf/descriptor/se_a.py:652-765).
+* ``plain``      the uncompressed model: as ``ops`` but the embedding nets
+                 run as matmuls (deepmd/pt/model/descriptor/se_a.py:823-845).
+
+Energies and virials are reduced per frame in float64.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import model as mdl
+from .ops import EnvMatResult, NeighborPlan, env_mat_packed, prod_force_se_a_impl, prod_virial_se_a_impl
+
+_P = ctypes.c_void_p
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class SeAModel:
+    def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
+                 device, dtype=torch.float32, tables=None, table_infos=None):
+        self.cfg = cfg
+        self.device = torch.device(device)
+        self.dtype = dtype
+        T = lambda a: torch.tensor(np.asarray(a), dtype=dtype, device=self.device)
+        self.emb = [[(T(l["w"]), T(l["b"]), l["skip"]) for l in net] for net in params["emb"]]
+        self.fit = []
+        for f in params["fit"]:
+            hidden = [(T(l["w"]), T(l["b"]), None if l["idt"] is None else T(l["idt"]), l["skip"])
+                      for l in f["hidden"]]
+            self.fit.append((hidden, T(f["final"]["w"]), T(f["final"]["b"])))
+        self.bias_atom_e = T(params["bias_atom_e"])
+        self.davg = T(davg).contiguous()
+        self.dstd = T(dstd).contiguous()
+        self.tables = None
+        if tables is not None:
+            self.tables = [T(t).contiguous() for t in tables]
+            self.table_infos = np.asarray(table_infos, np.float64)
+            self.table_info_t = [torch.tensor(i, dtype=dtype) for i in self.table_infos]  # CPU
+            ct = ctypes.c_double if dtype == torch.float64 else ctypes.c_float
+            self._tab_ptrs = (_P * len(self.tables))(*[t.data_ptr() for t in self.tables])
+            flat = self.table_infos.reshape(-1)
+            self._tab_infos = (ct * len(flat))(*flat.tolist())
+        self._sel_c = (ctypes.c_int * cfg.ntypes)(*[int(s) for s in cfg.sel])
+        self._sfx = L.sfx(dtype)
+        self._lib = L.load()
+
+    # ------------------------------------------------------------- batches --
+    def batch(self, atype_per_frame, boxes, max_cand: int = 0) -> "Batch":
+        return Batch(self, atype_per_frame, boxes, max_cand)
+
+    # ------------------------------------------------------------ fitting --
+    def fitting_fwd_bwd(self, t: int, D: torch.Tensor):
+        """Energy of type-t atoms and dE/dD (hidden tanh layers with idt /
+        skip where present, linear output; deepmd/pt/model/task/fitting.py
+        with deepmd/dpmodel/utils/network.py layer semantics)."""
+        hidden, wf, bf = self.fit[t]
+        h = D
+        cache = []
+        for w, b, idt, skip in hidden:
+            tt = torch.tanh(torch.addmm(b, h, w))
+            out = tt * idt if idt is not None else tt
+            if skip == "same":
+                out = out + h
+            cache.append((tt, idt, skip, w))
+            h = out
+        e = torch.addmm(bf, h, wf)[:, 0] + self.bias_atom_e[t]
+        g = wf[:, 0].expand(h.shape[0], -1)
+        for tt, idt, skip, w in reversed(cache):
+            gt = g * idt if idt is not None else g
+            gz = gt * (1 - tt * tt)
+            gin = torch.mm(gz, w.t())
+            if skip == "same":
+                gin = gin + g
+            g = gin
+        return e, g
+
+    def fitting_energy(self, t: int, D: torch.Tensor):
+        hidden, wf, bf = self.fit[t]
+        h = D
+        for w, b, idt, skip in hidden:
+            tt = torch.tanh(torch.addmm(b, h, w))
+            out = tt * idt if idt is not None else tt
+            if skip == "same":
+                out = out + h
+            h = out
+        return torch.addmm(bf, h, wf)[:, 0] + self.bias_atom_e[t]
+
+    # ------------------------------------------------------- chosen form --
+    def step_fused(self, b: "Batch", coord: torch.Tensor):
+        """E [nframes] f64, F [nloc_total, 3], virial [nframes, 9] f64."""
+        cfg = self.cfg
+        if self.tables is None:
+            raise RuntimeError("the fused form needs the compression tables")
+        M, A = cfg.neuron[-1], cfg.axis_neuron
+        n = b.nloc
+        env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth, list(cfg.sel),
+                       check_status=False, out=b.env)
+        lib = self._lib
+        L.check(getattr(lib, f"gbdp_se_a_descriptor_fwd_{self._sfx}")(
+            _ptr(b.X), _ptr(b.D), _ptr(b.env.em), _ptr(b.atype), self._tab_ptrs, self._tab_infos,
+            cfg.ntypes, self._sel_c, int(cfg.type_one_side), n, M, A, _stream()),
+            "se_a_descriptor_fwd")
+        for t in range(cfg.ntypes):
+            idx = b.type_idx[t]
+            if idx.numel() == 0:
+                continue
+            e, g = self.fitting_fwd_bwd(t, b.D.index_select(0, idx))
+            b.ae.index_copy_(0, idx, e)
+            b.dD.index_copy_(0, idx, g)
+        L.check(getattr(lib, f"gbdp_se_a_descriptor_bwd_{self._sfx}")(
+            _ptr(b.force), _ptr(b.vir), _ptr(b.X), _ptr(b.dD), _ptr(b.env.em), _ptr(b.env.nlist_ext),
+            _ptr(b.env.ext_coord), _ptr(b.env.ext_map), _ptr(b.atype), _ptr(self.dstd),
+            _ptr(b.atom_frame), _ptr(b.frame_aoff), _ptr(b.frame_eoff), self._tab_ptrs,
+            self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side),
+            ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), n, b.nframes, M, A,
+            _stream()), "se_a_descriptor_bwd")
+        b.energy.zero_()
+        b.energy.index_add_(0, b.frame_of_atom, b.ae.to(torch.float64))
+        return b.energy, b.force, b.vir
+
+    # --------------------------------------------- operator-contract forms --
+    def _descriptor_from_em(self, em: torch.Tensor, atype: torch.Tensor, compressed: bool):
+        cfg = self.cfg
+        n = em.shape[0]
+        sec = cfg.sec
+        M, A = cfg.neuron[-1], cfg.axis_neuron
+        X = torch.zeros((n, 4, M), dtype=self.dtype, device=self.device)
+        for tj in range(cfg.ntypes):
+            centres = [None] if cfg.type_one_side else list(range(cfg.ntypes))
+            for ti in centres:
+                k = tj if cfg.type_one_side else tj * cfg.ntypes + ti
+                rows = None if ti is None else torch.nonzero(atype == ti).reshape(-1)
+                rr = em[:, sec[tj]:sec[tj + 1], :] if rows is None else em[rows, sec[tj]:sec[tj + 1], :]
+                if rr.shape[0] == 0 or rr.shape[1] == 0:
+                    continue
+                ss = rr[:, :, :1]
+                if compressed:
+                    gr = torch.ops.deepmd.tabulate_fusion_se_a(
+                        self.tables[k], self.table_info_t[k], ss.reshape(-1, 1).contiguous(),
+                        rr.contiguous(), M)[0]
+                else:
+                    gg = ss
+                    for w, b_, skip in self.emb[k]:
+                        y = torch.tanh(torch.matmul(gg, w) + b_)
+                        if skip == "same":
+                            y = y + gg
+                        elif skip == "double":
+                            y = y + torch.cat([gg, gg], -1)
+                        gg = y
+                    gr = torch.matmul(rr.permute(0, 2, 1), gg)
+                X = X + gr if rows is None else X.index_add(0, rows, gr)
+        X = X / cfg.nnei
+        return torch.matmul(X.permute(0, 2, 1), X[:, :, :A]).reshape(n, M * A)
+
+    def step_ops(self, b: "Batch", coord: torch.Tensor, compressed: bool = True,
+                 deterministic: bool = False):
+        """The drop-in sequence through the operator contract, frame by frame
+        of the batch (the reference processes one frame at a time)."""
+        cfg = self.cfg
+        nnei = cfg.nnei
+        env = env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth,
+                             list(cfg.sel), need_deriv=True, need_rij=True, check_status=False)
+        em = env.em.detach().requires_grad_(True)
+        D = self._descriptor_from_em(em, b.atype, compressed)
+        E_atom = torch.zeros(b.nloc, dtype=self.dtype, device=self.device)
+        for t in range(cfg.ntypes):
+            idx = b.type_idx[t]
+            if idx.numel():
+                E_atom = E_atom.index_add(0, idx, self.fitting_energy(t, D.index_select(0, idx)))
+        net = torch.autograd.grad(E_atom.sum(), em)[0]
+        forces, virs = [], []
+        for f in range(b.nframes):
+            a0, a1 = int(b.plan.atom_off[f]), int(b.plan.atom_off[f]) + int(b.plan.nloc[f])
+            nl = int(b.plan.nloc[f])
+            natoms = torch.tensor([nl, nl] + [0] * cfg.ntypes, dtype=torch.int32)
+            nd = net[a0:a1].reshape(1, -1)
+            ed = env.em_deriv[a0:a1].reshape(1, -1)
+            nlst = env.nlist[a0:a1].reshape(1, -1)
+            forces.append(prod_force_se_a_impl(nd, ed, nlst, natoms, nnei, 0, deterministic).reshape(nl, 3))
+            v, _ = prod_virial_se_a_impl(nd, ed, env.rij[a0:a1].reshape(1, -1), nlst, natoms, nnei, 0,
+                                         deterministic)
+            virs.append(v.reshape(9))
+        E = torch.zeros(b.nframes, dtype=torch.float64, device=self.device)
+        E.index_add_(0, b.frame_of_atom, E_atom.detach().to(torch.float64))
+        return E, torch.cat(forces), torch.stack(virs).to(torch.float64)
+
+
+class Batch:
+    """Static per-batch state: the neighbour plan, type groups and every
+    buffer the fused step writes (fixed addresses, so the step can be
+    captured in a CUDA graph)."""
+
+    def __init__(self, model: SeAModel, atype_per_frame, boxes, max_cand: int = 0):
+        cfg = model.cfg
+        dev = model.device
+        dt = model.dtype
+        at = [np.asarray(a, np.int32).reshape(-1) for a in atype_per_frame]
+        self.nframes = len(at)
+        self.plan = NeighborPlan([len(a) for a in at], np.asarray(boxes, np.float64).reshape(-1, 9),
+                                 cfg.rcut, dev, dt, max_cand=max_cand)
+        self.nloc = int(self.plan.nloc_total)
+        flat = np.concatenate(at)
+        self.atype = torch.tensor(flat, dtype=torch.int32, device=dev)
+        fo = np.repeat(np.arange(self.nframes), [len(a) for a in at])
+        self.frame_of_atom = torch.tensor(fo, dtype=torch.int64, device=dev)
+        self.atom_frame = torch.tensor(fo, dtype=torch.int32, device=dev)
+        self.frame_aoff = torch.tensor(self.plan.atom_off, dtype=torch.int32, device=dev)
+        self.frame_eoff = torch.tensor(self.plan.ext_off, dtype=torch.int32, device=dev)
+        self.type_idx = [torch.tensor(np.nonzero(flat == t)[0], dtype=torch.int64, device=dev)
+                         for t in range(cfg.ntypes)]
+        n = self.nloc
+        nnei = cfg.nnei
+        M, A = cfg.neuron[-1], cfg.axis_neuron
+        e = EnvMatResult()
+        e.em = torch.empty((n, nnei, 4), dtype=dt, device=dev)
+        e.em_deriv = None
+        e.rij = None
+        e.nlist = torch.empty((n, nnei), dtype=torch.int32, device=dev)
+        e.nlist_ext = torch.empty((n, nnei), dtype=torch.int32, device=dev)
+        e.ext_coord = torch.empty((self.plan.ext_total, 3), dtype=dt, device=dev)
+        e.ext_type = torch.empty((self.plan.ext_total,), dtype=torch.int32, device=dev)
+        e.ext_map = torch.empty((self.plan.ext_total,), dtype=torch.int32, device=dev)
+        e.ext_nall = torch.empty((self.nframes,), dtype=torch.int32, device=dev)
+        self.env = e
+        self.X = torch.empty((n, 4, M), dtype=dt, device=dev)
+        self.D = torch.empty((n, M * A), dtype=dt, device=dev)
+        self.dD = torch.empty((n, M * A), dtype=dt, device=dev)
+        self.ae = torch.empty((n,), dtype=dt, device=dev)
+        self.force = torch.empty((n, 3), dtype=dt, device=dev)
+        self.vir = torch.empty((self.nframes, 9), dtype=torch.float64, device=dev)
+        self.energy = torch.empty((self.nframes,), dtype=torch.float64, device=dev)
+
+    def status(self) -> int:
+        """Device status word of the last neighbour build (0 = ok)."""
+        return L.load().gbdp_env_status(_ptr(self.plan.workspace), _stream())
+
+
+def build_model(cfg: mdl.SeAConfig, seed: int, stat_frames, device, dtype=torch.float32,
+                compressed: bool = True):
+    """Seeded parameters, davg/dstd from ``stat_frames`` (list of (coord,
+    atype, box)) computed with the GPU env matrix, the minimum neighbour
+    distance over them, and the tables."""
+    params = mdl.init_params(cfg, seed)
+    dev = torch.device(device)
+    nn = cfg.nnei
+    zeros = torch.zeros((cfg.ntypes, nn * 4), dtype=torch.float64, device=dev)
+    ones = torch.ones((cfg.ntypes, nn * 4), dtype=torch.float64, device=dev)
+    ems, ats = [], []
+    mind = np.inf
+    for c, t, b in stat_frames:
+        plan = NeighborPlan([len(t)], np.asarray(b).reshape(1, 9), cfg.rcut, dev, torch.float64)
+        r = env_mat_packed(plan, torch.tensor(c, dtype=torch.float64, device=dev),
+                           torch.tensor(t, dtype=torch.int32, device=dev), zeros, ones,
+                           cfg.rcut_smth, list(cfg.sel))
+        ems.append(r.em.cpu().numpy())
+        ats.append(np.asarray(t))
+        d = torch.linalg.norm(r.rij.reshape(-1, 3), dim=1)
+        d = d[r.nlist.reshape(-1) >= 0]
+        if d.numel():
+            mind = min(mind, float(d.min()))
+    davg, dstd = mdl.stats_from_env(ems, ats, cfg)
+    tables = infos = None
+    if compressed:
+        tables, infos = mdl.build_tables(params, davg, dstd, mind, cfg)
+    model = SeAModel(cfg, params, davg, dstd, dev, dtype, tables, infos)
+    model.params_np = params
+    model.min_nbor_dist = mind
+    model.tables_np = tables
+    model.infos_np = infos
+    return model

@@ -101,7 +101,10 @@ GBDP_API int gbdp_tabulate_fusion_se_a_grad_grad_f64(double* dz_dy, const double
  * reference's (ncell = floor(face distance / rcut), ngcell = int(rcut / cell)
  * + 1).  gbdp_nbr_plan_make fills the plan and the frame table on the host;
  * the caller copies the frame table (plan->nframes structs, plain bytes) to
- * device memory and passes that copy to the device entry points.
+ * device memory and passes that copy to the device entry points.  For float
+ * coordinates pass the float box values (exactly widened to double): the
+ * reference builds the cell grid and ghost shifts from the float box
+ * (source/lib/src/coord.cc:42-47).
  * ---------------------------------------------------------------------- */
 typedef struct gbdp_nbr_frame {
   double box[9];   /* rows are the cell vectors                          */
@@ -231,6 +234,49 @@ GBDP_API int gbdp_prod_virial_grad_a_f32(float* grad_net, const float* grad, con
 GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, const double* env_deriv,
                                 const double* rij, const int* nlist, int nloc, int nnei,
                                 int nframes, gbdp_stream stream);
+
+
+/* ------------------------------------------------------------------------
+ * Fused compressed se_e2_a descriptor (the batched "chosen form").
+ * Forward: X [nloc, 4, M] = sum over sections of the tabulated embedding
+ * contracted with the env rows, / nnei; D [nloc, M * axis_neuron] =
+ * X^T X[:, :axis_neuron] (DescrptBlockSeA.forward with compression,
+ * deepmd/pt/model/descriptor/se_a.py:786-866, tables as bound through
+ * deepmd::tabulate_fusion_se_a).  tables: HOST array of device table
+ * pointers, one per embedding net (ntypes nets if type_one_side, else
+ * ntypes^2 indexed tj * ntypes + ti); table_infos: HOST [n_tables * 6];
+ * sel: HOST [ntypes].  em comes from gbdp_prod_env_mat_a_*.
+ * Backward: from dE/dD, force [nloc, 3] (zeroed here, local indices, packed
+ * frames) and virial_acc [nframes, 9] (double, zeroed here) get the
+ * contributions of every real neighbour, the env-matrix derivative being
+ * recomputed from ext_coord (prod_force.cc:22-72, prod_virial.cc:22-68
+ * semantics).  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
+ * are device arrays describing the packed batch (see gbdp_nbr_frame).
+ * ---------------------------------------------------------------------- */
+GBDP_API int gbdp_se_a_descriptor_fwd_f32(float* X, float* D, const float* em, const int* atype,
+                                          const float* const* tables, const float* table_infos,
+                                          int ntypes, const int* sel, int type_one_side,
+                                          int nloc, int last_layer_size, int axis_neuron,
+                                          gbdp_stream stream);
+GBDP_API int gbdp_se_a_descriptor_fwd_f64(double* X, double* D, const double* em,
+                                          const int* atype, const double* const* tables,
+                                          const double* table_infos, int ntypes, const int* sel,
+                                          int type_one_side, int nloc, int last_layer_size,
+                                          int axis_neuron, gbdp_stream stream);
+GBDP_API int gbdp_se_a_descriptor_bwd_f32(
+    float* force, double* virial_acc, const float* X, const float* dE_dD, const float* em,
+    const int* nlist_ext, const float* ext_coord, const int* ext_map, const int* atype,
+    const float* std, const int* atom_frame, const int* frame_atom_off, const int* frame_ext_off,
+    const float* const* tables, const float* table_infos, int ntypes, const int* sel,
+    int type_one_side, float rcut_smth, float rcut, int nloc, int nframes, int last_layer_size,
+    int axis_neuron, gbdp_stream stream);
+GBDP_API int gbdp_se_a_descriptor_bwd_f64(
+    double* force, double* virial_acc, const double* X, const double* dE_dD, const double* em,
+    const int* nlist_ext, const double* ext_coord, const int* ext_map, const int* atype,
+    const double* std, const int* atom_frame, const int* frame_atom_off,
+    const int* frame_ext_off, const double* const* tables, const double* table_infos,
+    int ntypes, const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,
+    int nframes, int last_layer_size, int axis_neuron, gbdp_stream stream);
 
 #ifdef __cplusplus
 }

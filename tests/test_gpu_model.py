@@ -1,0 +1,116 @@
+"""End-to-end energy / force / virial of the three GPU forms against the FP64
+CPU composite (oracle/composite.py, the reference's op sequence).
+
+Stated tolerances (the spec bar is a force error <= 1e-5 eV/A vs FP64):
+  fp64 GPU: |dF| <= 1e-9 eV/A, |dE| / natoms <= 1e-10 eV, |dV| <= 1e-8 eV
+  fp32 GPU: |dF| <= 1e-5 eV/A, |dE| / natoms <= 1e-6 eV, |dV| <= 1e-3 eV
+"""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module")
+def mods(gb):
+    gb.load_library()
+    import importlib
+
+    return (importlib.import_module("dpmd_public_gb300.se_a"),
+            importlib.import_module("dpmd_public_gb300.model"),
+            importlib.import_module("dpmd_public_gb300.water"))
+
+
+@pytest.fixture(scope="module")
+def built(mods):
+    se_a, mdl, water = mods
+    cfg = mdl.SeAConfig()
+    stat = [water.water_frame(4, 12.42, 1000 + s) for s in range(4)]
+    m64 = se_a.build_model(cfg, 7, stat, DEV, torch.float64)
+    m32 = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), DEV,
+                        torch.float32, m64.tables_np, m64.infos_np)
+    return cfg, m64, m32
+
+
+TOL = {torch.float64: (1e-9, 1e-10, 1e-8), torch.float32: (1e-5, 1e-6, 1e-3)}
+
+
+def _ref(composite, cfg, m, frame, compressed=True):
+    c, t, b = frame
+    return composite.energy_force_virial(cfg, m.params_np, m.davg.cpu().numpy(), m.dstd.cpu().numpy(),
+                                         c, t, b, m.tables_np if compressed else None,
+                                         m.infos_np if compressed else None)
+
+
+def _check(E, F, V, ref, natoms, dtype):
+    ft, et, vt = TOL[dtype]
+    Er, Fr, Vr, _ = ref
+    assert abs(float(E) - Er) / natoms <= et, (float(E), Er)
+    assert np.abs(F - Fr).max() <= ft, np.abs(F - Fr).max()
+    assert np.abs(V - Vr).max() <= vt, np.abs(V - Vr).max()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("form", ["fused", "ops", "plain"])
+def test_forms_vs_fp64_composite(mods, built, dtype, form):
+    import composite
+
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    m = m64 if dtype == torch.float64 else m32
+    frame = water.water_frame(4, 12.42, 5)
+    b = m.batch([frame[1]], frame[2][None])
+    coord = torch.tensor(frame[0], dtype=dtype, device=DEV)
+    if form == "fused":
+        E, F, V = m.step_fused(b, coord)
+        assert b.status() == 0
+    else:
+        E, F, V = m.step_ops(b, coord, compressed=(form == "ops"))
+    ref = _ref(composite, cfg, m64, frame, compressed=(form != "plain"))
+    _check(E[0].item(), F.detach().cpu().numpy().astype(np.float64), V[0].cpu().numpy(), ref,
+           len(frame[1]), dtype)
+
+
+def test_fused_ragged_batch(mods, built):
+    import composite
+
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    frames = water.ragged_frames(5, seed=11, lo=8, hi=120)
+    b = m32.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    coord = torch.tensor(np.concatenate([f[0] for f in frames]), dtype=torch.float32, device=DEV)
+    E, F, V = m32.step_fused(b, coord)
+    Fn = F.cpu().numpy().astype(np.float64)
+    off = 0
+    for k, fr in enumerate(frames):
+        n = len(fr[1])
+        _check(E[k].item(), Fn[off:off + n], V[k].cpu().numpy(), _ref(composite, cfg, m64, fr), n,
+               torch.float32)
+        off += n
+
+
+def test_fused_graph_replay_matches_eager(mods, built):
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    frame = water.water_frame(4, 12.42, 9)
+    b = m32.batch([frame[1]], frame[2][None])
+    coord = torch.tensor(frame[0], dtype=torch.float32, device=DEV)
+    E0, F0, V0 = (x.clone() for x in m32.step_fused(b, coord))
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(2):
+            m32.step_fused(b, coord)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = m32.step_fused(b, coord)
+    coord.add_(0.0)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.allclose(out[0], E0, rtol=1e-6, atol=1e-6)
+    assert torch.allclose(out[1], F0, rtol=1e-4, atol=1e-6)
+    assert b.status() == 0

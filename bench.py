@@ -1,0 +1,439 @@
+#!/usr/bin/env python
+"""Benchmark: MD atom-steps/s of compressed se_e2_a on GB300.
+
+Workload (one "step" = one energy + force + virial evaluation with the
+neighbour list rebuilt): 4096 H2O (12,288 atoms) in a 49.68 A periodic box,
+the 16^3 lattice of the seeded water generator, compressed se_e2_a in FP32
+(rcut 6, rcut_smth 0.5, sel [46, 92], embedding [25, 50, 100] tabulated at
+stride 0.01 / 0.1, extrapolate 5, axis 16, fitting [240, 240, 240]), seeded
+random weights, davg/dstd from 16 seeded 192-atom frames.
+
+  value   chosen form (fused kernels, CUDA graph), inputs resident in HBM
+  e2e     same step through the public API with pinned host coordinates
+          copied in and energy / force / virial copied out every step
+  plain   the uncompressed drop-in (embedding nets as matmuls), eager
+Errors are stated against the FP64 CPU composite of the reference's op
+sequence on the same frame.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "MD atom-steps/s on 1 GB300, chosen vs plain form at stated force error vs FP64"
+WORKLOAD = ("4096 H2O (12288 atoms), 49.68 A PBC box, compressed se_e2_a FP32, "
+            "nlist rebuilt every step, energy+force+virial")
+N_SIDE, BOX, SEED = 16, 49.68, 20261203
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _frame():
+    from __graft_entry__ import load_package
+    import importlib
+
+    load_package()
+    water = importlib.import_module("dpmd_public_gb300.water")
+    return water.water_frame(N_SIDE, BOX, SEED)
+
+
+def _stat_frames():
+    import importlib
+
+    water = importlib.import_module("dpmd_public_gb300.water")
+    return [water.water_frame(4, 12.42, 5000 + s) for s in range(16)]
+
+
+# ---------------------------------------------------------------- clocks --
+class Clocks:
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.index = index
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------- CPU baseline --
+def cpu_baseline(frame, model_np, steps: int = 2, dtype=np.float32):
+    """The reference's CPU op sequence (oracle composite: env mat with the
+    brute-force build, tabulate, BLAS fitting, tabulate grad, force, virial)
+    on the full frame, timed on this host's cores."""
+    import composite
+    import oracle as O
+
+    cfg, params, davg, dstd, tabs, infos = model_np
+    c, t, b = frame
+    composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype)  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype)
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": len(t) / dt, "unit": "atom-steps/s", "cores": O.num_threads(),
+            "kind": "port", "s_per_step": dt,
+            "sample": f"full 12288-atom frame, {steps} steps after 1 warm-up, FP32, "
+                      f"oracle composite of the reference's CPU op sequence"}
+
+
+def reference_arm(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import oracle as O
+    from __graft_entry__ import load_package
+    import importlib
+
+    load_package()
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    cfg = mdl.SeAConfig()
+    params = mdl.init_params(cfg, SEED)
+    frame = _frame()
+    ems, ats, mind = [], [], np.inf
+    for c, t, b in _stat_frames():
+        em, emd, rij, nl = O.prod_env_mat_a_pbc(c, t, b, np.zeros((2, cfg.nnei * 4)),
+                                                np.ones((2, cfg.nnei * 4)), cfg.rcut, cfg.rcut_smth,
+                                                list(cfg.sel))
+        ems.append(em)
+        ats.append(t)
+        r = np.linalg.norm(rij.reshape(-1, 3), axis=1)
+        mind = min(mind, r[nl >= 0].min())
+    davg, dstd = mdl.stats_from_env(ems, ats, cfg)
+    tabs, infos = mdl.build_tables(params, davg, dstd, mind, cfg)
+    steps = max(1, min(args.steps, 3))
+    cb = cpu_baseline(frame, (cfg, params, davg, dstd, tabs, infos), steps=steps)
+    line = {"metric": METRIC, "value": cb["value"], "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": 1, "ms_per_step": cb["s_per_step"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "atoms": len(frame[1]), "form": "reference CPU op sequence"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ main --
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    torch.backends.cudnn.allow_tf32 = False
+
+    from __graft_entry__ import load_package
+    import importlib
+
+    pkg = load_package()
+    pkg.load_library()
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    cfg = mdl.SeAConfig()
+    c, t, b = _frame()
+    nat = len(t)
+    m64 = se_a.build_model(cfg, SEED, _stat_frames(), dev, torch.float64)
+    model = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
+                          torch.float32, m64.tables_np, m64.infos_np)
+    batch = model.batch([t], b[None])
+    coord = torch.tensor(c, dtype=torch.float32, device=dev)
+
+    # ---- capture the fused step in a CUDA graph
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            model.step_fused(batch, coord)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    st = batch.status()
+    if st != 0:
+        raise RuntimeError(f"neighbour build status {st}")
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        E_g, F_g, V_g = model.step_fused(batch, coord)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        graph.replay()
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        barrier()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (256 MB write), outside the events
+            starts[k].record()
+            graph.replay()
+            ends[k].record()
+        barrier()
+        wall = time.perf_counter() - wall0
+    step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    if ws > 1:
+        tt = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(tt)
+    value = ws * nat / (step_ms * 1e-3)
+    if batch.status() != 0:
+        raise RuntimeError("neighbour build reported a device status during the timed steps")
+
+    # ---- e2e through the public API: pinned host coords in, E/F/V out
+    h_coord = torch.tensor(c, dtype=torch.float32).pin_memory()
+    h_E = torch.empty(1, dtype=torch.float64).pin_memory()
+    h_F = torch.empty((nat, 3), dtype=torch.float32).pin_memory()
+    h_V = torch.empty((1, 9), dtype=torch.float64).pin_memory()
+    e_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for _ in range(3):
+        coord.copy_(h_coord, non_blocking=True)
+        graph.replay()
+    barrier()
+    for k in range(args.steps):
+        flush.zero_()
+        e_st[k].record()
+        coord.copy_(h_coord, non_blocking=True)
+        graph.replay()
+        h_E.copy_(E_g, non_blocking=True)
+        h_F.copy_(F_g, non_blocking=True)
+        h_V.copy_(V_g, non_blocking=True)
+        e_en[k].record()
+    barrier()
+    e2e_ms = sum(s.elapsed_time(e) for s, e in zip(e_st, e_en)) / args.steps
+    if ws > 1:
+        tt = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt)
+    e2e = {"value": ws * nat / (e2e_ms * 1e-3), "unit": "atom-steps/s",
+           "h2d_bytes_per_step": h_coord.numel() * 4,
+           "d2h_bytes_per_step": h_E.numel() * 8 + h_F.numel() * 4 + h_V.numel() * 8}
+
+    # ---- per-kernel times of the fused step (eager, events on the stream)
+    kt = kernel_times(model, batch, coord, flush, reps=max(3, min(args.steps, 10)))
+    dom = max(kt, key=lambda k: kt[k]["ms"])
+    peaks = _peaks()
+    roof = roofline(dom, kt[dom], nat, cfg, peaks)
+
+    # ---- plain (uncompressed) drop-in, eager, same frame
+    mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
+                       torch.float32)
+    for _ in range(2):
+        mp.step_ops(batch, coord, compressed=False)
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    n_plain = max(2, min(args.steps, 5))
+    for _ in range(n_plain):
+        Ep, Fp, Vp = mp.step_ops(batch, coord, compressed=False)
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - p0) / n_plain * 1e3
+
+    out = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded water generator, random-init weights)",
+           "config": {"workload": WORKLOAD, "atoms": nat, "form": "fused compressed, CUDA graph",
+                      "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
+                      "wall_s": wall},
+           "e2e": e2e, "gpu_launches": 8 * args.steps,
+           "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                     "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
+           "kernels_ms": {k: v["ms"] for k, v in kt.items()},
+           "roofline": roof, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu:
+        import oracle as O
+        import composite
+
+        np_model = (cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), m64.tables_np,
+                    m64.infos_np)
+        E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t, b, np_model[4], np_model[5])
+        Fn = F_g.detach().cpu().numpy().astype(np.float64)
+        out["errors_vs_fp64"] = {
+            "force_max_abs_eV_per_A": float(np.abs(Fn - F64).max()),
+            "force_rms_eV_per_A": float(np.sqrt(((Fn - F64) ** 2).mean())),
+            "energy_per_atom_eV": abs(float(E_g[0]) - E64) / nat,
+            "virial_max_abs_eV": float(np.abs(V_g[0].cpu().numpy() - V64).max()),
+            "plain_force_max_abs_eV_per_A": float(np.abs(Fp.detach().cpu().numpy() - F64).max()),
+            "reference": "FP64 CPU composite (oracle) of the compressed model"}
+        out["cpu_baseline"] = {k: v for k, v in cpu_baseline((c, t, b), np_model, steps=2).items()
+                               if k != "s_per_step"}
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def kernel_times(model, batch, coord, flush, reps: int = 5):
+    """Average device time of each part of the fused step (CUDA events on
+    the launching stream, L2 flushed before each part)."""
+    import ctypes
+
+    import torch
+
+    se_a = sys.modules["dpmd_public_gb300.se_a"]
+    L = sys.modules["dpmd_public_gb300._lib"]
+    cfg = model.cfg
+    M, A = cfg.neuron[-1], cfg.axis_neuron
+    lib = model._lib
+    P = lambda x: ctypes.c_void_p(x.data_ptr())
+    S = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    b = batch
+    ops = sys.modules["dpmd_public_gb300.ops"]
+
+    def env():
+        ops.env_mat_packed(b.plan, coord, b.atype, model.davg, model.dstd, cfg.rcut_smth, list(cfg.sel),
+                           check_status=False, out=b.env)
+
+    def fwd():
+        lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), model._tab_ptrs,
+                                         model._tab_infos, cfg.ntypes, model._sel_c,
+                                         int(cfg.type_one_side), b.nloc, M, A, S())
+
+    def fit():
+        for t in range(cfg.ntypes):
+            idx = b.type_idx[t]
+            e, g = model.fitting_fwd_bwd(t, b.D.index_select(0, idx))
+            b.ae.index_copy_(0, idx, e)
+            b.dD.index_copy_(0, idx, g)
+
+    def bwd():
+        lib.gbdp_se_a_descriptor_bwd_f32(
+            P(b.force), P(b.vir), P(b.X), P(b.dD), P(b.env.em), P(b.env.nlist_ext), P(b.env.ext_coord),
+            P(b.env.ext_map), P(b.atype), P(model.dstd), P(b.atom_frame), P(b.frame_aoff), P(b.frame_eoff),
+            model._tab_ptrs, model._tab_infos, cfg.ntypes, model._sel_c, int(cfg.type_one_side),
+            ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), b.nloc, b.nframes, M, A, S())
+
+    parts = {"env_nlist": env, "desc_fwd": fwd, "fitting_gemm": fit, "desc_bwd": bwd}
+    res = {}
+    for name, fn in parts.items():
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            torch.cuda.synchronize()
+            ts.append(s.elapsed_time(e))
+        res[name] = {"ms": statistics.median(ts)}
+    return res
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
+
+
+# algorithmic HBM bytes per local atom of each part (FP32, nnei 138, M 100,
+# A 16): inputs read once, outputs written once
+def _alg_bytes(name, cfg):
+    nn, M, A = cfg.nnei, cfg.neuron[-1], cfg.axis_neuron
+    f = 4
+    if name == "env_nlist":
+        # coord + type in; em, nlist (local + ext) out; ghosts ~0.9 x nloc x 16 B
+        return 12 + 4 + nn * 4 * f + 2 * nn * 4 + 16
+    if name == "desc_fwd":
+        return nn * 4 * f + 4 * M * f + M * A * f + 4  # em in; X, D out
+    if name == "desc_bwd":
+        # X, dE/dD, em, nlist_ext in; ~91 neighbour coords (L2) ; force out
+        return 4 * M * f + M * A * f + nn * 4 * f + nn * 4 + 12
+    if name == "fitting_gemm":
+        return 2 * M * A * f  # D in, dE/dD out
+    return 0
+
+
+def roofline(name, t, nat, cfg, peaks):
+    alg = _alg_bytes(name, cfg) * nat
+    ms = t["ms"]
+    ach = alg / (ms * 1e-3) / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": ach / peaks["hbm_gbs"], "traffic": None, "peak_src": peaks["src"],
+            "alg_bytes_per_launch": alg, "ms_per_launch": ms}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -383,20 +383,16 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
                            check_status=False, out=b.env)
 
     def fwd():
-        lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), model._tab_ptrs,
+        lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), P(b.drow), model._tab_ptrs,
                                          model._tab_infos, cfg.ntypes, model._sel_c,
                                          int(cfg.type_one_side), b.nloc, M, A, S())
 
     def fit():
-        for t in range(cfg.ntypes):
-            idx = b.type_idx[t]
-            e, g = model.fitting_fwd_bwd(t, b.D.index_select(0, idx))
-            b.ae.index_copy_(0, idx, e)
-            b.dD.index_copy_(0, idx, g)
+        model.fitting_rows(b)
 
     def bwd():
         lib.gbdp_se_a_descriptor_bwd_f32(
-            P(b.force), P(b.vir), P(b.X), P(b.dD), P(b.env.em), P(b.env.nlist_ext), P(b.env.ext_coord),
+            P(b.force), P(b.vir), P(b.X), P(b.dD), P(b.drow), P(b.env.em), P(b.env.nlist_ext), P(b.env.ext_coord),
             P(b.env.ext_map), P(b.atype), P(model.dstd), P(b.atom_frame), P(b.frame_aoff), P(b.frame_eoff),
             model._tab_ptrs, model._tab_infos, cfg.ntypes, model._sel_c, int(cfg.type_one_side),
             ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), b.nloc, b.nframes, M, A, S())

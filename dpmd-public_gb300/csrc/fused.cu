@@ -59,7 +59,8 @@ __device__ __forceinline__ void load_coef6<float>(float* a, const float* __restr
 template <typename T, int NQ, int A>
 __global__ void __launch_bounds__(kFWarps * 32)
     k_desc_fwd(T* __restrict__ X, T* __restrict__ D, const T* __restrict__ em,
-               const int* __restrict__ atype, TabSet<T> ts, int nloc, int nnei, int M) {
+               const int* __restrict__ atype, const int* __restrict__ drow, TabSet<T> ts,
+               int nloc, int nnei, int M) {
   __shared__ T xs[kFWarps][4][NQ * 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kFWarps + warp;
@@ -134,7 +135,8 @@ __global__ void __launch_bounds__(kFWarps * 32)
   for (int q = 0; q < NQ; ++q) {
     const int k = q * 32 + lane;
     if (k >= M) continue;
-    T* d = D + ((size_t)i * M + k) * A;
+    const size_t r = drow ? (size_t)drow[i] : (size_t)i;
+    T* d = D + (r * M + k) * A;
 #pragma unroll
     for (int a = 0; a < A; ++a) {
       T v = acc[q][0] * xs[warp][0][a] + acc[q][1] * xs[warp][1][a] +
@@ -172,7 +174,7 @@ struct BwdGeom {
 template <typename T, int NQ, int A>
 __global__ void __launch_bounds__(kFWarps * 32)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
-               const T* __restrict__ dD, const T* __restrict__ em,
+               const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
                const int* __restrict__ ext_map, const int* __restrict__ atype,
                const T* __restrict__ stdv, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
@@ -190,7 +192,8 @@ __global__ void __launch_bounds__(kFWarps * 32)
     const int m = t / M, k = t - m * M;
     xs[m * MP + k] = X[(size_t)i * 4 * M + t];
   }
-  for (int t = lane; t < M * A; t += 32) gs[t] = dD[(size_t)i * M * A + t];
+  const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
+  for (int t = lane; t < M * A; t += 32) gs[t] = dD[drow_i * M * A + t];
   __syncwarp();
   const T inv = T(1) / T(nnei);
   // dX[m][k] = sum_a G[k][a] X[m][a] + [k < A] sum_k' G[k'][k] X[m][k']
@@ -335,8 +338,9 @@ int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntype
 }
 
 template <typename T>
-int desc_fwd(T* X, T* D, const T* em, const int* atype, const T* const* tables, const T* infos,
-             int ntypes, const int* sel, int one_side, int nloc, int M, int A, cudaStream_t st) {
+int desc_fwd(T* X, T* D, const T* em, const int* atype, const int* drow, const T* const* tables,
+             const T* infos, int ntypes, const int* sel, int one_side, int nloc, int M, int A,
+             cudaStream_t st) {
   TabSet<T> ts;
   int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side);
   if (rc) return rc;
@@ -347,19 +351,19 @@ int desc_fwd(T* X, T* D, const T* em, const int* atype, const T* const* tables, 
   const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
   const int nq = (M + 31) / 32;
   if (nq == 4)
-    k_desc_fwd<T, 4, 16><<<grid, block, 0, st>>>(X, D, em, atype, ts, nloc, nnei, M);
+    k_desc_fwd<T, 4, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
   else if (nq == 3)
-    k_desc_fwd<T, 3, 16><<<grid, block, 0, st>>>(X, D, em, atype, ts, nloc, nnei, M);
+    k_desc_fwd<T, 3, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
   else if (nq == 2)
-    k_desc_fwd<T, 2, 16><<<grid, block, 0, st>>>(X, D, em, atype, ts, nloc, nnei, M);
+    k_desc_fwd<T, 2, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
   else
-    k_desc_fwd<T, 1, 16><<<grid, block, 0, st>>>(X, D, em, atype, ts, nloc, nnei, M);
+    k_desc_fwd<T, 1, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
   GBDP_CHECK_LAUNCH("se_a_descriptor_fwd");
   return GBDP_OK;
 }
 
 template <typename T>
-int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const T* em,
+int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow, const T* em,
              const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,
              const T* stdv, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
@@ -384,9 +388,9 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const T* em,
     auto kern = k_desc_bwd<T, NQV, 16>;                                                        \
     if (smem > 48 * 1024)                                                                      \
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
-    kern<<<grid, block, smem, st>>>(force, vir_acc, X, dD, em, nlist_ext, ext_coord, ext_map,  \
-                                    atype, stdv, geo, ts, (T)rcut_smth, (T)rcut, nloc, nnei,   \
-                                    M);                                                        \
+    kern<<<grid, block, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,     \
+                                    ext_map, atype, stdv, geo, ts, (T)rcut_smth, (T)rcut,      \
+                                    nloc, nnei, M);                                            \
   }
   if (nq == 4)
     GBDP_LAUNCH_BWD(4)
@@ -408,20 +412,21 @@ using namespace gbdp;
 
 #define GBDP_FUSED_ENTRY(T, SFX)                                                                \
   extern "C" int gbdp_se_a_descriptor_fwd_##SFX(                                                \
-      T* X, T* D, const T* em, const int* atype, const T* const* tables, const T* table_infos,  \
-      int ntypes, const int* sel, int type_one_side, int nloc, int last_layer_size,            \
-      int axis_neuron, gbdp_stream stream) {                                                    \
-    return desc_fwd<T>(X, D, em, atype, tables, table_infos, ntypes, sel, type_one_side, nloc, \
-                       last_layer_size, axis_neuron, (cudaStream_t)stream);                    \
+      T* X, T* D, const T* em, const int* atype, const int* d_row, const T* const* tables,      \
+      const T* table_infos, int ntypes, const int* sel, int type_one_side, int nloc,           \
+      int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
+    return desc_fwd<T>(X, D, em, atype, d_row, tables, table_infos, ntypes, sel, type_one_side, \
+                       nloc, last_layer_size, axis_neuron, (cudaStream_t)stream);              \
   }                                                                                             \
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
-      T* force, double* virial_acc, const T* X, const T* dE_dD, const T* em,                   \
+      T* force, double* virial_acc, const T* X, const T* dE_dD, const int* d_row, const T* em, \
       const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,          \
       const T* std, const int* atom_frame, const int* frame_atom_off,                          \
       const int* frame_ext_off, const T* const* tables, const T* table_infos, int ntypes,      \
       const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
-    return desc_bwd<T>(force, virial_acc, X, dE_dD, em, nlist_ext, ext_coord, ext_map, atype,  \
+    return desc_bwd<T>(force, virial_acc, X, dE_dD, d_row, em, nlist_ext, ext_coord, ext_map,  \
+                       atype,                                                                  \
                        std, atom_frame, frame_atom_off, frame_ext_off, tables, table_infos,    \
                        ntypes, sel, type_one_side, rcut_smth, rcut, nloc, nframes,             \
                        last_layer_size, axis_neuron, (cudaStream_t)stream);                    \

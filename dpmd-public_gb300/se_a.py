@@ -40,8 +40,17 @@ def _stream():
 
 
 class SeAModel:
+    FIT_MODES = ("fp32", "tf32x3", "bf16")
+
     def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
-                 device, dtype=torch.float32, tables=None, table_infos=None):
+                 device, dtype=torch.float32, tables=None, table_infos=None, fit_mode="fp32"):
+        """fit_mode selects the fitting GEMMs: "fp32" (cuBLAS SGEMM),
+        "tf32x3" (each operand split into a TF32 head and a remainder, three
+        tensor-core products, FP32-level accuracy) or "bf16" (BF16 tensor
+        cores with FP32 accumulation, a stated larger error)."""
+        if fit_mode not in self.FIT_MODES:
+            raise ValueError(f"fit_mode must be one of {self.FIT_MODES}")
+        self.fit_mode = fit_mode if dtype == torch.float32 else "fp32"
         self.cfg = cfg
         self.device = torch.device(device)
         self.dtype = dtype
@@ -53,6 +62,17 @@ class SeAModel:
                       for l in f["hidden"]]
             self.fit.append((hidden, T(f["final"]["w"]), T(f["final"]["b"])))
         self.bias_atom_e = T(params["bias_atom_e"])
+        # transposed / split copies of the fitting weights for the GEMM modes
+        self._wsplit = {}
+        for f in self.fit:
+            for w, *_ in f[0]:
+                self._wsplit[w.data_ptr()] = _split_tf32(w) + (w.to(torch.bfloat16),)
+        self._wt = {}
+        for f in self.fit:
+            for w, *_ in f[0]:
+                wt = w.t().contiguous()
+                self._wt[w.data_ptr()] = wt
+                self._wsplit[wt.data_ptr()] = _split_tf32(wt) + (wt.to(torch.bfloat16),)
         self.davg = T(davg).contiguous()
         self.dstd = T(dstd).contiguous()
         self.tables = None
@@ -73,15 +93,39 @@ class SeAModel:
         return Batch(self, atype_per_frame, boxes, max_cand)
 
     # ------------------------------------------------------------ fitting --
-    def fitting_fwd_bwd(self, t: int, D: torch.Tensor):
+    def _mm(self, a: torch.Tensor, w: torch.Tensor, out=None):
+        """a @ w in the selected fitting mode (w is a weight matrix whose
+        split copies were prepared at construction)."""
+        if self.fit_mode == "fp32":
+            return torch.mm(a, w, out=out)
+        w_hi, w_lo, w_bf = self._wsplit[w.data_ptr()]
+        if self.fit_mode == "bf16":
+            r = torch.mm(a.to(torch.bfloat16), w_bf).to(torch.float32)
+            if out is not None:
+                out.copy_(r)
+                return out
+            return r
+        a_hi, a_lo = _split_tf32(a)
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = True
+        try:
+            r = torch.mm(a_hi, w_hi, out=out)
+            r.addmm_(a_hi, w_lo)
+            r.addmm_(a_lo, w_hi)
+        finally:
+            torch.backends.cuda.matmul.allow_tf32 = prev
+        return r
+
+    def fitting_fwd_bwd(self, t: int, D: torch.Tensor, dD_out=None):
         """Energy of type-t atoms and dE/dD (hidden tanh layers with idt /
         skip where present, linear output; deepmd/pt/model/task/fitting.py
-        with deepmd/dpmodel/utils/network.py layer semantics)."""
+        with deepmd/dpmodel/utils/network.py layer semantics).  dE/dD is
+        written into ``dD_out`` when given."""
         hidden, wf, bf = self.fit[t]
         h = D
         cache = []
         for w, b, idt, skip in hidden:
-            tt = torch.tanh(torch.addmm(b, h, w))
+            tt = torch.tanh(self._mm(h, w).add_(b))
             out = tt * idt if idt is not None else tt
             if skip == "same":
                 out = out + h
@@ -89,12 +133,15 @@ class SeAModel:
             h = out
         e = torch.addmm(bf, h, wf)[:, 0] + self.bias_atom_e[t]
         g = wf[:, 0].expand(h.shape[0], -1)
-        for tt, idt, skip, w in reversed(cache):
+        for k, (tt, idt, skip, w) in enumerate(reversed(cache)):
             gt = g * idt if idt is not None else g
             gz = gt * (1 - tt * tt)
-            gin = torch.mm(gz, w.t())
+            last = k == len(cache) - 1
+            gin = self._mm(gz, self._wt[w.data_ptr()], out=dD_out if (last and skip != "same") else None)
             if skip == "same":
                 gin = gin + g
+                if last and dD_out is not None:
+                    dD_out.copy_(gin)
             g = gin
         return e, g
 
@@ -121,26 +168,30 @@ class SeAModel:
                        check_status=False, out=b.env)
         lib = self._lib
         L.check(getattr(lib, f"gbdp_se_a_descriptor_fwd_{self._sfx}")(
-            _ptr(b.X), _ptr(b.D), _ptr(b.env.em), _ptr(b.atype), self._tab_ptrs, self._tab_infos,
-            cfg.ntypes, self._sel_c, int(cfg.type_one_side), n, M, A, _stream()),
+            _ptr(b.X), _ptr(b.D), _ptr(b.env.em), _ptr(b.atype), _ptr(b.drow), self._tab_ptrs,
+            self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side), n, M, A, _stream()),
             "se_a_descriptor_fwd")
-        for t in range(cfg.ntypes):
-            idx = b.type_idx[t]
-            if idx.numel() == 0:
-                continue
-            e, g = self.fitting_fwd_bwd(t, b.D.index_select(0, idx))
-            b.ae.index_copy_(0, idx, e)
-            b.dD.index_copy_(0, idx, g)
+        self.fitting_rows(b)
         L.check(getattr(lib, f"gbdp_se_a_descriptor_bwd_{self._sfx}")(
-            _ptr(b.force), _ptr(b.vir), _ptr(b.X), _ptr(b.dD), _ptr(b.env.em), _ptr(b.env.nlist_ext),
+            _ptr(b.force), _ptr(b.vir), _ptr(b.X), _ptr(b.dD), _ptr(b.drow), _ptr(b.env.em),
+            _ptr(b.env.nlist_ext),
             _ptr(b.env.ext_coord), _ptr(b.env.ext_map), _ptr(b.atype), _ptr(self.dstd),
             _ptr(b.atom_frame), _ptr(b.frame_aoff), _ptr(b.frame_eoff), self._tab_ptrs,
             self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side),
             ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), n, b.nframes, M, A,
             _stream()), "se_a_descriptor_bwd")
         b.energy.zero_()
-        b.energy.index_add_(0, b.frame_of_atom, b.ae.to(torch.float64))
+        b.energy.index_add_(0, b.frame_of_row, b.ae.to(torch.float64))
         return b.energy, b.force, b.vir
+
+    def fitting_rows(self, b: "Batch"):
+        """Per-type fitting over the type-contiguous rows of D (each atom
+        through its own type's net only)."""
+        for t, (s0, nt) in enumerate(b.type_rows):
+            if nt == 0:
+                continue
+            e, _ = self.fitting_fwd_bwd(t, b.D[s0:s0 + nt], dD_out=b.dD[s0:s0 + nt])
+            b.ae[s0:s0 + nt].copy_(e)
 
     # --------------------------------------------- operator-contract forms --
     def _descriptor_from_em(self, em: torch.Tensor, atype: torch.Tensor, compressed: bool):
@@ -209,6 +260,87 @@ class SeAModel:
         return E, torch.cat(forces), torch.stack(virs).to(torch.float64)
 
 
+def _split_tf32(x: torch.Tensor):
+    """x = hi + lo with hi exactly representable in TF32 (10 explicit
+    mantissa bits, low 13 bits cleared) and lo the remainder."""
+    hi = (x.contiguous().view(torch.int32) & -8192).view(torch.float32)
+    return hi, x - hi
+
+
+def energy_std_loss(E, F, V, E_ref, F_ref, V_ref, natoms: int, pref_e=0.02, pref_f=1000.0,
+                    pref_v=0.02):
+    """EnergyStdLoss with fixed prefactors (deepmd/pt/loss/ener.py:197-360):
+    pref_e * mean((E - E_ref)^2) / natoms^2 ... as the reference scales the
+    energy and virial terms by 1/natoms (atom_norm), plus pref_f * mean of the
+    squared force error."""
+    inv = 1.0 / natoms
+    l_e = ((E - E_ref) ** 2).mean() * inv * inv
+    l_f = ((F - F_ref) ** 2).mean()
+    l_v = ((V - V_ref) ** 2).mean() * inv * inv
+    return pref_e * l_e + pref_f * l_f + pref_v * l_v
+
+
+class Trainable:
+    """Fitting-net parameters of a compressed model as autograd leaves, and
+    a training forward that keeps the graph through the force (double
+    backward: tabulate grad-grad, prod_force_grad / prod_virial_grad)."""
+
+    def __init__(self, model: SeAModel):
+        self.model = model
+        self.params = []
+        fit = []
+        for hidden, wf, bf in model.fit:
+            h = []
+            for w, b, idt, skip in hidden:
+                w = w.clone().requires_grad_(True)
+                b = b.clone().requires_grad_(True)
+                idt = None if idt is None else idt.clone().requires_grad_(True)
+                self.params += [w, b] + ([idt] if idt is not None else [])
+                h.append((w, b, idt, skip))
+            wf = wf.clone().requires_grad_(True)
+            bf = bf.clone().requires_grad_(True)
+            self.params += [wf, bf]
+            fit.append((h, wf, bf))
+        self.fit = fit
+
+    def energy_force_virial(self, b: "Batch", coord, compressed: bool = True):
+        m = self.model
+        cfg = m.cfg
+        nnei = cfg.nnei
+        env = env_mat_packed(b.plan, coord, b.atype, m.davg, m.dstd, cfg.rcut_smth, list(cfg.sel),
+                             need_deriv=True, need_rij=True, check_status=False)
+        em = env.em.detach().requires_grad_(True)
+        D = m._descriptor_from_em(em, b.atype, compressed)
+        E_atom = torch.zeros(b.nloc, dtype=m.dtype, device=m.device)
+        for t in range(cfg.ntypes):
+            idx = b.type_idx[t]
+            if idx.numel() == 0:
+                continue
+            hidden, wf, bf = self.fit[t]
+            h = D.index_select(0, idx)
+            for w, bb, idt, skip in hidden:
+                tt = torch.tanh(h @ w + bb)
+                out = tt * idt if idt is not None else tt
+                h = out + h if skip == "same" else out
+            E_atom = E_atom.index_add(0, idx, (h @ wf + bf)[:, 0] + m.bias_atom_e[t])
+        net = torch.autograd.grad(E_atom.sum(), em, create_graph=True)[0]
+        from .ops import ProdForceFn, ProdVirialFn
+
+        F, V = [], []
+        for f in range(b.nframes):
+            a0 = int(b.plan.atom_off[f])
+            nl = int(b.plan.nloc[f])
+            natoms = torch.tensor([nl, nl] + [0] * cfg.ntypes, dtype=torch.int32)
+            nd = net[a0:a0 + nl].reshape(1, -1)
+            ed = env.em_deriv[a0:a0 + nl].reshape(1, -1)
+            nls = env.nlist[a0:a0 + nl].reshape(1, -1)
+            F.append(ProdForceFn.apply(nd, ed, nls, natoms, nnei, 0).reshape(nl, 3))
+            V.append(ProdVirialFn.apply(nd, ed, env.rij[a0:a0 + nl].reshape(1, -1), nls, natoms, nnei,
+                                        0)[0].reshape(9))
+        E = torch.zeros(b.nframes, dtype=m.dtype, device=m.device).index_add(0, b.frame_of_atom, E_atom)
+        return E, torch.cat(F), torch.stack(V)
+
+
 class Batch:
     """Static per-batch state: the neighbour plan, type groups and every
     buffer the fused step writes (fixed addresses, so the step can be
@@ -232,6 +364,15 @@ class Batch:
         self.frame_eoff = torch.tensor(self.plan.ext_off, dtype=torch.int32, device=dev)
         self.type_idx = [torch.tensor(np.nonzero(flat == t)[0], dtype=torch.int64, device=dev)
                          for t in range(cfg.ntypes)]
+        # rows of D / dE/dD grouped by type (stable within a type)
+        order = np.argsort(flat, kind="stable")
+        drow = np.empty_like(order)
+        drow[order] = np.arange(len(order))
+        self.drow = torch.tensor(drow, dtype=torch.int32, device=dev)
+        counts = [int((flat == t).sum()) for t in range(cfg.ntypes)]
+        starts = np.concatenate([[0], np.cumsum(counts)[:-1]]) if counts else []
+        self.type_rows = [(int(s0), int(c0)) for s0, c0 in zip(starts, counts)]
+        self.frame_of_row = torch.tensor(fo[order], dtype=torch.int64, device=dev)
         n = self.nloc
         nnei = cfg.nnei
         M, A = cfg.neuron[-1], cfg.axis_neuron

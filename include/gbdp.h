@@ -245,7 +245,9 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * deepmd::tabulate_fusion_se_a).  tables: HOST array of device table
  * pointers, one per embedding net (ntypes nets if type_one_side, else
  * ntypes^2 indexed tj * ntypes + ti); table_infos: HOST [n_tables * 6];
- * sel: HOST [ntypes].  em comes from gbdp_prod_env_mat_a_*.
+ * sel: HOST [ntypes].  em comes from gbdp_prod_env_mat_a_*.  d_row (device,
+ * may be NULL for the identity) gives the row of D / dE_dD that belongs to
+ * atom i, so that a caller can keep each type's rows contiguous.
  * Backward: from dE/dD, force [nloc, 3] (zeroed here, local indices, packed
  * frames) and virial_acc [nframes, 9] (double, zeroed here) get the
  * contributions of every real neighbour, the env-matrix derivative being
@@ -254,24 +256,27 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * are device arrays describing the packed batch (see gbdp_nbr_frame).
  * ---------------------------------------------------------------------- */
 GBDP_API int gbdp_se_a_descriptor_fwd_f32(float* X, float* D, const float* em, const int* atype,
-                                          const float* const* tables, const float* table_infos,
+                                          const int* d_row, const float* const* tables, const float* table_infos,
                                           int ntypes, const int* sel, int type_one_side,
                                           int nloc, int last_layer_size, int axis_neuron,
                                           gbdp_stream stream);
 GBDP_API int gbdp_se_a_descriptor_fwd_f64(double* X, double* D, const double* em,
-                                          const int* atype, const double* const* tables,
+                                          const int* atype, const int* d_row,
+                                          const double* const* tables,
                                           const double* table_infos, int ntypes, const int* sel,
                                           int type_one_side, int nloc, int last_layer_size,
                                           int axis_neuron, gbdp_stream stream);
 GBDP_API int gbdp_se_a_descriptor_bwd_f32(
-    float* force, double* virial_acc, const float* X, const float* dE_dD, const float* em,
+    float* force, double* virial_acc, const float* X, const float* dE_dD, const int* d_row,
+    const float* em,
     const int* nlist_ext, const float* ext_coord, const int* ext_map, const int* atype,
     const float* std, const int* atom_frame, const int* frame_atom_off, const int* frame_ext_off,
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
     int type_one_side, float rcut_smth, float rcut, int nloc, int nframes, int last_layer_size,
     int axis_neuron, gbdp_stream stream);
 GBDP_API int gbdp_se_a_descriptor_bwd_f64(
-    double* force, double* virial_acc, const double* X, const double* dE_dD, const double* em,
+    double* force, double* virial_acc, const double* X, const double* dE_dD, const int* d_row,
+    const double* em,
     const int* nlist_ext, const double* ext_coord, const int* ext_map, const int* atype,
     const double* std, const int* atom_frame, const int* frame_atom_off,
     const int* frame_ext_off, const double* const* tables, const double* table_infos,

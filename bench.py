@@ -181,6 +181,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error")
+    ap.add_argument("--fit-mode", default="fp32", choices=["fp32", "tf32x3", "bf16"],
+                    help="fitting GEMMs: FP32 SIMT, split TF32 (FP32-level accuracy) or BF16")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: set up, then 2 fused steps and 1 operator-form step "
                          "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
@@ -213,7 +215,7 @@ def main():
     nat = len(t)
     m64 = se_a.build_model(cfg, SEED, _stat_frames(), dev, torch.float64)
     model = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
-                          torch.float32, m64.tables_np, m64.infos_np)
+                          torch.float32, m64.tables_np, m64.infos_np, fit_mode=args.fit_mode)
     batch = model.batch([t], b[None])
     coord = torch.tensor(c, dtype=torch.float32, device=dev)
 
@@ -330,6 +332,7 @@ def main():
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded water generator, random-init weights)",
            "config": {"workload": WORKLOAD, "atoms": nat, "form": "fused compressed, CUDA graph",
+                      "fitting_gemm": args.fit_mode,
                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
                       "wall_s": wall},
            "e2e": e2e, "gpu_launches": 8 * args.steps,

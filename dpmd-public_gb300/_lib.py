@@ -66,6 +66,7 @@ _SIGS = {
     "gbdp_env_workspace_bytes": (_Z, [_P, _I]),
     "gbdp_env_status": (_I, [_P, _P]),
     "gbdp_prod_workspace_bytes": (_Z, [_I, _I, _I, _I, _I]),
+    "gbdp_prod_env_mat_a_noalloc_f32": (_I, [_P] * 16 + [_F, _P, _I, _P]),
 }
 for _s in ("f32", "f64"):
     _SIGS.update({

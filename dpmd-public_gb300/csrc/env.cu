@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -827,4 +828,78 @@ extern "C" int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij
   return env_launch<double>(em, em_deriv, rij, nlist, nlist_ext, ext_coord, ext_type, ext_map,
                             ext_nall, coord, atype, avg, std, plan, frames_dev, rcut_smth, sel,
                             ntypes, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------ allocation-free variant --
+// Scratch for gbdp_prod_env_mat_a_noalloc_f32: a file-scope device array, so
+// callers that must not allocate device memory can still run the periodic
+// neighbour build.  Every GPU that loads the library holds it until exit.
+// The last kNoAllocFrameBytes hold the copied frame table.
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
+constexpr size_t kNoAllocFrameBytes = size_t(64) << 10;    // 64 KiB (315 frames)
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_env_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array for the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+int noalloc_scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: cudaGetDevice");
+  GBDP_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices,
+               "prod_env_mat_a_noalloc: device ordinal %d above %d", dev, kNoAllocMaxDevices - 1);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_env_noalloc_scratch);
+    if (e != cudaSuccess)
+      return cuda_status(e, "prod_env_mat_a_noalloc: cudaGetSymbolAddress");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return GBDP_OK;
+}
+}  // namespace
+
+extern "C" int gbdp_prod_env_mat_a_noalloc_f32(
+    float* em, float* em_deriv, float* rij, int* nlist, int* nlist_ext, float* ext_coord,
+    int* ext_type, int* ext_map, int* ext_nall, int* status, const float* coord,
+    const int* atype, const float* avg, const float* std, const gbdp_nbr_plan* plan,
+    const gbdp_nbr_frame* frames_host, float rcut_smth, const int* sel, int ntypes,
+    gbdp_stream stream) {
+  GBDP_REQUIRE(plan && frames_host && status, "prod_env_mat_a_noalloc: null plan/frames/status");
+  const size_t need = carve(*plan, nullptr, 0).bytes;
+  const size_t room = kNoAllocScratchBytes - kNoAllocFrameBytes;
+  GBDP_REQUIRE(need <= room,
+               "prod_env_mat_a_noalloc: this batch needs %zu scratch bytes, the built-in "
+               "scratch holds %zu (use gbdp_prod_env_mat_a_f32 with a workspace)",
+               need, room);
+  const size_t fbytes = sizeof(gbdp_nbr_frame) * (size_t)plan->nframes;
+  GBDP_REQUIRE(fbytes <= kNoAllocFrameBytes,
+               "prod_env_mat_a_noalloc: %d frames exceed the built-in frame table (%zu)",
+               plan->nframes, kNoAllocFrameBytes / sizeof(gbdp_nbr_frame));
+  void* base = nullptr;
+  int rc = noalloc_scratch_address(&base);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned char* frames_dev = static_cast<unsigned char*>(base) + room;
+  cudaError_t e = cudaMemcpyAsync(frames_dev, frames_host, fbytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: frame table copy");
+  rc = env_launch<float>(em, em_deriv, rij, nlist, nlist_ext, ext_coord, ext_type, ext_map,
+                         ext_nall, coord, atype, avg, std, plan,
+                         reinterpret_cast<const gbdp_nbr_frame*>(frames_dev), rcut_smth, sel,
+                         ntypes, base, room, st);
+  if (rc) return rc;
+  // hand the device status word to the caller's buffer (stream-ordered)
+  e = cudaMemcpyAsync(status, base, sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: status copy");
+  return GBDP_OK;
 }

@@ -177,6 +177,33 @@ GBDP_API int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij, 
                             int ntypes, void* workspace, size_t workspace_bytes,
                             gbdp_stream stream);
 
+/* Allocation-free variant of gbdp_prod_env_mat_a_f32 (float only).  It has
+ * no counterpart in the reference.  It is for callers that cannot allocate
+ * device memory at the point of the call: a host MD engine that owns all
+ * device memory through its own pool and forbids driver allocations inside
+ * its force callback, or code that runs while a stream is being captured,
+ * where cudaMalloc is not allowed.  Instead of a caller workspace it uses a
+ * built-in 16 MiB device scratch array that every GPU loading the library
+ * holds until exit (enough for a batch of roughly 100k atoms at water
+ * density); a batch whose workspace would exceed 16 MiB - 64 KiB, or with
+ * more than 315 frames, is rejected with GBDP_ERR_INVALID and a message.
+ * The frame table is passed on the HOST (frames_host) and copied into the
+ * scratch; `status` is a caller-provided device int that receives the
+ * device status word (GBDP_OK or a GBDP_STATUS_* code) in stream order.
+ * Other arguments and outputs are those of gbdp_prod_env_mat_a_f32.
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls share the one array and it keeps
+ * the last call's contents (counters are cleared at the start of every
+ * call): calls that overlap on the GPU, on any stream, race with each
+ * other.  The function itself never calls cudaMalloc or cudaFree. */
+GBDP_API int gbdp_prod_env_mat_a_noalloc_f32(
+    float* em, float* em_deriv, float* rij, int* nlist, int* nlist_ext, float* ext_coord,
+    int* ext_type, int* ext_map, int* ext_nall, int* status, const float* coord,
+    const int* atype, const float* avg, const float* std, const gbdp_nbr_plan* plan,
+    const gbdp_nbr_frame* frames_host, float rcut_smth, const int* sel, int ntypes,
+    gbdp_stream stream);
+
 /* Synchronise `stream` and return the device status word of an env-mat
  * workspace (GBDP_OK or a GBDP_STATUS_* code). */
 GBDP_API int gbdp_env_status(const void* workspace, gbdp_stream stream);

@@ -171,6 +171,39 @@ struct BwdGeom {
   const int* frame_eoff;   // [nframes] first extended slot of each frame
 };
 
+// Sum of v[0..31] over the 32 lanes, scattered: lane l returns the total of
+// value l.  31 shuffles for 32 sums (instead of 5 per sum): at the step with
+// offset o every lane keeps the half of its values selected by lane bit o and
+// adds the partner's copy of that half.
+template <typename T>
+__device__ __forceinline__ T reduce_scatter32(T (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < o; ++k) {
+      const T send = up ? v[k] : v[k + o];
+      const T keep = up ? v[k + o] : v[k];
+      v[k] = keep + __shfl_xor_sync(kFull, send, o);
+    }
+  }
+  return v[0];
+}
+
+constexpr int kBwdGroup = 6;  // neighbours per reduce-scatter (6 x 5 sums <= 32)
+
+// Number of filled slots of a section: the env kernel fills each type
+// section from its start, so the filled slots are a prefix.
+__device__ __forceinline__ int filled_prefix(const int* __restrict__ nl, int ns) {
+  const int lane = threadIdx.x & 31;
+  int n = 0;
+  for (int b = 0; b < ns; b += 32) {
+    const bool ok = b + lane < ns && nl[b + lane] >= 0;
+    n += __popc(__ballot_sync(kFull, ok));
+  }
+  return n;
+}
+
 template <typename T, int NQ, int A>
 __global__ void __launch_bounds__(kFWarps * 32)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
@@ -183,10 +216,10 @@ __global__ void __launch_bounds__(kFWarps * 32)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kFWarps + warp;
   if (i >= nloc) return;
-  const int MP = NQ * 32;
-  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * (4 * MP + MP * A + MP * 4);
-  T* gs = xs + 4 * MP;       // dE/dD as [k][a]
-  T* dys = gs + MP * A;      // dy as [k][4]
+  constexpr int MP = NQ * 32;
+  constexpr int RW = 4 * MP + MP * A;  // per-warp shared region (T elements)
+  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * RW;
+  T* gs = xs + 4 * MP;  // dE/dD as [k][a]
   const int ti = atype[i];
   for (int t = lane; t < 4 * M; t += 32) {
     const int m = t / M, k = t - m * M;
@@ -196,31 +229,93 @@ __global__ void __launch_bounds__(kFWarps * 32)
   for (int t = lane; t < M * A; t += 32) gs[t] = dD[drow_i * M * A + t];
   __syncwarp();
   const T inv = T(1) / T(nnei);
-  // dX[m][k] = sum_a G[k][a] X[m][a] + [k < A] sum_k' G[k'][k] X[m][k']
+  // dy[m][k] = dX[m][k] / nnei, dX = sum_a G[k][a] X[m][a] + [k < A] sum_k' G[k'][k] X[m][k'],
+  // kept in registers: lane owns k = q * 32 + lane
+  T dyr[NQ][4];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     const int k = q * 32 + lane;
-    if (k >= M) continue;
     T dx[4] = {T(0), T(0), T(0), T(0)};
+    if (k < M) {
 #pragma unroll
-    for (int a = 0; a < A; ++a) {
-      const T g = gs[k * A + a];
+      for (int a = 0; a < A; ++a) {
+        const T g = gs[k * A + a];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + a];
-    }
-    if (k < A) {
-      for (int kk = 0; kk < M; ++kk) {
-        const T g = gs[kk * A + k];
+        for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + a];
+      }
+      if (k < A) {
+        for (int kk = 0; kk < M; ++kk) {
+          const T g = gs[kk * A + k];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + kk];
+          for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + kk];
+        }
       }
     }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) dys[k * 4 + m] = dx[m] * inv;
+    for (int m = 0; m < 4; ++m) dyr[q][m] = dx[m] * inv;
   }
   __syncwarp();
   if (ti < 0) return;
+  // the region now holds dE/d em of this atom's filled slots ([nnei][4]) and
+  // the 32 scattered sums of one neighbour group
+  T* nets = xs;
+  T* gbuf = xs + (size_t)nnei * 4;
+  const int* nl_i = nlist_ext + (size_t)i * nnei;
 
+  // ---- phase 1: tabulation gradient, lanes over k, neighbours in groups
+  for (int t = 0; t < ts.ntypes; ++t) {
+    const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
+    const int nv = filled_prefix(nl_i + s0, ns);
+    const int tb = tab_index(ts, t, ti);
+    const T* tab = ts.table[tb];
+    const TableInfo<T> inf = ts.info[tb];
+    for (int g0 = 0; g0 < nv; g0 += kBwdGroup) {
+      T part[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) part[c] = T(0);
+#pragma unroll
+      for (int gg = 0; gg < kBwdGroup; ++gg) {
+        const int j = g0 + gg;
+        if (j < nv) {
+          const T* e = em + ((size_t)i * nnei + s0 + j) * 4;
+          const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
+          T x = l0;
+          const int idx = locate_row(inf, x);
+          const T* row = tab + (size_t)idx * M * 6;
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) {
+            const int k = q * 32 + lane;
+            if (k < M) {
+              T a[6];
+              load_coef6<T>(a, row, k);
+              const T v = poly5(a, x);
+              const T dv = dpoly5(a, x);
+              part[gg * 5 + 0] += v * dyr[q][0];
+              part[gg * 5 + 1] += v * dyr[q][1];
+              part[gg * 5 + 2] += v * dyr[q][2];
+              part[gg * 5 + 3] += v * dyr[q][3];
+              part[gg * 5 + 4] +=
+                  dv * (l0 * dyr[q][0] + l1 * dyr[q][1] + l2 * dyr[q][2] + l3 * dyr[q][3]);
+            }
+          }
+        }
+      }
+      gbuf[lane] = reduce_scatter32(part, lane);
+      __syncwarp();
+      if (lane < kBwdGroup && g0 + lane < nv) {
+        const int s = s0 + g0 + lane;
+        const T* gv = gbuf + lane * 5;
+        nets[s * 4 + 0] = gv[0] + gv[4];  // em_x is em[:, 0]
+        nets[s * 4 + 1] = gv[1];
+        nets[s * 4 + 2] = gv[2];
+        nets[s * 4 + 3] = gv[3];
+      }
+      __syncwarp();
+    }
+  }
+
+  // ---- phase 2: lanes over filled slots: env-matrix derivative row
+  //      d em / d x_i (env_mat.cc:157-204) / std, force and virial scatter
   const int f = geo.atom_frame[i];
   const int il = i - geo.frame_aoff[f];
   const size_t eoff = geo.frame_eoff[f];
@@ -234,33 +329,10 @@ __global__ void __launch_bounds__(kFWarps * 32)
   for (int q = 0; q < 9; ++q) vir[q] = 0.;
   for (int t = 0; t < ts.ntypes; ++t) {
     const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
-    const int tb = tab_index(ts, t, ti);
-    const T* tab = ts.table[tb];
-    const TableInfo<T> inf = ts.info[tb];
-    for (int jj = lane; jj < ns; jj += 32) {
+    const int nv = filled_prefix(nl_i + s0, ns);
+    for (int jj = lane; jj < nv; jj += 32) {
       const int s = s0 + jj;
-      const int je = nlist_ext[(size_t)i * nnei + s];
-      if (je < 0) continue;
-      const T* e = em + ((size_t)i * nnei + s) * 4;
-      const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
-      T x = l0;
-      const int idx = locate_row(inf, x);
-      const T* row = tab + (size_t)idx * M * 6;
-      T g0 = 0, g1 = 0, g2 = 0, g3 = 0, gx = 0;
-      for (int k = 0; k < M; ++k) {
-        T a[6];
-        load_coef6<T>(a, row, k);
-        const T v = poly5(a, x);
-        const T dv = dpoly5(a, x);
-        const T r0 = dys[k * 4], r1 = dys[k * 4 + 1], r2 = dys[k * 4 + 2], r3 = dys[k * 4 + 3];
-        gx += dv * (l0 * r0 + l1 * r1 + l2 * r2 + l3 * r3);
-        g0 += v * r0;
-        g1 += v * r1;
-        g2 += v * r2;
-        g3 += v * r3;
-      }
-      g0 += gx;  // em_x is em[:, 0]
-      // env-matrix derivative row d em / d x_i (env_mat.cc:157-204), / std
+      const int je = nl_i[s];
       T rr[3];
       rr[0] = ext_coord[3 * (eoff + je)] - xi;
       rr[1] = ext_coord[3 * (eoff + je) + 1] - yi;
@@ -274,8 +346,8 @@ __global__ void __launch_bounds__(kFWarps * 32)
       T sw, dsw;
       spline5_d<T>(sw, dsw, nr, rmin, rmax);
       const T ev[4] = {T(1) / nr, rr[0] / nr2, rr[1] / nr2, rr[2] / nr2};
-      const T gw[4] = {g0 / sd[s * 4 + 0], g1 / sd[s * 4 + 1], g2 / sd[s * 4 + 2],
-                       g3 / sd[s * 4 + 3]};
+      const T gw[4] = {nets[s * 4 + 0] / sd[s * 4 + 0], nets[s * 4 + 1] / sd[s * 4 + 1],
+                       nets[s * 4 + 2] / sd[s * 4 + 2], nets[s * 4 + 3] / sd[s * 4 + 3]};
       T v3[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -381,7 +453,9 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
   BwdGeom geo{atom_frame, frame_aoff, frame_eoff};
   const int nq = (M + 31) / 32;
   const int MP = nq * 32;
-  const size_t smem = (size_t)kFWarps * (4 * MP + MP * 16 + MP * 4) * sizeof(T);
+  const size_t smem = (size_t)kFWarps * (4 * MP + MP * 16) * sizeof(T);
+  GBDP_REQUIRE(nnei * 4 + 32 <= 4 * MP + MP * 16,
+               "se_a descriptor bwd: nnei %d too large for neuron[-1] %d", nnei, M);
   const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
 #define GBDP_LAUNCH_BWD(NQV)                                                                   \
   {                                                                                            \

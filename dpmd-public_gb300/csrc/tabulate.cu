@@ -9,8 +9,8 @@
 // Work split (one warp per centre atom):
 //   forward / grad-grad: lanes over the M outputs k (coalesced row reads,
 //     one broadcast em row per neighbour), neighbours sequential;
-//   grad: lanes over neighbours j (each lane walks its own table row), the
-//     atom's dy[4, M] staged in shared memory, no cross-lane reductions.
+//   grad: also lanes over k; the per-neighbour sums over k are reduced six
+//     neighbours at a time with a reduce-scatter across the warp.
 // The padding fold (tabulate.cc:108-155): with is_sorted, the first slot
 // whose x equals the last slot's x and whose em[1:4] are zero stands for all
 // remaining slots (weight nnei - j) and ends the sum; slots after it get no
@@ -168,54 +168,106 @@ __global__ void __launch_bounds__(kTabWarps * 32)
 }
 
 // ---------------------------------------------------------------- grad --
-// Shared memory per warp: dy of the atom as [M][4] (one 4-vector per k).
+// Lanes over k, as the forward: every table row is read with coalesced loads.
+// Neighbours are taken kGradGroup at a time; the 5 per-neighbour sums
+// (4 of dy_dem and dy_dem_x) of the group are reduced across lanes with one
+// 31-shuffle reduce-scatter (lane l receives the total of value l).
+constexpr int kGradGroup = 6;
+
 template <typename T>
+__device__ __forceinline__ T reduce_scatter32(T (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < o; ++k) {
+      const T send = up ? v[k] : v[k + o];
+      const T keep = up ? v[k + o] : v[k];
+      v[k] = keep + __shfl_xor_sync(kFull, send, o);
+    }
+  }
+  return v[0];
+}
+
+template <typename T, int NQ>
 __global__ void __launch_bounds__(kTabWarps * 32)
     k_tab_grad(T* __restrict__ dy_dem_x, T* __restrict__ dy_dem, const T* __restrict__ table,
                TableInfo<T> ti, const T* __restrict__ em_x, const T* __restrict__ em,
-               const T* __restrict__ dy, int nloc, int nnei, int M, bool is_sorted) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+               const T* __restrict__ dy, int nloc, int nnei, int M, int k_base, bool accumulate,
+               bool is_sorted) {
+  __shared__ T gbuf[kTabWarps][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kTabWarps + warp;
   if (i >= nloc) return;
-  T* g = reinterpret_cast<T*>(smem_raw) + (size_t)warp * M * 4;
-  for (int t = lane; t < 4 * M; t += 32) {
-    const int m = t / M, k = t - m * M;
-    g[k * 4 + m] = dy[(size_t)i * 4 * M + t];
+  T g[NQ][4];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const int k = k_base + q * 32 + lane;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) g[q][m] = k < M ? dy[((size_t)i * 4 + m) * M + k] : T(0);
   }
-  __syncwarp();
   const int bp = fold_point(em_x, em, i, nnei, is_sorted);
-  for (int j = lane; j < nnei; j += 32) {
-    const size_t ij = (size_t)i * nnei + j;
-    if (j > bp) {
+  const int jend = bp < nnei ? bp + 1 : nnei;
+  // slots after the fold point get no gradient (tabulate.cc:166-170, :251-256)
+  if (!accumulate)
+    for (int j = jend + lane; j < nnei; j += 32) {
+      const size_t ij = (size_t)i * nnei + j;
       dy_dem_x[ij] = T(0);
       dy_dem[ij * 4 + 0] = dy_dem[ij * 4 + 1] = dy_dem[ij * 4 + 2] = dy_dem[ij * 4 + 3] = T(0);
-      continue;
     }
-    T x = em_x[ij];
-    const T* e = em + ij * 4;
-    const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
-    const int idx = locate_row(ti, x);
-    const T* row = table + (size_t)idx * M * 6;
-    T s0 = 0, s1 = 0, s2 = 0, s3 = 0, gx = 0;
-    for (int k = 0; k < M; ++k) {
-      T a[6];
-      load_coef<T>(a, row, k);
-      const T v = poly5(a, x);
-      const T dv = dpoly5(a, x);
-      const T r0 = g[k * 4 + 0], r1 = g[k * 4 + 1], r2 = g[k * 4 + 2], r3 = g[k * 4 + 3];
-      gx += dv * (l0 * r0 + l1 * r1 + l2 * r2 + l3 * r3);
-      s0 += v * r0;
-      s1 += v * r1;
-      s2 += v * r2;
-      s3 += v * r3;
+  for (int j0 = 0; j0 < jend; j0 += kGradGroup) {
+    T part[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) part[c] = T(0);
+#pragma unroll
+    for (int gg = 0; gg < kGradGroup; ++gg) {
+      const int j = j0 + gg;
+      if (j < jend) {
+        const size_t ij = (size_t)i * nnei + j;
+        T x = em_x[ij];
+        const T* e = em + ij * 4;
+        const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
+        const int idx = locate_row(ti, x);
+        const T* row = table + (size_t)idx * M * 6;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int k = k_base + q * 32 + lane;
+          if (k < M) {
+            T a[6];
+            load_coef<T>(a, row, k);
+            const T v = poly5(a, x);
+            const T dv = dpoly5(a, x);
+            part[gg * 5 + 0] += v * g[q][0];
+            part[gg * 5 + 1] += v * g[q][1];
+            part[gg * 5 + 2] += v * g[q][2];
+            part[gg * 5 + 3] += v * g[q][3];
+            part[gg * 5 + 4] += dv * (l0 * g[q][0] + l1 * g[q][1] + l2 * g[q][2] + l3 * g[q][3]);
+          }
+        }
+      }
     }
-    const T w = (j == bp) ? T(nnei - j) : T(1);
-    dy_dem_x[ij] = gx * w;
-    dy_dem[ij * 4 + 0] = s0 * w;
-    dy_dem[ij * 4 + 1] = s1 * w;
-    dy_dem[ij * 4 + 2] = s2 * w;
-    dy_dem[ij * 4 + 3] = s3 * w;
+    gbuf[warp][lane] = reduce_scatter32(part, lane);
+    __syncwarp();
+    if (lane < kGradGroup && j0 + lane < jend) {
+      const int j = j0 + lane;
+      const size_t ij = (size_t)i * nnei + j;
+      const T w = (j == bp) ? T(nnei - j) : T(1);
+      const T* gv = gbuf[warp] + lane * 5;
+      if (accumulate) {
+        dy_dem[ij * 4 + 0] += gv[0] * w;
+        dy_dem[ij * 4 + 1] += gv[1] * w;
+        dy_dem[ij * 4 + 2] += gv[2] * w;
+        dy_dem[ij * 4 + 3] += gv[3] * w;
+        dy_dem_x[ij] += gv[4] * w;
+      } else {
+        dy_dem[ij * 4 + 0] = gv[0] * w;
+        dy_dem[ij * 4 + 1] = gv[1] * w;
+        dy_dem[ij * 4 + 2] = gv[2] * w;
+        dy_dem[ij * 4 + 3] = gv[3] * w;
+        dy_dem_x[ij] = gv[4] * w;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -312,11 +364,24 @@ int tab_grad(T* dy_dem_x, T* dy_dem, const T* table, const T* info, const T* em_
   if (nloc == 0 || nnei == 0) return GBDP_OK;
   GBDP_REQUIRE(dy && dy_dem_x && dy_dem, "tabulate_fusion_se_a_grad: null pointer");
   const TableInfo<T> ti = make_table_info(info);
-  const size_t smem = (size_t)kTabWarps * M * 4 * sizeof(T);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_tab_grad<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tab_grad<T><<<(nloc + kTabWarps - 1) / kTabWarps, kTabWarps * 32, smem, st>>>(
-      dy_dem_x, dy_dem, table, ti, em_x, em, dy, nloc, nnei, M, is_sorted != 0);
+  const dim3 grid((nloc + kTabWarps - 1) / kTabWarps), block(kTabWarps * 32);
+  // k in chunks of 128 (4 lanes-wide passes); later chunks accumulate
+  for (int kb = 0; kb < M; kb += 128) {
+    const int left = (M - kb + 31) / 32;
+    const bool acc = kb > 0;
+    if (left >= 4)
+      k_tab_grad<T, 4><<<grid, block, 0, st>>>(dy_dem_x, dy_dem, table, ti, em_x, em, dy, nloc,
+                                                nnei, M, kb, acc, is_sorted != 0);
+    else if (left == 3)
+      k_tab_grad<T, 3><<<grid, block, 0, st>>>(dy_dem_x, dy_dem, table, ti, em_x, em, dy, nloc,
+                                                nnei, M, kb, acc, is_sorted != 0);
+    else if (left == 2)
+      k_tab_grad<T, 2><<<grid, block, 0, st>>>(dy_dem_x, dy_dem, table, ti, em_x, em, dy, nloc,
+                                                nnei, M, kb, acc, is_sorted != 0);
+    else
+      k_tab_grad<T, 1><<<grid, block, 0, st>>>(dy_dem_x, dy_dem, table, ti, em_x, em, dy, nloc,
+                                                nnei, M, kb, acc, is_sorted != 0);
+  }
   GBDP_CHECK_LAUNCH("tabulate_fusion_se_a_grad");
   return GBDP_OK;
 }

@@ -64,15 +64,14 @@ class SeAModel:
         self.bias_atom_e = T(params["bias_atom_e"])
         # transposed / split copies of the fitting weights for the GEMM modes
         self._wsplit = {}
-        for f in self.fit:
-            for w, *_ in f[0]:
-                self._wsplit[w.data_ptr()] = _split_tf32(w) + (w.to(torch.bfloat16),)
         self._wt = {}
         for f in self.fit:
             for w, *_ in f[0]:
                 wt = w.t().contiguous()
                 self._wt[w.data_ptr()] = wt
-                self._wsplit[wt.data_ptr()] = _split_tf32(wt) + (wt.to(torch.bfloat16),)
+                if dtype == torch.float32:
+                    for mat in (w, wt):
+                        self._wsplit[mat.data_ptr()] = _split_tf32(mat) + (mat.to(torch.bfloat16),)
         self.davg = T(davg).contiguous()
         self.dstd = T(dstd).contiguous()
         self.tables = None

@@ -1,0 +1,41 @@
+"""Velocity-Verlet NVE on the fused step: the graph-captured step replays
+the eager integration, and total energy is conserved (FP64, 192 atoms,
+dt 0.5 fs, 200 steps: |E(t) - E(0)| / N <= 2e-5 eV)."""
+
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def test_nve_graph_matches_eager_and_conserves_energy(gb):
+    gb.load_library()
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    md = importlib.import_module("dpmd_public_gb300.md")
+    cfg = mdl.SeAConfig()
+    stat = [water.water_frame(4, 12.42, 3000 + s) for s in range(4)]
+    m = se_a.build_model(cfg, 23, stat, DEV, torch.float64)
+    c, t, b = water.water_frame(4, 12.42, 77)
+    v = md.maxwell_boltzmann(t, 330.0, 5)
+    eager = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.5)
+    for _ in range(5):
+        eager._step()
+    xe = eager.x.clone()
+    g = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.5)
+    g.capture()
+    g.run(5)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(g.x, xe, atol=1e-10, rtol=1e-10)
+    e0 = g.total_energy()
+    worst = 0.0
+    for _ in range(20):
+        g.run(10)
+        worst = max(worst, abs(g.total_energy() - e0) / len(t))
+    assert worst <= 2e-5, worst
+    assert g.batch.status() == 0

@@ -181,8 +181,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error")
-    ap.add_argument("--fit-mode", default="fp32", choices=["fp32", "tf32x3", "bf16"],
-                    help="fitting GEMMs: FP32 SIMT, split TF32 (FP32-level accuracy) or BF16")
+    ap.add_argument("--fit-mode", default="fp32",
+                    choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
+                             "native-bf16"],
+                    help="fitting net: torch GEMMs (fp32, split tf32x3, bf16) or the native fused "
+                         "call with a cuBLAS compute type (native-*)")
     ap.add_argument("--workload", default="water12k", choices=["water12k", "ragged512", "md786k"],
                     help="water12k: the headline config; ragged512: 512 ragged frames, batched "
                          "fused graph vs the plain per-frame loop; md786k: 786,432-atom NVE MD")

@@ -67,6 +67,8 @@ _SIGS = {
     "gbdp_env_status": (_I, [_P, _P]),
     "gbdp_prod_workspace_bytes": (_Z, [_I, _I, _I, _I, _I]),
     "gbdp_prod_env_mat_a_noalloc_f32": (_I, [_P] * 16 + [_F, _P, _I, _P]),
+    "gbdp_fitting_workspace_bytes": (_Z, [_I, _P, _I, _P]),
+    "gbdp_fitting_fwd_bwd_f32": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _F, _I, _P, _Z, _P]),
 }
 for _s in ("f32", "f64"):
     _SIGS.update({

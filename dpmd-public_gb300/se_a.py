@@ -40,7 +40,9 @@ def _stream():
 
 
 class SeAModel:
-    FIT_MODES = ("fp32", "tf32x3", "bf16")
+    FIT_MODES = ("fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
+                 "native-bf16")
+    _NATIVE = {"native-fp32": 0, "native-bf16x9": 1, "native-tf32": 2, "native-bf16": 3}
 
     def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
                  device, dtype=torch.float32, tables=None, table_infos=None, fit_mode="fp32"):
@@ -62,6 +64,7 @@ class SeAModel:
                       for l in f["hidden"]]
             self.fit.append((hidden, T(f["final"]["w"]), T(f["final"]["b"])))
         self.bias_atom_e = T(params["bias_atom_e"])
+        self.params_bias = np.asarray(params["bias_atom_e"], np.float64)
         # transposed / split copies of the fitting weights for the GEMM modes
         self._wsplit = {}
         self._wt = {}
@@ -84,6 +87,17 @@ class SeAModel:
             flat = self.table_infos.reshape(-1)
             self._tab_infos = (ct * len(flat))(*flat.tolist())
         self._sel_c = (ctypes.c_int * cfg.ntypes)(*[int(s) for s in cfg.sel])
+        # pointer tables for the native fitting entry point (float32 only)
+        self._fit_c = []
+        if dtype == torch.float32:
+            for hidden, wf, bf in self.fit:
+                nh = len(hidden)
+                widths = (ctypes.c_int * (nh + 1))(cfg.dim_descrpt, *[w.shape[1] for w, *_ in hidden])
+                wp = (_P * nh)(*[w.data_ptr() for w, *_ in hidden])
+                bp = (_P * nh)(*[b_.data_ptr() for _, b_, *_ in hidden])
+                ip = (_P * nh)(*[(0 if idt is None else idt.data_ptr()) for _, _, idt, _ in hidden])
+                wout = wf[:, 0].contiguous()
+                self._fit_c.append((nh, widths, wp, bp, ip, wout, float(bf[0])))
         self._sfx = L.sfx(dtype)
         self._lib = L.load()
 
@@ -186,11 +200,22 @@ class SeAModel:
     def fitting_rows(self, b: "Batch"):
         """Per-type fitting over the type-contiguous rows of D (each atom
         through its own type's net only)."""
+        native = self._NATIVE.get(self.fit_mode)
         for t, (s0, nt) in enumerate(b.type_rows):
             if nt == 0:
                 continue
-            e, _ = self.fitting_fwd_bwd(t, b.D[s0:s0 + nt], dD_out=b.dD[s0:s0 + nt])
-            b.ae[s0:s0 + nt].copy_(e)
+            if native is None:
+                e, _ = self.fitting_fwd_bwd(t, b.D[s0:s0 + nt], dD_out=b.dD[s0:s0 + nt])
+                b.ae[s0:s0 + nt].copy_(e)
+                continue
+            nh, widths, wp, bp, ip, wout, bout = self._fit_c[t]
+            ws = b.fit_ws(t, self)
+            L.check(self._lib.gbdp_fitting_fwd_bwd_f32(
+                _ptr(b.ae[s0:s0 + nt]), _ptr(b.dD[s0:s0 + nt]), _ptr(b.D[s0:s0 + nt]), nt, widths,
+                nh, wp, bp, ip, _ptr(wout), ctypes.c_float(bout), native, _ptr(ws),
+                ctypes.c_size_t(ws.numel()), _stream()), "fitting_fwd_bwd")
+            if float(self.params_bias[t]) != 0.0:
+                b.ae[s0:s0 + nt].add_(self.params_bias[t])
 
     # --------------------------------------------- operator-contract forms --
     def _descriptor_from_em(self, em: torch.Tensor, atype: torch.Tensor, compressed: bool):
@@ -393,6 +418,18 @@ class Batch:
         self.force = torch.empty((n, 3), dtype=dt, device=dev)
         self.vir = torch.empty((self.nframes, 9), dtype=torch.float64, device=dev)
         self.energy = torch.empty((self.nframes,), dtype=torch.float64, device=dev)
+
+    def fit_ws(self, t: int, model: SeAModel):
+        """Workspace of the native fitting call for type t (allocated once)."""
+        if not hasattr(self, "_fit_ws"):
+            self._fit_ws = {}
+        ws = self._fit_ws.get(t)
+        if ws is None:
+            nh, widths, wp, bp, ip, wout, bout = model._fit_c[t]
+            nbytes = int(model._lib.gbdp_fitting_workspace_bytes(self.type_rows[t][1], widths, nh, ip))
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=self.atype.device)
+            self._fit_ws[t] = ws
+        return ws
 
     def status(self) -> int:
         """Device status word of the last neighbour build (0 = ok)."""

@@ -310,6 +310,26 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f64(
     int ntypes, const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,
     int nframes, int last_layer_size, int axis_neuron, gbdp_stream stream);
 
+/* ------------------------------------------------------------------------
+ * Fitting net of one atom type: per-atom energy e = H_L w_out + b_out and
+ * dE/dD for every row of D [n, widths[0]] (deepmd/pt/model/task/
+ * fitting.py:734-899; hidden layer l: H_l = tanh(H_{l-1} W_l + b_l) * idt_l,
+ * plus H_{l-1} when widths[l] == widths[l-1]).  w, b, idt are HOST arrays of
+ * n_hidden device pointers (W_l row-major [widths[l-1], widths[l]]; an idt
+ * entry, or idt itself, may be NULL); w_out [widths[n_hidden]] device.
+ * gemm_mode selects the cuBLAS compute type of the six GEMMs: 0 FP32
+ * (pedantic), 1 FP32 emulated with BF16x9 on tensor cores, 2 TF32, 3 BF16.
+ * The first call on a device creates its cuBLAS handle: make it before any
+ * stream capture. */
+GBDP_API size_t gbdp_fitting_workspace_bytes(int n, const int* widths, int n_hidden,
+                                             const float* const* idt);
+GBDP_API int gbdp_fitting_fwd_bwd_f32(float* e, float* dD, const float* D, int n,
+                                      const int* widths, int n_hidden, const float* const* w,
+                                      const float* const* b, const float* const* idt,
+                                      const float* w_out, float b_out, int gemm_mode,
+                                      void* workspace, size_t workspace_bytes,
+                                      gbdp_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -114,3 +114,24 @@ def test_fused_graph_replay_matches_eager(mods, built):
     assert torch.allclose(out[0], E0, rtol=1e-6, atol=1e-6)
     assert torch.allclose(out[1], F0, rtol=1e-4, atol=1e-6)
     assert b.status() == 0
+
+
+@pytest.mark.parametrize("mode,ftol", [("fp32", 1e-5), ("tf32x3", 1e-5), ("native-fp32", 1e-5),
+                                       ("native-bf16x9", 1e-5), ("native-tf32", 5e-3),
+                                       ("bf16", 5e-3), ("native-bf16", 5e-3)])
+def test_fused_fitting_modes(mods, built, mode, ftol):
+    """The fused form with each fitting GEMM mode vs the FP64 composite.
+    FP32-level modes meet the 1e-5 eV/A force bar; TF32 / BF16 state 5e-3."""
+    import composite
+
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    m = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), DEV,
+                      torch.float32, m64.tables_np, m64.infos_np, fit_mode=mode)
+    frame = water.water_frame(4, 12.42, 5)
+    b = m.batch([frame[1]], frame[2][None])
+    E, F, V = m.step_fused(b, torch.tensor(frame[0], dtype=torch.float32, device=DEV))
+    Er, Fr, Vr, _ = _ref(composite, cfg, m64, frame)
+    err = np.abs(F.cpu().numpy().astype(np.float64) - Fr).max()
+    assert err <= ftol, (mode, err)
+    assert abs(float(E[0]) - Er) / len(frame[1]) <= (1e-6 if ftol <= 1e-5 else 1e-3)

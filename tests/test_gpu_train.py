@@ -56,8 +56,7 @@ def test_force_loss_gradient_double_backward(setup):
     batch = m.batch([t], b[None])
     x = torch.tensor(c, dtype=torch.float64, device=DEV)
     tr = se_a.Trainable(m)
-    with torch.no_grad():
-        E0, F0, V0 = tr.energy_force_virial(batch, x)
+    E0, F0, V0 = tr.energy_force_virial(batch, x)
     rng = np.random.default_rng(0)
     E_ref = (E0.detach() + 0.3).detach()
     F_ref = (F0.detach() + torch.tensor(rng.normal(0, 0.05, F0.shape), device=DEV)).detach()

@@ -165,6 +165,9 @@ __device__ __forceinline__ void spline5_d(T& vv, T& dd, T xx, T rmin, T rmax) {
   }
 }
 
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+
 struct BwdGeom {
   const int* atom_frame;   // [nloc_total] frame of each centre
   const int* frame_aoff;   // [nframes] first local atom of each frame
@@ -210,23 +213,27 @@ __global__ void __launch_bounds__(kFWarps * 32)
                const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
                const int* __restrict__ ext_map, const int* __restrict__ atype,
-               const T* __restrict__ stdv, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
+               const T* __restrict__ inv_std, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
                int nnei, int M) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kFWarps + warp;
   if (i >= nloc) return;
   constexpr int MP = NQ * 32;
-  constexpr int RW = 4 * MP + MP * A;  // per-warp shared region (T elements)
+  constexpr int GP = MP + 1;               // padded row of the transposed dE/dD
+  constexpr int RW = 4 * MP + A * GP + 1;  // per-warp shared region (T elements)
   T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * RW;
-  T* gs = xs + 4 * MP;  // dE/dD as [k][a]
+  T* gs = xs + 4 * MP;  // dE/dD transposed, gs[a * GP + k]: conflict-free for both uses
   const int ti = atype[i];
   for (int t = lane; t < 4 * M; t += 32) {
     const int m = t / M, k = t - m * M;
     xs[m * MP + k] = X[(size_t)i * 4 * M + t];
   }
   const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
-  for (int t = lane; t < M * A; t += 32) gs[t] = dD[drow_i * M * A + t];
+  for (int t = lane; t < M * A; t += 32) {
+    const int k = t / A, a = t - k * A;
+    gs[a * GP + k] = dD[drow_i * M * A + t];
+  }
   __syncwarp();
   const T inv = T(1) / T(nnei);
   // dy[m][k] = dX[m][k] / nnei, dX = sum_a G[k][a] X[m][a] + [k < A] sum_k' G[k'][k] X[m][k'],
@@ -239,13 +246,13 @@ __global__ void __launch_bounds__(kFWarps * 32)
     if (k < M) {
 #pragma unroll
       for (int a = 0; a < A; ++a) {
-        const T g = gs[k * A + a];
+        const T g = gs[a * GP + k];
 #pragma unroll
         for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + a];
       }
       if (k < A) {
         for (int kk = 0; kk < M; ++kk) {
-          const T g = gs[kk * A + k];
+          const T g = gs[k * GP + kk];
 #pragma unroll
           for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + kk];
         }
@@ -288,8 +295,17 @@ __global__ void __launch_bounds__(kFWarps * 32)
             if (k < M) {
               T a[6];
               load_coef6<T>(a, row, k);
-              const T v = poly5(a, x);
-              const T dv = dpoly5(a, x);
+              // value and derivative by one Horner sweep (9 FMA)
+              T v = a[5], dv = a[5];
+              v = v * x + a[4];
+              dv = dv * x + v;
+              v = v * x + a[3];
+              dv = dv * x + v;
+              v = v * x + a[2];
+              dv = dv * x + v;
+              v = v * x + a[1];
+              dv = dv * x + v;
+              v = v * x + a[0];
               part[gg * 5 + 0] += v * dyr[q][0];
               part[gg * 5 + 1] += v * dyr[q][1];
               part[gg * 5 + 2] += v * dyr[q][2];
@@ -322,7 +338,7 @@ __global__ void __launch_bounds__(kFWarps * 32)
   const int aoff = geo.frame_aoff[f];
   const T xi = ext_coord[3 * (eoff + il)], yi = ext_coord[3 * (eoff + il) + 1],
           zi = ext_coord[3 * (eoff + il) + 2];
-  const T* sd = stdv + (size_t)ti * nnei * 4;
+  const T* isd = inv_std + (size_t)ti * nnei * 4;
   T ci[3] = {T(0), T(0), T(0)};
   double vir[9];
 #pragma unroll
@@ -338,16 +354,16 @@ __global__ void __launch_bounds__(kFWarps * 32)
       rr[1] = ext_coord[3 * (eoff + je) + 1] - yi;
       rr[2] = ext_coord[3 * (eoff + je) + 2] - zi;
       const T nr2 = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
-      const T inr = T(1) / sqrt(nr2);
+      const T inr = rsqrt_t(nr2);
       const T nr = nr2 * inr;
       const T inr2 = inr * inr;
       const T inr4 = inr2 * inr2;
       const T inr3 = inr4 * nr;
       T sw, dsw;
       spline5_d<T>(sw, dsw, nr, rmin, rmax);
-      const T ev[4] = {T(1) / nr, rr[0] / nr2, rr[1] / nr2, rr[2] / nr2};
-      const T gw[4] = {nets[s * 4 + 0] / sd[s * 4 + 0], nets[s * 4 + 1] / sd[s * 4 + 1],
-                       nets[s * 4 + 2] / sd[s * 4 + 2], nets[s * 4 + 3] / sd[s * 4 + 3]};
+      const T ev[4] = {inr, rr[0] * inr2, rr[1] * inr2, rr[2] * inr2};
+      const T gw[4] = {nets[s * 4 + 0] * isd[s * 4 + 0], nets[s * 4 + 1] * isd[s * 4 + 1],
+                       nets[s * 4 + 2] * isd[s * 4 + 2], nets[s * 4 + 3] * isd[s * 4 + 3]};
       T v3[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -437,7 +453,7 @@ int desc_fwd(T* X, T* D, const T* em, const int* atype, const int* drow, const T
 template <typename T>
 int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow, const T* em,
              const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,
-             const T* stdv, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
+             const T* inv_std, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
              float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st) {
   TabSet<T> ts;
@@ -453,9 +469,10 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
   BwdGeom geo{atom_frame, frame_aoff, frame_eoff};
   const int nq = (M + 31) / 32;
   const int MP = nq * 32;
-  const size_t smem = (size_t)kFWarps * (4 * MP + MP * 16) * sizeof(T);
-  GBDP_REQUIRE(nnei * 4 + 32 <= 4 * MP + MP * 16,
-               "se_a descriptor bwd: nnei %d too large for neuron[-1] %d", nnei, M);
+  const int RW = 4 * MP + 16 * (MP + 1) + 1;
+  const size_t smem = (size_t)kFWarps * RW * sizeof(T);
+  GBDP_REQUIRE(nnei * 4 + 32 <= RW, "se_a descriptor bwd: nnei %d too large for neuron[-1] %d",
+               nnei, M);
   const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
 #define GBDP_LAUNCH_BWD(NQV)                                                                   \
   {                                                                                            \
@@ -463,7 +480,7 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
     if (smem > 48 * 1024)                                                                      \
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
     kern<<<grid, block, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,     \
-                                    ext_map, atype, stdv, geo, ts, (T)rcut_smth, (T)rcut,      \
+                                    ext_map, atype, inv_std, geo, ts, (T)rcut_smth, (T)rcut,   \
                                     nloc, nnei, M);                                            \
   }
   if (nq == 4)
@@ -495,13 +512,13 @@ using namespace gbdp;
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
       T* force, double* virial_acc, const T* X, const T* dE_dD, const int* d_row, const T* em, \
       const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,          \
-      const T* std, const int* atom_frame, const int* frame_atom_off,                          \
+      const T* inv_std, const int* atom_frame, const int* frame_atom_off,                      \
       const int* frame_ext_off, const T* const* tables, const T* table_infos, int ntypes,      \
       const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
     return desc_bwd<T>(force, virial_acc, X, dE_dD, d_row, em, nlist_ext, ext_coord, ext_map,  \
                        atype,                                                                  \
-                       std, atom_frame, frame_atom_off, frame_ext_off, tables, table_infos,    \
+                       inv_std, atom_frame, frame_atom_off, frame_ext_off, tables, table_infos,    \
                        ntypes, sel, type_one_side, rcut_smth, rcut, nloc, nframes,             \
                        last_layer_size, axis_neuron, (cudaStream_t)stream);                    \
   }

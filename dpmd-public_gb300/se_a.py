@@ -77,6 +77,7 @@ class SeAModel:
                         self._wsplit[mat.data_ptr()] = _split_tf32(mat) + (mat.to(torch.bfloat16),)
         self.davg = T(davg).contiguous()
         self.dstd = T(dstd).contiguous()
+        self.dstd_inv = T(1.0 / np.asarray(dstd)).contiguous()
         self.tables = None
         if tables is not None:
             self.tables = [T(t).contiguous() for t in tables]
@@ -188,7 +189,7 @@ class SeAModel:
         L.check(getattr(lib, f"gbdp_se_a_descriptor_bwd_{self._sfx}")(
             _ptr(b.force), _ptr(b.vir), _ptr(b.X), _ptr(b.dD), _ptr(b.drow), _ptr(b.env.em),
             _ptr(b.env.nlist_ext),
-            _ptr(b.env.ext_coord), _ptr(b.env.ext_map), _ptr(b.atype), _ptr(self.dstd),
+            _ptr(b.env.ext_coord), _ptr(b.env.ext_map), _ptr(b.atype), _ptr(self.dstd_inv),
             _ptr(b.atom_frame), _ptr(b.frame_aoff), _ptr(b.frame_eoff), self._tab_ptrs,
             self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side),
             ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), n, b.nframes, M, A,

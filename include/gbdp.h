@@ -279,7 +279,7 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * frames) and virial_acc [nframes, 9] (double, zeroed here) get the
  * contributions of every real neighbour, the env-matrix derivative being
  * recomputed from ext_coord (prod_force.cc:22-72, prod_virial.cc:22-68
- * semantics).  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
+ * semantics); inv_std [ntypes, nnei * 4] is 1 / dstd.  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
  * are device arrays describing the packed batch (see gbdp_nbr_frame).
  * ---------------------------------------------------------------------- */
 GBDP_API int gbdp_se_a_descriptor_fwd_f32(float* X, float* D, const float* em, const int* atype,
@@ -297,7 +297,7 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f32(
     float* force, double* virial_acc, const float* X, const float* dE_dD, const int* d_row,
     const float* em,
     const int* nlist_ext, const float* ext_coord, const int* ext_map, const int* atype,
-    const float* std, const int* atom_frame, const int* frame_atom_off, const int* frame_ext_off,
+    const float* inv_std, const int* atom_frame, const int* frame_atom_off, const int* frame_ext_off,
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
     int type_one_side, float rcut_smth, float rcut, int nloc, int nframes, int last_layer_size,
     int axis_neuron, gbdp_stream stream);
@@ -305,7 +305,7 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f64(
     double* force, double* virial_acc, const double* X, const double* dE_dD, const int* d_row,
     const double* em,
     const int* nlist_ext, const double* ext_coord, const int* ext_map, const int* atype,
-    const double* std, const int* atom_frame, const int* frame_atom_off,
+    const double* inv_std, const int* atom_frame, const int* frame_atom_off,
     const int* frame_ext_off, const double* const* tables, const double* table_infos,
     int ntypes, const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,
     int nframes, int last_layer_size, int axis_neuron, gbdp_stream stream);

@@ -1,6 +1,9 @@
 """Velocity-Verlet NVE on the fused step: the graph-captured step replays
-the eager integration, and total energy is conserved (FP64, 192 atoms,
-dt 0.5 fs, 200 steps: |E(t) - E(0)| / N <= 2e-5 eV)."""
+the eager integration, and total energy is conserved over a short run
+(FP64, 192 atoms, dt 0.25 fs, 40 steps: |E(t) - E(0)| / N <= 1e-5 eV).
+With random weights the potential has no short-range repulsion, so longer
+runs let atoms approach until the tables are clamped; the short window
+checks the integrator and the force/energy consistency only."""
 
 import importlib
 
@@ -23,19 +26,19 @@ def test_nve_graph_matches_eager_and_conserves_energy(gb):
     m = se_a.build_model(cfg, 23, stat, DEV, torch.float64)
     c, t, b = water.water_frame(4, 12.42, 77)
     v = md.maxwell_boltzmann(t, 330.0, 5)
-    eager = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.5)
+    eager = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.25)
     for _ in range(5):
         eager._step()
     xe = eager.x.clone()
-    g = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.5)
+    g = md.NVE(m, m.batch([t], b[None]), c, v, t, dt=0.25)
     g.capture()
     g.run(5)
     torch.cuda.synchronize()
     torch.testing.assert_close(g.x, xe, atol=1e-10, rtol=1e-10)
     e0 = g.total_energy()
     worst = 0.0
-    for _ in range(20):
-        g.run(10)
+    for _ in range(8):
+        g.run(5)
         worst = max(worst, abs(g.total_energy() - e0) / len(t))
-    assert worst <= 2e-5, worst
+    assert worst <= 1e-5, worst
     assert g.batch.status() == 0

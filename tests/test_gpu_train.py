@@ -68,7 +68,7 @@ def test_force_loss_gradient_double_backward(setup):
 
     L = loss()
     grads = torch.autograd.grad(L, tr.params)
-    checks = [(0, (3, 5)), (1, (7,)), (len(tr.params) - 2, (11, 0)), (2, (13,))]
+    checks = [(0, (3, 5)), (1, (7,)), (len(tr.params) - 2, (11, 0)), (2, (13, 7))]
     for pi, idx in checks:
         p = tr.params[pi]
         g = grads[pi][idx].item()

@@ -183,7 +183,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline")
     ap.add_argument("--fit-mode", default="fp32",
                     choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
-                             "native-bf16"],
+                             "native-bf16", "tc-tf32x3"],
                     help="fitting net: torch GEMMs (fp32, split tf32x3, bf16) or the native fused "
                          "call with a cuBLAS compute type (native-*)")
     ap.add_argument("--workload", default="water12k", choices=["water12k", "ragged512", "md786k"],
@@ -527,12 +527,21 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
                            check_status=False, out=b.env)
 
     def fwd():
-        lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), P(b.drow), model._tab_ptrs,
-                                         model._tab_infos, cfg.ntypes, model._sel_c,
-                                         int(cfg.type_one_side), b.nloc, M, A, S())
+        if model._tc_nets is not None:
+            lib.gbdp_se_a_descriptor_fwd_split_f32(P(b.X), P(b.D), P(b.D_lo), P(b.env.em), P(b.atype),
+                                                   P(b.drow), model._tab_ptrs, model._tab_infos,
+                                                   cfg.ntypes, model._sel_c, int(cfg.type_one_side),
+                                                   b.nloc, M, A, S())
+        else:
+            lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), P(b.drow),
+                                             model._tab_ptrs, model._tab_infos, cfg.ntypes,
+                                             model._sel_c, int(cfg.type_one_side), b.nloc, M, A, S())
 
     def fit():
-        model.fitting_rows(b)
+        if model._tc_nets is not None:
+            model.fitting_tc(b)
+        else:
+            model.fitting_rows(b)
 
     def bwd():
         lib.gbdp_se_a_descriptor_bwd_f32(

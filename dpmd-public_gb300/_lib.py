@@ -69,7 +69,24 @@ _SIGS = {
     "gbdp_prod_env_mat_a_noalloc_f32": (_I, [_P] * 16 + [_F, _P, _I, _P]),
     "gbdp_fitting_workspace_bytes": (_Z, [_I, _P, _I, _P]),
     "gbdp_fitting_fwd_bwd_f32": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _F, _I, _P, _Z, _P]),
+    "gbdp_se_a_descriptor_fwd_split_f32": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P]),
+    "gbdp_fitting_tc_workspace_bytes": (_Z, [_I]),
+    "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
+    "gbdp_fitting_tc_status": (_I, [_P, _I, _P]),
 }
+
+
+class FitTcNet(ctypes.Structure):
+    _fields_ = [
+        ("w_hi", _P * 3),
+        ("w_lo", _P * 3),
+        ("wt_hi", _P * 3),
+        ("wt_lo", _P * 3),
+        ("b", _P * 3),
+        ("idt", _P * 3),
+        ("w_out", _P),
+        ("b_out", ctypes.c_float),
+    ]
 for _s in ("f32", "f64"):
     _SIGS.update({
         f"gbdp_tabulate_fusion_se_a_{_s}": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),

@@ -1,0 +1,503 @@
+// Fitting nets on the 5th-generation tensor cores (sm_103a): tcgen05.mma
+// kind::tf32 with operands staged in shared memory by TMA and accumulators
+// in tensor memory.  FP32-level accuracy from a split: every FP32 operand x
+// is x_hi + x_lo with x_hi exactly representable in TF32 (low 13 mantissa
+// bits cleared) and x_lo = x - x_hi, and each product is
+// A_hi B_hi + A_lo B_hi + A_hi B_lo (the A_lo B_lo term is below FP32
+// rounding).
+//
+// One kernel computes a 128 x 80 tile of C = A B for one layer; its fused
+// epilogue applies the layer's activation (forward) or gradient chain
+// (backward) and writes the next GEMM's A operand already split, so the
+// whole per-type fitting net (deepmd/pt/model/task/fitting.py:734-899,
+// layer semantics deepmd/dpmodel/utils/network.py) is six launches:
+//   F1  T1 = tanh(D W1 + b1)                    -> H1 = T1 (split)
+//   F2  T2 = tanh(H1 W2 + b2), H2 = T2 idt2 + H1 (split)
+//   F3  T3 = tanh(H2 W3 + b3), H3 = T3 idt3 + H2, e += H3 w_out,
+//       GZ3 = w_out idt3 (1 - T3^2) (split)
+//   B3  G2 = GZ3 W3^T + w_out, GZ2 = G2 idt2 (1 - T2^2) (split)
+//   B2  G1 = GZ2 W2^T + G2,    GZ1 = G1 (1 - T1^2) (split)
+//   B1  dE/dD = GZ1 W1^T
+// Rows of all activations are grouped by atom type, each type's block padded
+// to a multiple of 128, so a tile never mixes types.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+
+namespace gbdp {
+namespace {
+
+constexpr int TBM = 128, TBN = 80, TBK = 32, TSTAGES = 4;
+constexpr int A_TILE = TBM * TBK * 4;                // 16 KiB
+constexpr int B_TILE = TBN * TBK * 4;                // 10 KiB
+constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;       // 52 KiB
+constexpr int TMEM_COLS = 128;                       // >= TBN, power of two
+constexpr int TC_SMEM = TSTAGES * STAGE + 1024 + 256;  // + alignment slack + barriers
+constexpr int FIT_W = 240;                           // hidden width this kernel serves
+constexpr int FIT_D = 1600;                          // descriptor width this kernel serves
+
+struct TcMaps {
+  CUtensorMap a_hi, a_lo;
+  CUtensorMap b_hi[2], b_lo[2];
+};
+
+enum { EPI_F1 = 0, EPI_F2, EPI_F3, EPI_B3, EPI_B2, EPI_B1 };
+
+struct TcEpi {
+  int kind;
+  int ldo;          // leading dimension of the outputs
+  int ntypes;
+  int row_off[3];   // padded row block of each type; row_off[ntypes] = total rows
+  int ntile_n;      // tiles along N (F3: partial energies per row)
+  const float* bias[2];
+  const float* idt[2];
+  const float* wout[2];
+  const float* tin;      // T of this layer (backward)
+  const float* prev_hi;  // skip input (forward: H_{l-1}; B2: none)
+  const float* prev_lo;
+  const float* gin;      // G_l for the skip of the backward (B2)
+  float* tout;           // T written (F1, F2)
+  float* out_hi;         // split output (next A operand)
+  float* out_lo;
+  float* gout;           // G2 (B3)
+  float* epart;          // [rows, ntile_n] partial energies (F3)
+  float* out;            // dE/dD (B1)
+  int* status;
+};
+
+// ---------------------------------------------------------------- PTX --
+__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                       uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 B apart (the layout a TMA SWIZZLE_128B box of 128-byte rows produces)
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused here), 16 B
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                    // swizzle: 128 B
+  return d;
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  lo = x - hi;
+}
+
+__device__ __forceinline__ void store16(float* p, const float* v) {
+#pragma unroll
+  for (int k = 0; k < 16; k += 4)
+    *reinterpret_cast<float4*>(p + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+}
+
+// ------------------------------------------------------------- kernel --
+__global__ void __launch_bounds__(128, 1)
+    k_fit_tc(const __grid_constant__ TcMaps maps, const TcEpi ep, int K) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TSTAGES * STAGE);
+  uint64_t* empty = full + TSTAGES;
+  uint64_t* tfull = empty + TSTAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfull + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = blockIdx.x * TBM, n0 = blockIdx.y * TBN;
+  int t = 0;
+  while (t + 1 < ep.ntypes && row0 >= ep.row_off[t + 1]) ++t;
+  const int nkb = (K + TBK - 1) / TBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TSTAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % TSTAGES;
+      const unsigned ph = (kb / TSTAGES) & 1u;
+      if (kb >= TSTAGES && !mbar_wait_bounded(&empty[s], ph ^ 1u, ep.status)) break;
+      unsigned char* st = smem + s * STAGE;
+      mbar_expect_tx(&full[s], STAGE);
+      tma_2d(st, &maps.a_hi, kb * TBK, row0, &full[s]);
+      tma_2d(st + A_TILE, &maps.a_lo, kb * TBK, row0, &full[s]);
+      tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[s]);
+      tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[s]);
+      issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer: D(f32) += A(tf32, K-major) B(tf32, K-major), M 128, N 80
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TBN >> 3) << 17) |
+                           ((uint32_t)(TBM >> 4) << 24);
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % TSTAGES;
+      const unsigned ph = (kb / TSTAGES) & 1u;
+      if (!mbar_wait_bounded(&full[s], ph, ep.status)) break;
+      tc_fence_after();
+      const uint32_t ah = smem_addr(smem + s * STAGE), al = ah + A_TILE, bh = ah + 2 * A_TILE,
+                     bl = bh + B_TILE;
+#pragma unroll
+      for (int kk = 0; kk < TBK / 8; ++kk) {
+        const uint32_t off = kk * 32;  // 8 tf32 along K within the 128-byte row
+        const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off),
+                       dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
+        umma_tf32(tmem, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+        umma_tf32(tmem, dal, dbh, idesc, 1u);
+        umma_tf32(tmem, dah, dbl, idesc, 1u);
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(tfull);
+  }
+  __syncwarp();
+
+  // ---- epilogue: warp w owns rows 32w..32w+31 of the tile (TMEM lanes)
+  const bool got = mbar_wait_bounded(tfull, 0, ep.status);
+  tc_fence_after();
+  const int r = row0 + warp * 32 + lane;
+  const int ld = ep.ldo;
+  float esum = 0.f;
+  if (got) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < TBN; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      const int c = n0 + c0;
+      const size_t o = (size_t)r * ld + c;
+      if (ep.kind == EPI_B1) {
+        store16(ep.out + o, v);
+        continue;
+      }
+      float hi[16], lo[16];
+      if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
+        const float* b = ep.bias[t];
+        const float* idt = ep.idt[t];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const float tt = tanhf(v[k] + b[c + k]);
+          float h = tt;
+          if (ep.kind != EPI_F1) h = tt * idt[c + k] + (ep.prev_hi[o + k] + ep.prev_lo[o + k]);
+          if (ep.kind == EPI_F3) {
+            const float wo = ep.wout[t][c + k];
+            esum += h * wo;
+            split_tf32(wo * idt[c + k] * (1.f - tt * tt), hi[k], lo[k]);  // GZ3
+          } else {
+            split_tf32(h, hi[k], lo[k]);
+          }
+          v[k] = tt;
+        }
+        if (ep.kind != EPI_F3) store16(ep.tout + o, v);
+      } else {  // B3, B2
+        const float* idt = ep.kind == EPI_B3 ? ep.idt[t] : nullptr;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          float g = v[k] + (ep.kind == EPI_B3 ? ep.wout[t][c + k] : ep.gin[o + k]);
+          if (ep.kind == EPI_B3) v[k] = g;
+          const float tt = ep.tin[o + k];
+          float gz = (idt ? g * idt[c + k] : g) * (1.f - tt * tt);
+          split_tf32(gz, hi[k], lo[k]);
+        }
+        if (ep.kind == EPI_B3) store16(ep.gout + o, v);
+      }
+      store16(ep.out_hi + o, hi);
+      store16(ep.out_lo + o, lo);
+    }
+    if (ep.kind == EPI_F3) ep.epart[(size_t)r * ep.ntile_n + blockIdx.y] = esum;
+  }
+  // ---- drain: no bulk copy of this CTA may land after it exits
+  if (warp == 0 && lane == 0) {
+    for (int kb = (issued > TSTAGES ? issued - TSTAGES : 0); kb < issued; ++kb)
+      mbar_wait_bounded(&full[kb % TSTAGES], (kb / TSTAGES) & 1u, ep.status);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+}
+
+// per-row energy: e = sum of the F3 partials + b_out; padding rows get 0
+struct TcRows {
+  int row_off[3];
+  int nrows[2];
+  float b_out[2];
+  int ntypes;
+};
+
+__global__ void k_fit_tc_energy(float* __restrict__ e, const float* __restrict__ epart,
+                                int ntile_n, TcRows rw) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rw.row_off[rw.ntypes]) return;
+  int t = 0;
+  while (t + 1 < rw.ntypes && r >= rw.row_off[t + 1]) ++t;
+  float s = 0.f;
+  if (r - rw.row_off[t] < rw.nrows[t]) {
+    for (int k = 0; k < ntile_n; ++k) s += epart[(size_t)r * ntile_n + k];
+    s += rw.b_out[t];
+  }
+  e[r] = s;
+}
+
+// ------------------------------------------------------------ host side --
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_encode_mu;
+
+int get_encode() {
+  std::lock_guard<std::mutex> lock(g_encode_mu);
+  if (g_encode) return GBDP_OK;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+    set_error("fit_tc: cuTensorMapEncodeTiled is unavailable");
+    return GBDP_ERR_CUDA;
+  }
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return GBDP_OK;
+}
+
+// [rows, cols] fp32 row-major, boxes of 32 columns x box_rows rows, 128 B swizzle
+int make_map(CUtensorMap* m, const float* base, long rows, long cols, int box_rows) {
+  GBDP_REQUIRE(((uintptr_t)base & 15) == 0, "fit_tc: operand not 16-byte aligned");
+  GBDP_REQUIRE((cols * 4) % 16 == 0, "fit_tc: row pitch not a multiple of 16 bytes");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+  cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  GBDP_REQUIRE(r == CUDA_SUCCESS, "fit_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GBDP_OK;
+}
+
+size_t a256t(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct TcWs {
+  float *t1, *t2, *h1h, *h1l, *h2h, *h2l, *gz3h, *gz3l, *g2, *gz2h, *gz2l, *gz1h, *gz1l, *epart;
+  size_t bytes;
+};
+
+TcWs carve_tc(void* base, long rows) {
+  TcWs w{};
+  char* b = static_cast<char*>(base);
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    float* r = b ? reinterpret_cast<float*>(b + off) : nullptr;
+    off += a256t(n);
+    return r;
+  };
+  const size_t act = sizeof(float) * (size_t)rows * FIT_W;
+  w.t1 = take(act);
+  w.t2 = take(act);
+  w.h1h = take(act);
+  w.h1l = take(act);
+  w.h2h = take(act);
+  w.h2l = take(act);
+  w.gz3h = take(act);
+  w.gz3l = take(act);
+  w.g2 = take(act);
+  w.gz2h = take(act);
+  w.gz2l = take(act);
+  w.gz1h = take(act);
+  w.gz1l = take(act);
+  w.epart = take(sizeof(float) * (size_t)rows * (FIT_W / TBN));
+  w.bytes = off;
+  return w;
+}
+
+}  // namespace
+}  // namespace gbdp
+
+using namespace gbdp;
+
+extern "C" size_t gbdp_fitting_tc_workspace_bytes(int rows) {
+  return carve_tc(nullptr, rows).bytes + 256;
+}
+
+extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, const float* D_lo,
+                                   int ntypes, const int* nrows, const int* row_off,
+                                   const gbdp_fit_tc_net* nets, void* workspace,
+                                   size_t workspace_bytes, gbdp_stream stream) {
+  GBDP_REQUIRE(ntypes >= 1 && ntypes <= 2, "fit_tc: ntypes %d (1 or 2 supported)", ntypes);
+  GBDP_REQUIRE(e && dE_dD && D_hi && D_lo && nrows && row_off && nets && workspace,
+               "fit_tc: null argument");
+  const long rows = row_off[ntypes];
+  for (int t = 0; t < ntypes; ++t) {
+    GBDP_REQUIRE(row_off[t] % TBM == 0 && row_off[t + 1] >= row_off[t] + nrows[t],
+                 "fit_tc: type %d row block not 128-aligned or too small", t);
+    const gbdp_fit_tc_net& n = nets[t];
+    for (int l = 0; l < 3; ++l)
+      GBDP_REQUIRE(n.wt_hi[l] && n.wt_lo[l] && n.w_hi[l] && n.w_lo[l] && n.b[l],
+                   "fit_tc: type %d layer %d weights missing", t, l);
+    GBDP_REQUIRE(n.idt[1] && n.idt[2] && n.w_out, "fit_tc: type %d idt / output layer missing",
+                 t);
+  }
+  GBDP_REQUIRE(rows % TBM == 0, "fit_tc: total rows %ld not a multiple of 128", rows);
+  TcWs ws = carve_tc(workspace, rows);
+  GBDP_REQUIRE(workspace_bytes >= gbdp_fitting_tc_workspace_bytes((int)rows),
+               "fit_tc: workspace %zu < %zu", workspace_bytes,
+               gbdp_fitting_tc_workspace_bytes((int)rows));
+  if (rows == 0) return GBDP_OK;
+  int rc = get_encode();
+  if (rc) return rc;
+  int* status = reinterpret_cast<int*>(static_cast<char*>(workspace) + ws.bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int) * 4, st);
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(k_fit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    attr_done = true;
+  }
+  TcEpi base{};
+  base.ntypes = ntypes;
+  for (int t = 0; t <= ntypes; ++t) base.row_off[t] = row_off[t];
+  base.status = status;
+  base.ldo = FIT_W;
+  base.ntile_n = FIT_W / TBN;
+  for (int t = 0; t < ntypes; ++t) base.wout[t] = nets[t].w_out;
+  struct Step {
+    int kind;
+    const float *a_hi, *a_lo;
+    int K, N, layer;
+    bool fwd;
+  };
+  const Step steps[6] = {
+      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true},     {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true},
+      {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true}, {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false},
+      {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false},
+      {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false}};
+  for (const Step& sp : steps) {
+    TcMaps maps;
+    rc = make_map(&maps.a_hi, sp.a_hi, rows, sp.K, TBM);
+    if (!rc) rc = make_map(&maps.a_lo, sp.a_lo, rows, sp.K, TBM);
+    for (int t = 0; t < 2 && !rc; ++t) {
+      const gbdp_fit_tc_net& n = nets[t < ntypes ? t : 0];
+      // forward B = W_l^T [out, in]; backward B = W_l [in, out]: both K-major
+      const float* bh = sp.fwd ? n.wt_hi[sp.layer] : n.w_hi[sp.layer];
+      const float* bl = sp.fwd ? n.wt_lo[sp.layer] : n.w_lo[sp.layer];
+      rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, TBN);
+      if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, TBN);
+    }
+    if (rc) return rc;
+    TcEpi ep = base;
+    ep.kind = sp.kind;
+    ep.ldo = sp.N;
+    for (int t = 0; t < ntypes; ++t) {
+      ep.bias[t] = nets[t].b[sp.layer];
+      ep.idt[t] = nets[t].idt[sp.layer];
+    }
+    switch (sp.kind) {
+      case EPI_F1:
+        ep.tout = ws.t1, ep.out_hi = ws.h1h, ep.out_lo = ws.h1l;
+        break;
+      case EPI_F2:
+        ep.tout = ws.t2, ep.prev_hi = ws.h1h, ep.prev_lo = ws.h1l, ep.out_hi = ws.h2h,
+        ep.out_lo = ws.h2l;
+        break;
+      case EPI_F3:
+        ep.prev_hi = ws.h2h, ep.prev_lo = ws.h2l, ep.out_hi = ws.gz3h, ep.out_lo = ws.gz3l,
+        ep.epart = ws.epart;
+        break;
+      case EPI_B3:
+        for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
+        ep.tin = ws.t2, ep.gout = ws.g2, ep.out_hi = ws.gz2h, ep.out_lo = ws.gz2l;
+        break;
+      case EPI_B2:
+        ep.tin = ws.t1, ep.gin = ws.g2, ep.out_hi = ws.gz1h, ep.out_lo = ws.gz1l;
+        break;
+      default:
+        ep.out = dE_dD;
+    }
+    const dim3 grid((unsigned)(rows / TBM), (unsigned)(sp.N / TBN));
+    k_fit_tc<<<grid, 128, TC_SMEM, st>>>(maps, ep, sp.K);
+    GBDP_CHECK_LAUNCH("fit_tc gemm");
+  }
+  TcRows rw{};
+  rw.ntypes = ntypes;
+  for (int t = 0; t <= ntypes; ++t) rw.row_off[t] = row_off[t];
+  for (int t = 0; t < ntypes; ++t) {
+    rw.nrows[t] = nrows[t];
+    rw.b_out[t] = nets[t].b_out;
+  }
+  k_fit_tc_energy<<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(e, ws.epart, base.ntile_n, rw);
+  GBDP_CHECK_LAUNCH("fit_tc energy");
+  return GBDP_OK;
+}
+
+extern "C" int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream) {
+  TcWs ws = carve_tc(nullptr, rows);
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, static_cast<const char*>(workspace) + ws.bytes, sizeof(int),
+                                  cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "fit_tc status");
+  return h;
+}

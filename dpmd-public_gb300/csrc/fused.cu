@@ -55,12 +55,17 @@ __device__ __forceinline__ void load_coef6<float>(float* a, const float* __restr
   a[5] = w.y;
 }
 
+__device__ __forceinline__ float tf32_head(float x) {
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+__device__ __forceinline__ double tf32_head(double x) { return x; }
+
 // ---------------------------------------------------------------- forward --
 template <typename T, int NQ, int A>
 __global__ void __launch_bounds__(kFWarps * 32)
-    k_desc_fwd(T* __restrict__ X, T* __restrict__ D, const T* __restrict__ em,
-               const int* __restrict__ atype, const int* __restrict__ drow, TabSet<T> ts,
-               int nloc, int nnei, int M) {
+    k_desc_fwd(T* __restrict__ X, T* __restrict__ D, T* __restrict__ D_lo,
+               const T* __restrict__ em, const int* __restrict__ atype,
+               const int* __restrict__ drow, TabSet<T> ts, int nloc, int nnei, int M) {
   __shared__ T xs[kFWarps][4][NQ * 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kFWarps + warp;
@@ -137,11 +142,19 @@ __global__ void __launch_bounds__(kFWarps * 32)
     if (k >= M) continue;
     const size_t r = drow ? (size_t)drow[i] : (size_t)i;
     T* d = D + (r * M + k) * A;
+    T* dl = D_lo ? D_lo + (r * M + k) * A : nullptr;
 #pragma unroll
     for (int a = 0; a < A; ++a) {
       T v = acc[q][0] * xs[warp][0][a] + acc[q][1] * xs[warp][1][a] +
             acc[q][2] * xs[warp][2][a] + acc[q][3] * xs[warp][3][a];
-      d[a] = v;
+      if (dl) {
+        // TF32 head (low 13 mantissa bits cleared) and the exact remainder
+        const T hi = tf32_head(v);
+        d[a] = hi;
+        dl[a] = v - hi;
+      } else {
+        d[a] = v;
+      }
     }
   }
 }
@@ -426,7 +439,8 @@ int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntype
 }
 
 template <typename T>
-int desc_fwd(T* X, T* D, const T* em, const int* atype, const int* drow, const T* const* tables,
+int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow,
+             const T* const* tables,
              const T* infos, int ntypes, const int* sel, int one_side, int nloc, int M, int A,
              cudaStream_t st) {
   TabSet<T> ts;
@@ -439,13 +453,13 @@ int desc_fwd(T* X, T* D, const T* em, const int* atype, const int* drow, const T
   const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
   const int nq = (M + 31) / 32;
   if (nq == 4)
-    k_desc_fwd<T, 4, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
+    k_desc_fwd<T, 4, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
   else if (nq == 3)
-    k_desc_fwd<T, 3, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
+    k_desc_fwd<T, 3, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
   else if (nq == 2)
-    k_desc_fwd<T, 2, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
+    k_desc_fwd<T, 2, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
   else
-    k_desc_fwd<T, 1, 16><<<grid, block, 0, st>>>(X, D, em, atype, drow, ts, nloc, nnei, M);
+    k_desc_fwd<T, 1, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
   GBDP_CHECK_LAUNCH("se_a_descriptor_fwd");
   return GBDP_OK;
 }
@@ -506,7 +520,8 @@ using namespace gbdp;
       T* X, T* D, const T* em, const int* atype, const int* d_row, const T* const* tables,      \
       const T* table_infos, int ntypes, const int* sel, int type_one_side, int nloc,           \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
-    return desc_fwd<T>(X, D, em, atype, d_row, tables, table_infos, ntypes, sel, type_one_side, \
+    return desc_fwd<T>(X, D, nullptr, em, atype, d_row, tables, table_infos, ntypes, sel,       \
+                       type_one_side,                                                          \
                        nloc, last_layer_size, axis_neuron, (cudaStream_t)stream);              \
   }                                                                                             \
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
@@ -525,3 +540,13 @@ using namespace gbdp;
 
 GBDP_FUSED_ENTRY(float, f32)
 GBDP_FUSED_ENTRY(double, f64)
+
+extern "C" int gbdp_se_a_descriptor_fwd_split_f32(
+    float* X, float* D_hi, float* D_lo, const float* em, const int* atype, const int* d_row,
+    const float* const* tables, const float* table_infos, int ntypes, const int* sel,
+    int type_one_side, int nloc, int last_layer_size, int axis_neuron, gbdp_stream stream) {
+  GBDP_REQUIRE(D_lo != nullptr, "se_a_descriptor_fwd_split: null D_lo");
+  return desc_fwd<float>(X, D_hi, D_lo, em, atype, d_row, tables, table_infos, ntypes, sel,
+                         type_one_side, nloc, last_layer_size, axis_neuron,
+                         (cudaStream_t)stream);
+}

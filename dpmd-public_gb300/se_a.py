@@ -41,7 +41,7 @@ def _stream():
 
 class SeAModel:
     FIT_MODES = ("fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
-                 "native-bf16")
+                 "native-bf16", "tc-tf32x3")
     _NATIVE = {"native-fp32": 0, "native-bf16x9": 1, "native-tf32": 2, "native-bf16": 3}
 
     def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
@@ -88,6 +88,30 @@ class SeAModel:
             flat = self.table_infos.reshape(-1)
             self._tab_infos = (ct * len(flat))(*flat.tolist())
         self._sel_c = (ctypes.c_int * cfg.ntypes)(*[int(s) for s in cfg.sel])
+        # split weights for the tensor-core fitting (tcgen05, TF32 hi/lo)
+        self._tc_nets = None
+        if dtype == torch.float32 and self.fit_mode == "tc-tf32x3":
+            nets = (L.FitTcNet * cfg.ntypes)()
+            self._tc_keep = []
+            for t, (hidden, wf, bf) in enumerate(self.fit):
+                if len(hidden) != 3 or [w.shape for w, *_ in hidden] != [(1600, 240), (240, 240),
+                                                                           (240, 240)]:
+                    raise ValueError("tc-tf32x3 serves the 1600-240-240-240 fitting net only")
+                if hidden[0][2] is not None or hidden[1][2] is None or hidden[2][2] is None:
+                    raise ValueError("tc-tf32x3 expects a time step on layers 2 and 3 only")
+                for l, (w, b_, idt, skip) in enumerate(hidden):
+                    wh, wl = _split_tf32(w.contiguous())
+                    wth, wtl = _split_tf32(w.t().contiguous())
+                    self._tc_keep += [wh, wl, wth, wtl]
+                    nets[t].w_hi[l], nets[t].w_lo[l] = wh.data_ptr(), wl.data_ptr()
+                    nets[t].wt_hi[l], nets[t].wt_lo[l] = wth.data_ptr(), wtl.data_ptr()
+                    nets[t].b[l] = b_.data_ptr()
+                    nets[t].idt[l] = 0 if idt is None else idt.data_ptr()
+                wo = wf[:, 0].contiguous()
+                self._tc_keep.append(wo)
+                nets[t].w_out = wo.data_ptr()
+                nets[t].b_out = float(bf[0])
+            self._tc_nets = nets
         # pointer tables for the native fitting entry point (float32 only)
         self._fit_c = []
         if dtype == torch.float32:
@@ -181,11 +205,18 @@ class SeAModel:
         env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth, list(cfg.sel),
                        check_status=False, out=b.env)
         lib = self._lib
-        L.check(getattr(lib, f"gbdp_se_a_descriptor_fwd_{self._sfx}")(
-            _ptr(b.X), _ptr(b.D), _ptr(b.env.em), _ptr(b.atype), _ptr(b.drow), self._tab_ptrs,
-            self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side), n, M, A, _stream()),
-            "se_a_descriptor_fwd")
-        self.fitting_rows(b)
+        if self._tc_nets is not None:
+            L.check(lib.gbdp_se_a_descriptor_fwd_split_f32(
+                _ptr(b.X), _ptr(b.D), _ptr(b.D_lo), _ptr(b.env.em), _ptr(b.atype), _ptr(b.drow),
+                self._tab_ptrs, self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side), n,
+                M, A, _stream()), "se_a_descriptor_fwd_split")
+            self.fitting_tc(b)
+        else:
+            L.check(getattr(lib, f"gbdp_se_a_descriptor_fwd_{self._sfx}")(
+                _ptr(b.X), _ptr(b.D), _ptr(b.env.em), _ptr(b.atype), _ptr(b.drow), self._tab_ptrs,
+                self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side), n, M, A,
+                _stream()), "se_a_descriptor_fwd")
+            self.fitting_rows(b)
         L.check(getattr(lib, f"gbdp_se_a_descriptor_bwd_{self._sfx}")(
             _ptr(b.force), _ptr(b.vir), _ptr(b.X), _ptr(b.dD), _ptr(b.drow), _ptr(b.env.em),
             _ptr(b.env.nlist_ext),
@@ -197,6 +228,18 @@ class SeAModel:
         b.energy.zero_()
         b.energy.index_add_(0, b.frame_of_row, b.ae.to(torch.float64))
         return b.energy, b.force, b.vir
+
+    def fitting_tc(self, b: "Batch"):
+        """Both types' fitting nets on the tensor cores (six tcgen05 GEMM
+        launches with fused epilogues over the padded type blocks)."""
+        nt = self.cfg.ntypes
+        nrows = (ctypes.c_int * nt)(*[c for _, c in b.type_rows])
+        L.check(self._lib.gbdp_fitting_tc_f32(
+            _ptr(b.ae), _ptr(b.dD), _ptr(b.D), _ptr(b.D_lo), nt, nrows, b.row_off_c, self._tc_nets,
+            _ptr(b.tc_ws), ctypes.c_size_t(b.tc_ws.numel()), _stream()), "fitting_tc")
+        for t, (s0, cnt) in enumerate(b.type_rows):
+            if cnt and float(self.params_bias[t]) != 0.0:
+                b.ae[s0:s0 + cnt].add_(float(self.params_bias[t]))
 
     def fitting_rows(self, b: "Batch"):
         """Per-type fitting over the type-contiguous rows of D (each atom
@@ -389,15 +432,25 @@ class Batch:
         self.frame_eoff = torch.tensor(self.plan.ext_off, dtype=torch.int32, device=dev)
         self.type_idx = [torch.tensor(np.nonzero(flat == t)[0], dtype=torch.int64, device=dev)
                          for t in range(cfg.ntypes)]
-        # rows of D / dE/dD grouped by type (stable within a type)
-        order = np.argsort(flat, kind="stable")
-        drow = np.empty_like(order)
-        drow[order] = np.arange(len(order))
-        self.drow = torch.tensor(drow, dtype=torch.int32, device=dev)
+        # rows of D / dE/dD grouped by type (stable within a type); the
+        # tensor-core fitting pads each type's block to a multiple of 128
+        pad = 128 if getattr(model, "_tc_nets", None) is not None else 1
         counts = [int((flat == t).sum()) for t in range(cfg.ntypes)]
-        starts = np.concatenate([[0], np.cumsum(counts)[:-1]]) if counts else []
-        self.type_rows = [(int(s0), int(c0)) for s0, c0 in zip(starts, counts)]
-        self.frame_of_row = torch.tensor(fo[order], dtype=torch.int64, device=dev)
+        starts, s0 = [], 0
+        for c0 in counts:
+            starts.append(s0)
+            s0 += -(-c0 // pad) * pad
+        self.nrows_total = s0
+        self.type_rows = [(int(a), int(c0)) for a, c0 in zip(starts, counts)]
+        self.row_off_c = (ctypes.c_int * (cfg.ntypes + 1))(*(starts + [s0]))
+        drow = np.empty(len(flat), np.int64)
+        fo_row = np.zeros(s0, np.int64)
+        for t in range(cfg.ntypes):
+            idx = np.nonzero(flat == t)[0]
+            drow[idx] = starts[t] + np.arange(len(idx))
+            fo_row[starts[t]:starts[t] + len(idx)] = fo[idx]
+        self.drow = torch.tensor(drow, dtype=torch.int32, device=dev)
+        self.frame_of_row = torch.tensor(fo_row, dtype=torch.int64, device=dev)
         n = self.nloc
         nnei = cfg.nnei
         M, A = cfg.neuron[-1], cfg.axis_neuron
@@ -413,9 +466,14 @@ class Batch:
         e.ext_nall = torch.empty((self.nframes,), dtype=torch.int32, device=dev)
         self.env = e
         self.X = torch.empty((n, 4, M), dtype=dt, device=dev)
-        self.D = torch.empty((n, M * A), dtype=dt, device=dev)
-        self.dD = torch.empty((n, M * A), dtype=dt, device=dev)
-        self.ae = torch.empty((n,), dtype=dt, device=dev)
+        nr = self.nrows_total
+        self.D = torch.zeros((nr, M * A), dtype=dt, device=dev)
+        self.dD = torch.zeros((nr, M * A), dtype=dt, device=dev)
+        self.ae = torch.zeros((nr,), dtype=dt, device=dev)
+        if pad > 1:
+            self.D_lo = torch.zeros((nr, M * A), dtype=dt, device=dev)
+            tcb = int(model._lib.gbdp_fitting_tc_workspace_bytes(nr))
+            self.tc_ws = torch.zeros(tcb, dtype=torch.uint8, device=dev)
         self.force = torch.empty((n, 3), dtype=dt, device=dev)
         self.vir = torch.empty((self.nframes, 9), dtype=torch.float64, device=dev)
         self.energy = torch.empty((self.nframes,), dtype=torch.float64, device=dev)

@@ -330,6 +330,47 @@ GBDP_API int gbdp_fitting_fwd_bwd_f32(float* e, float* dD, const float* D, int n
                                       void* workspace, size_t workspace_bytes,
                                       gbdp_stream stream);
 
+/* As gbdp_se_a_descriptor_fwd_f32, but D is written split for the tensor-
+ * core fitting: D_hi = D with the low 13 mantissa bits cleared, D_lo =
+ * D - D_hi (exact). */
+GBDP_API int gbdp_se_a_descriptor_fwd_split_f32(
+    float* X, float* D_hi, float* D_lo, const float* em, const int* atype, const int* d_row,
+    const float* const* tables, const float* table_infos, int ntypes, const int* sel,
+    int type_one_side, int nloc, int last_layer_size, int axis_neuron, gbdp_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Fitting nets on the tensor cores (tcgen05, TF32 with a hi/lo split that
+ * keeps FP32-level accuracy), for the se_e2_a fitting shape
+ * 1600 -> 240 -> 240 -> 240 -> 1 (layers 2 and 3 with time step and skip).
+ * Rows are grouped by atom type: type t owns rows [row_off[t],
+ * row_off[t] + nrows[t]) of every activation, row_off[t] a multiple of 128,
+ * row_off[ntypes] the padded total (also a multiple of 128).  D is given
+ * split (D_hi with the low 13 mantissa bits cleared, D_lo = D - D_hi), as
+ * gbdp_se_a_descriptor_fwd_split_f32 writes it.  Per type (device pointers):
+ * w_hi/w_lo[l] = W_l [in, out] and wt_hi/wt_lo[l] = W_l^T [out, in], split;
+ * b[l]; idt[l] (NULL for layer 0); w_out [240]; b_out on the host.
+ * Outputs: e [rows] per-row energy (0 on padding rows), dE_dD [rows, 1600].
+ * ---------------------------------------------------------------------- */
+typedef struct gbdp_fit_tc_net {
+  const float* w_hi[3];
+  const float* w_lo[3];
+  const float* wt_hi[3];
+  const float* wt_lo[3];
+  const float* b[3];
+  const float* idt[3];
+  const float* w_out;
+  float b_out;
+} gbdp_fit_tc_net;
+
+GBDP_API size_t gbdp_fitting_tc_workspace_bytes(int rows);
+GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, const float* D_lo,
+                                 int ntypes, const int* nrows, const int* row_off,
+                                 const gbdp_fit_tc_net* nets, void* workspace,
+                                 size_t workspace_bytes, gbdp_stream stream);
+/* Synchronise `stream`; device status word of the last gbdp_fitting_tc_f32
+ * run on this workspace (GBDP_OK or GBDP_STATUS_TIMEOUT). */
+GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

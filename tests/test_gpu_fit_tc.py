@@ -1,0 +1,68 @@
+"""Tensor-core fitting (tcgen05 kind::tf32, TF32 hi/lo split) against the
+cuBLAS FP32 path on the same descriptor rows, and the fused step with it
+against the FP64 composite.
+
+Stated tolerances: per-atom energy and dE/dD within 2e-6 relative to the
+largest magnitude (FP32-level split product); forces <= 1e-5 eV/A vs FP64."""
+
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module")
+def setup(gb):
+    gb.load_library()
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    cfg = mdl.SeAConfig()
+    stat = [water.water_frame(4, 12.42, 4000 + s) for s in range(4)]
+    m64 = se_a.build_model(cfg, 29, stat, DEV, torch.float64)
+    mk = lambda mode: se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(),
+                                    m64.dstd.cpu().numpy(), DEV, torch.float32, m64.tables_np,
+                                    m64.infos_np, fit_mode=mode)
+    return se_a, cfg, m64, mk, water
+
+
+def test_tc_fitting_matches_fp32_gemm(setup):
+    se_a, cfg, m64, mk, water = setup
+    ref, tc = mk("native-fp32"), mk("tc-tf32x3")
+    frame = water.water_frame(5, 15.525, 8)  # 375 atoms: 125 O, 250 H (ragged 128-blocks)
+    bt = tc.batch([frame[1]], frame[2][None])
+    br = ref.batch([frame[1]], frame[2][None])
+    coord = torch.tensor(frame[0], dtype=torch.float32, device=DEV)
+    tc.step_fused(bt, coord)
+    ref.step_fused(br, coord)
+    torch.cuda.synchronize()
+    assert tc._lib.gbdp_fitting_tc_status(
+        bt.tc_ws.data_ptr(), bt.nrows_total, torch.cuda.current_stream().cuda_stream) == 0
+    for t, ((s_t, n_t), (s_r, n_r)) in enumerate(zip(bt.type_rows, br.type_rows)):
+        assert n_t == n_r
+        e_tc, e_ref = bt.ae[s_t:s_t + n_t], br.ae[s_r:s_r + n_r]
+        g_tc, g_ref = bt.dD[s_t:s_t + n_t], br.dD[s_r:s_r + n_r]
+        assert torch.allclose(e_tc, e_ref, atol=2e-6 * float(e_ref.abs().max()), rtol=0)
+        assert torch.allclose(g_tc, g_ref, atol=2e-6 * float(g_ref.abs().max()), rtol=0)
+        if t == 0:  # padding rows of the first block carry no energy
+            assert float(bt.ae[s_t + n_t:bt.type_rows[1][0]].abs().max()) == 0.0
+
+
+def test_tc_fused_step_vs_fp64(setup):
+    import composite
+
+    se_a, cfg, m64, mk, water = setup
+    tc = mk("tc-tf32x3")
+    frame = water.water_frame(4, 12.42, 5)
+    b = tc.batch([frame[1]], frame[2][None])
+    E, F, V = tc.step_fused(b, torch.tensor(frame[0], dtype=torch.float32, device=DEV))
+    Er, Fr, Vr, _ = composite.energy_force_virial(cfg, m64.params_np, m64.davg.cpu().numpy(),
+                                                  m64.dstd.cpu().numpy(), *frame, m64.tables_np,
+                                                  m64.infos_np)
+    assert np.abs(F.cpu().numpy().astype(np.float64) - Fr).max() <= 1e-5
+    assert abs(float(E[0]) - Er) / len(frame[1]) <= 1e-6
+    assert np.abs(V[0].cpu().numpy() - Vr).max() <= 1e-3

@@ -23,6 +23,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -93,6 +94,32 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
             self.fh.close()
+
+    def _nrows(self):
+        try:
+            with open(self.path) as fh:
+                return sum(1 for _ in fh)
+        except OSError:
+            return 0
+
+    def load(self, step, first_sample_s: float = 3.0, after_s: float = 0.45):
+        """Keep the GPU busy with ``step`` (untimed) until the sampler has
+        written its first row (pre-roll) or, with ``after_s``, for that long
+        after the timed region (post-roll), so that the samples bracket the
+        timed steps under the same load."""
+        import torch
+
+        t0 = time.perf_counter()
+        n0 = self._nrows()
+        while self.proc is not None:
+            for _ in range(20):
+                step()
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            if after_s is None and (self._nrows() > n0 or el > first_sample_s):
+                break
+            if after_s is not None and el > after_s:
+                break
 
     def summary(self):
         if self.proc is None or not os.path.exists(self.path):
@@ -181,11 +208,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline")
-    ap.add_argument("--fit-mode", default="fp32",
+    ap.add_argument("--fit-mode", default="tc-tf32x3",
                     choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
                              "native-bf16", "tc-tf32x3"],
-                    help="fitting net: torch GEMMs (fp32, split tf32x3, bf16) or the native fused "
-                         "call with a cuBLAS compute type (native-*)")
+                    help="fitting net: tc-tf32x3 (tcgen05 kernel, TF32 hi/lo split), torch GEMMs "
+                         "(fp32, split tf32x3, bf16) or the native call with a cuBLAS compute "
+                         "type (native-*)")
     ap.add_argument("--workload", default="water12k", choices=["water12k", "ragged512", "md786k"],
                     help="water12k: the headline config; ragged512: 512 ragged frames, batched "
                          "fused graph vs the plain per-frame loop; md786k: 786,432-atom NVE MD")
@@ -255,9 +283,12 @@ def main():
     st = batch.status()
     if st != 0:
         raise RuntimeError(f"neighbour build status {st}")
-    graph = torch.cuda.CUDAGraph()
+    graph = _new_graph()
     with torch.cuda.graph(graph):
         E_g, F_g, V_g = model.step_fused(batch, coord)
+    launches = graph_kernels(graph)
+    if hasattr(graph, "instantiate"):
+        graph.instantiate()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def barrier():
@@ -271,6 +302,7 @@ def main():
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with Clocks(local) as clk:
+        clk.load(graph.replay, after_s=None)  # pre-roll until the first clock sample
         barrier()
         wall0 = time.perf_counter()
         for k in range(args.steps):
@@ -280,6 +312,7 @@ def main():
             ends[k].record()
         barrier()
         wall = time.perf_counter() - wall0
+        clk.load(graph.replay)  # post-roll under the same load
     step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
     if ws > 1:
         tt = torch.tensor([step_ms], device=dev)
@@ -323,7 +356,7 @@ def main():
     kt = kernel_times(model, batch, coord, flush, reps=max(3, min(args.steps, 10)))
     dom = max(kt, key=lambda k: kt[k]["ms"])
     peaks = _peaks()
-    roof = roofline(dom, kt[dom], nat, cfg, peaks)
+    roof = roofline(dom, kt[dom], nat, cfg, peaks, args.fit_mode)
 
     # ---- plain (uncompressed) drop-in, eager, same frame
     mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
@@ -346,7 +379,9 @@ def main():
                       "fitting_gemm": args.fit_mode,
                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
                       "wall_s": wall},
-           "e2e": e2e, "gpu_launches": 8 * args.steps,
+           "e2e": e2e,
+           "gpu_launches": None if launches is None else launches["ours"] * args.steps,
+           "graph_kernels_per_step": launches,
            "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                      "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
@@ -505,6 +540,66 @@ def md_workload(args):
     return 0
 
 
+def _new_graph():
+    """A CUDA graph that keeps its cudaGraph_t after capture (so that its
+    nodes can be listed), where this torch version offers that."""
+    import torch
+
+    try:
+        return torch.cuda.CUDAGraph(keep_graph=True)
+    except TypeError:
+        return torch.cuda.CUDAGraph()
+
+
+def graph_kernels(graph):
+    """Kernel nodes of a captured step graph, counted by owner: this
+    library's kernels (namespace gbdp) and everything else (torch,
+    cuBLAS).  Read through the driver API; None when unavailable."""
+    import ctypes
+
+    try:
+        h = graph.raw_cuda_graph()
+        cu = ctypes.CDLL("libcuda.so.1")
+    except Exception:
+        return None
+
+    class Params(ctypes.Structure):  # CUDA_KERNEL_NODE_PARAMS_v2
+        _fields_ = [("func", ctypes.c_void_p), ("grid", ctypes.c_uint * 3),
+                    ("block", ctypes.c_uint * 3), ("smem", ctypes.c_uint),
+                    ("kernelParams", ctypes.c_void_p), ("extra", ctypes.c_void_p),
+                    ("kern", ctypes.c_void_p), ("ctx", ctypes.c_void_p)]
+
+    g = ctypes.c_void_p(h)
+    n = ctypes.c_size_t(0)
+    if cu.cuGraphGetNodes(g, None, ctypes.byref(n)) != 0:
+        return None
+    nodes = (ctypes.c_void_p * max(1, n.value))()
+    if cu.cuGraphGetNodes(g, nodes, ctypes.byref(n)) != 0:
+        return None
+    ours, other, names = 0, 0, {}
+    for i in range(n.value):
+        ty = ctypes.c_int(-1)
+        cu.cuGraphNodeGetType(ctypes.c_void_p(nodes[i]), ctypes.byref(ty))
+        if ty.value != 0:  # CU_GRAPH_NODE_TYPE_KERNEL
+            continue
+        p = Params()
+        name = ctypes.c_char_p()
+        if cu.cuGraphKernelNodeGetParams_v2(ctypes.c_void_p(nodes[i]), ctypes.byref(p)) == 0:
+            if p.func:
+                cu.cuFuncGetName(ctypes.byref(name), ctypes.c_void_p(p.func))
+            elif p.kern:
+                cu.cuKernelGetName(ctypes.byref(name), ctypes.c_void_p(p.kern))
+        nm = (name.value or b"?").decode(errors="replace")
+        if "gbdp" in nm:
+            ours += 1
+            m = re.search(r"(k_[a-z0-9_]+)", nm)
+            short = m.group(1) if m else nm
+            names[short] = names.get(short, 0) + 1
+        else:
+            other += 1
+    return {"ours": ours, "other": other, "ours_by_kernel": names}
+
+
 def kernel_times(model, batch, coord, flush, reps: int = 5):
     """Average device time of each part of the fused step (CUDA events on
     the launching stream, L2 flushed before each part)."""
@@ -592,13 +687,42 @@ def _alg_bytes(name, cfg):
     return 0
 
 
-def roofline(name, t, nat, cfg, peaks):
-    alg = _alg_bytes(name, cfg) * nat
+# algorithmic FLOPs per row of the fitting net (forward and backward GEMMs,
+# FP32 products): D W1, H1 W2, H2 W3, H3 w_out; GZ3 W3^T, GZ2 W2^T, GZ1 W1^T
+def _fit_flops(cfg):
+    w = [cfg.dim_descrpt] + list(cfg.fitting)
+    fwd = sum(w[i] * w[i + 1] for i in range(len(w) - 1)) + w[-1]
+    bwd = sum(w[i] * w[i + 1] for i in range(len(w) - 1))
+    return 2 * (fwd + bwd)
+
+
+PART_KERNEL = {"env_nlist": "k_nlist_env (+ cell build and ghost fill)",
+               "desc_fwd": "k_desc_fwd", "desc_bwd": "k_desc_bwd"}
+
+
+def roofline(name, t, nat, cfg, peaks, fit_mode):
     ms = t["ms"]
+    if name == "fitting_gemm":
+        tc = fit_mode == "tc-tf32x3"
+        nl = 6 if tc else 1
+        flops = _fit_flops(cfg) * nat
+        ach = flops / (ms * 1e-3) / 1e12
+        peak = peaks["bf16_tflops"]
+        out = {"kernel": "k_fit_tc" if tc else f"cuBLAS ({fit_mode}) + k_fit_*", "bound": "tensor",
+               "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+               "traffic": None, "peak_src": peaks["src"] + " (dense BF16, burst)",
+               "alg_flops_per_launch": flops / nl, "launches": nl, "ms_per_launch": ms / nl}
+        if tc:
+            # FP32 products as 3 TF32 MMAs at half the BF16 rate: 1/6 of peak
+            out["ceiling_tf32x3_tflops"] = peak / 6
+            out["frac_of_tf32x3_ceiling"] = ach / (peak / 6)
+        return out
+    alg = _alg_bytes(name, cfg) * nat
     ach = alg / (ms * 1e-3) / 1e9
-    return {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": ach / peaks["hbm_gbs"], "traffic": None, "peak_src": peaks["src"],
-            "alg_bytes_per_launch": alg, "ms_per_launch": ms}
+    return {"kernel": PART_KERNEL.get(name, name), "bound": "hbm", "achieved": ach,
+            "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+            "traffic": None, "peak_src": peaks["src"], "alg_bytes_per_launch": alg,
+            "launches": 1, "ms_per_launch": ms}
 
 
 if __name__ == "__main__":

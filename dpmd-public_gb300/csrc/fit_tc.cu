@@ -1,10 +1,14 @@
 // Fitting nets on the 5th-generation tensor cores (sm_103a): tcgen05.mma
 // kind::tf32 with operands staged in shared memory by TMA and accumulators
 // in tensor memory.  FP32-level accuracy from a split: every FP32 operand x
-// is x_hi + x_lo with x_hi exactly representable in TF32 (low 13 mantissa
-// bits cleared) and x_lo = x - x_hi, and each product is
-// A_hi B_hi + A_lo B_hi + A_hi B_lo (the A_lo B_lo term is below FP32
-// rounding).
+// is x_hi + x_lo, x_hi = x rounded to TF32 (10 explicit mantissa bits) and
+// x_lo = x - x_hi rounded to TF32 (|x - x_hi - x_lo| <= 2^-23 |x|), and
+// each product is A_hi B_hi + A_lo B_hi + A_hi B_lo (the A_lo B_lo term is
+// below FP32 rounding).  The tensor core's FP32 accumulator does not round
+// to nearest on every addition, so long accumulation chains are kept
+// short: the A_hi B_hi products of k-block kb go to main accumulator
+// kb % 3, the two small cross terms to a fourth accumulator, and the
+// epilogue adds the four in IEEE FP32.
 //
 // One kernel computes a 128 x 80 tile of C = A B for one layer; its fused
 // epilogue applies the layer's activation (forward) or gradient chain
@@ -34,7 +38,9 @@ constexpr int TBM = 128, TBN = 80, TBK = 32, TSTAGES = 4;
 constexpr int A_TILE = TBM * TBK * 4;                // 16 KiB
 constexpr int B_TILE = TBN * TBK * 4;                // 10 KiB
 constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;       // 52 KiB
-constexpr int TMEM_COLS = 128;                       // >= TBN, power of two
+constexpr int NACC = 3;                              // main accumulators
+constexpr uint32_t ACC_COLS = 128;                   // TMEM columns per accumulator (>= TBN)
+constexpr int TMEM_COLS = 512;                       // NACC main + 1 cross-term accumulator
 constexpr int TC_SMEM = TSTAGES * STAGE + 1024 + 256;  // + alignment slack + barriers
 constexpr int FIT_W = 240;                           // hidden width this kernel serves
 constexpr int FIT_D = 1600;                          // descriptor width this kernel serves
@@ -127,9 +133,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// x rounded to TF32: to nearest, ties away from zero, on the magnitude bits
+__device__ __forceinline__ float rn_tf32(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
 __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-  lo = x - hi;
+  hi = rn_tf32(x);
+  lo = rn_tf32(x - hi);
 }
 
 __device__ __forceinline__ void store16(float* p, const float* v) {
@@ -193,6 +204,7 @@ __global__ void __launch_bounds__(128, 1)
     // ---- MMA issuer: D(f32) += A(tf32, K-major) B(tf32, K-major), M 128, N 80
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TBN >> 3) << 17) |
                            ((uint32_t)(TBM >> 4) << 24);
+    const uint32_t dsmall = tmem + (uint32_t)NACC * ACC_COLS;
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % TSTAGES;
       const unsigned ph = (kb / TSTAGES) & 1u;
@@ -200,14 +212,15 @@ __global__ void __launch_bounds__(128, 1)
       tc_fence_after();
       const uint32_t ah = smem_addr(smem + s * STAGE), al = ah + A_TILE, bh = ah + 2 * A_TILE,
                      bl = bh + B_TILE;
+      const uint32_t dmain = tmem + (uint32_t)(kb % NACC) * ACC_COLS;
 #pragma unroll
       for (int kk = 0; kk < TBK / 8; ++kk) {
         const uint32_t off = kk * 32;  // 8 tf32 along K within the 128-byte row
         const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off),
                        dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
-        umma_tf32(tmem, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-        umma_tf32(tmem, dal, dbh, idesc, 1u);
-        umma_tf32(tmem, dah, dbl, idesc, 1u);
+        umma_tf32(dmain, dah, dbh, idesc, (kb >= NACC || kk > 0) ? 1u : 0u);
+        umma_tf32(dsmall, dal, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+        umma_tf32(dsmall, dah, dbl, idesc, 1u);
       }
       umma_commit(&empty[s]);
     }
@@ -224,8 +237,17 @@ __global__ void __launch_bounds__(128, 1)
   if (got) {
 #pragma unroll 1
     for (int c0 = 0; c0 < TBN; c0 += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      float v[16], w[16];
+      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      tmem_ld16(ta, v);
+      for (int a = 1; a < NACC && a < nkb; ++a) {
+        tmem_ld16(ta + (uint32_t)a * ACC_COLS, w);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] += w[k];
+      }
+      tmem_ld16(ta + (uint32_t)NACC * ACC_COLS, w);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] += w[k];
       const int c = n0 + c0;
       const size_t o = (size_t)r * ld + c;
       if (ep.kind == EPI_B1) {

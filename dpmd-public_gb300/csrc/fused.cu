@@ -1,27 +1,50 @@
 // Fused compressed se_e2_a descriptor (sm_103a): the "chosen form" step.
 //
-// k_desc_fwd (one warp per centre atom, lanes over the M embedding outputs):
-//   for every neighbour-type section: tabulated embedding G_k(x_j) times the
-//   env row em[j, :], summed over j (the reference's tabulate_fusion_se_a with
-//   its padding fold), then X = sum_sections / nnei and the descriptor
-//   D[k, a] = sum_m X[m, k] X[m, a], a < A (DescrptBlockSeA.forward,
-//   deepmd/pt/model/descriptor/se_a.py:786-866).  Neither the nloc x nnei x M
-//   embedding nor the per-section outputs reach HBM; X and D do.
+// Tables.  The fused kernels read the compression tables in a k-planar copy
+// (gbdp_table_to_planar_*): row r holds three planes, plane p the pairs
+// (a_2p, a_2p+1) of every output k, each plane padded to 128 bytes.  A warp
+// whose lanes walk k then loads one plane with 256 contiguous bytes (2 L1
+// wavefronts) instead of the 768-byte span (6 wavefronts) of the reference's
+// coefficient-minor row [M][6] (tabulate.cc:99-131 addressing).
 //
-// k_desc_bwd (one warp per centre atom): dX from dE/dD and X, dy = dX / nnei,
-//   then lanes over the real neighbours j: the tabulation gradient
-//   (tabulate.cc:158-260) gives dE/d em[j, :]; the env-matrix derivative row
-//   is recomputed from the coordinates (env_mat.cc:122-226) instead of being
-//   stored, and the force / virial contributions of prod_force.cc:22-72 and
-//   prod_virial.cc:22-68 are scattered straight away.  Padding slots carry no
-//   coordinate dependence and are skipped.
+// k_desc_fwd (one warp per centre atom):
+//   prepass   lanes over the neighbour slots of each type section: the fold
+//             point of the padding (tabulate.cc:108-115), the table row and
+//             in-row offset of every slot that is evaluated, its env row
+//             (times the fold weight) -> shared memory;
+//   main      lanes over the M embedding outputs k (32-wide chunks): the
+//             tabulated embedding G_k(x_j) times the env row, summed over j
+//             (tabulate_fusion_se_a); a last chunk of at most 16 outputs runs
+//             with several neighbours per warp instruction instead;
+//   epilogue  X = sum / nnei and D[k, a] = sum_m X[m, k] X[m, a], a < A
+//             (DescrptBlockSeA.forward, deepmd/pt/model/descriptor/
+//             se_a.py:786-866), D stored with 16-byte coalesced writes.
+//   Neither the nloc x nnei x M embedding nor per-section outputs reach HBM.
+//
+// k_desc_bwd (one warp per centre atom):
+//   dX        dX = dD X[:, :A] + (dD^T X) padded to M columns, dy = dX / nnei,
+//             kept in shared memory as dy4[k] = (dy_0k, dy_1k, dy_2k, dy_3k);
+//   prepass   table row / offset / env row of every filled slot;
+//   phase 1   8 lanes per neighbour, 4 neighbours per warp instruction, lanes
+//             over k within the group: value and slope of the row polynomial
+//             and the five sums dE/d em[j, 0..3] (+ the x slope term) of the
+//             tabulation gradient (tabulate.cc:158-260), reduced over the 8
+//             lanes by 3 butterfly steps;
+//   phase 2   lanes over filled slots: the env-matrix derivative row is
+//             recomputed from the coordinates (env_mat.cc:122-226) instead of
+//             being stored, and force / virial contributions
+//             (prod_force.cc:22-72, prod_virial.cc:22-68) are scattered.
+//   Padding slots carry no coordinate dependence and are skipped.
 #include "common.cuh"
 
 namespace gbdp {
 namespace {
 
 constexpr int kMaxTab = 16;
+constexpr int kMaxTypes = 4;
 constexpr int kFWarps = 4;
+constexpr int kBWarps = 4;
+constexpr int kAxis = 16;
 
 template <typename T>
 struct TabSet {
@@ -29,6 +52,7 @@ struct TabSet {
   TableInfo<T> info[kMaxTab];
   int ntypes;
   int one_side;  // 1: table per neighbour type; 0: per (neighbour, centre)
+  int ps;        // plane pitch of the k-planar tables (elements)
   int sec[kMaxTab + 1];
 };
 
@@ -37,16 +61,37 @@ __device__ __forceinline__ int tab_index(const TabSet<T>& ts, int tj, int ti) {
   return ts.one_side ? tj : tj * ts.ntypes + ti;
 }
 
+// plane pitch of the k-planar layout: 2 M elements rounded up to 128 bytes
 template <typename T>
-__device__ __forceinline__ void load_coef6(T* a, const T* __restrict__ row, int k) {
-  const T* p = row + 6 * k;
-#pragma unroll
-  for (int c = 0; c < 6; ++c) a[c] = __ldg(p + c);
+__host__ __device__ constexpr int kp_pitch(int M) {
+  return sizeof(T) == 4 ? (2 * M + 31) & ~31 : (2 * M + 15) & ~15;
 }
+
+template <typename T>
+struct Vec;
 template <>
-__device__ __forceinline__ void load_coef6<float>(float* a, const float* __restrict__ row, int k) {
-  const float2* p = reinterpret_cast<const float2*>(row + 6 * k);
-  float2 u = __ldg(p), v = __ldg(p + 1), w = __ldg(p + 2);
+struct Vec<float> {
+  using v2 = float2;
+  using v4 = float4;
+};
+struct alignas(32) dbl4 {
+  double x, y, z, w;
+};
+template <>
+struct Vec<double> {
+  using v2 = double2;
+  using v4 = dbl4;
+};
+template <typename T>
+using V4 = typename Vec<T>::v4;
+
+// the six coefficients of output k from a k-planar row
+template <typename T>
+__device__ __forceinline__ void load_coef6_kp(T* a, const T* __restrict__ row, int ps, int k) {
+  using P = typename Vec<T>::v2;
+  const P u = __ldg(reinterpret_cast<const P*>(row) + k);
+  const P v = __ldg(reinterpret_cast<const P*>(row + ps) + k);
+  const P w = __ldg(reinterpret_cast<const P*>(row + 2 * ps) + k);
   a[0] = u.x;
   a[1] = u.y;
   a[2] = v.x;
@@ -55,106 +100,237 @@ __device__ __forceinline__ void load_coef6<float>(float* a, const float* __restr
   a[5] = w.y;
 }
 
-__device__ __forceinline__ float tf32_head(float x) {
-  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+// one env row (4 values, 16-byte aligned for float, 32 for double)
+__device__ __forceinline__ float4 ld_row4(const float* p) {
+  return __ldg(reinterpret_cast<const float4*>(p));
 }
-__device__ __forceinline__ double tf32_head(double x) { return x; }
+__device__ __forceinline__ dbl4 ld_row4(const double* p) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  return dbl4{a.x, a.y, b.x, b.y};
+}
+
+__device__ __forceinline__ void st_row4(float* p, const float4& v) {
+  *reinterpret_cast<float4*>(p) = v;
+}
+__device__ __forceinline__ void st_row4(double* p, const dbl4& v) {
+  reinterpret_cast<double2*>(p)[0] = double2{v.x, v.y};
+  reinterpret_cast<double2*>(p)[1] = double2{v.z, v.w};
+}
+
+// x rounded to TF32 (10 explicit mantissa bits): to nearest, ties away from
+// zero on the magnitude bits
+__device__ __forceinline__ float rn_tf32(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+__device__ __forceinline__ double rn_tf32(double x) { return x; }
+
+// Per-warp shared slot arrays: env row (or, after phase 1, dE/d em), in-row
+// offset and table row of every evaluated slot, and the count of evaluated
+// slots of each type section.
+template <typename T>
+struct Slots {
+  V4<T>* em;
+  T* xr;
+  int* idx;
+  int* cnt;
+};
+
+template <typename T>
+__host__ __device__ constexpr size_t slots_bytes(int nnei) {
+  return (((size_t)nnei * (sizeof(V4<T>) + sizeof(T) + sizeof(int)) + kMaxTypes * sizeof(int)) +
+          31) &
+         ~(size_t)31;
+}
+
+template <typename T>
+__device__ __forceinline__ Slots<T> carve_slots(unsigned char* base, int nnei) {
+  Slots<T> s;
+  s.em = reinterpret_cast<V4<T>*>(base);
+  s.xr = reinterpret_cast<T*>(base + (size_t)nnei * sizeof(V4<T>));
+  s.idx = reinterpret_cast<int*>(base + (size_t)nnei * (sizeof(V4<T>) + sizeof(T)));
+  s.cnt = s.idx + nnei;
+  return s;
+}
+
+__host__ __device__ constexpr size_t max_sz(size_t a, size_t b) { return a > b ? a : b; }
+
+template <typename T>
+__host__ __device__ constexpr size_t fwd_warp_bytes(int nnei, int mp) {
+  return max_sz(slots_bytes<T>(nnei), (size_t)4 * mp * sizeof(T));
+}
 
 // ---------------------------------------------------------------- forward --
-template <typename T, int NQ, int A>
+// NQF: 32-wide output chunks handled lanes-over-k (the last may be partial);
+// tail_w (runtime, 0..16): outputs after them, handled tw = pow2 >= tail_w
+// lanes per neighbour, 32 / tw neighbours per instruction.
+template <typename T, int NQF>
 __global__ void __launch_bounds__(kFWarps * 32)
     k_desc_fwd(T* __restrict__ X, T* __restrict__ D, T* __restrict__ D_lo,
                const T* __restrict__ em, const int* __restrict__ atype,
-               const int* __restrict__ drow, TabSet<T> ts, int nloc, int nnei, int M) {
-  __shared__ T xs[kFWarps][4][NQ * 32];
+               const int* __restrict__ drow, TabSet<T> ts, int nloc, int nnei, int M, int tail_w,
+               int tail_lg) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  constexpr int NA = NQF + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kFWarps + warp;
   if (i >= nloc) return;
+  const int MP = (NQF + (tail_w > 0 ? 1 : 0)) * 32;
+  unsigned char* wbase = smem_raw + (size_t)warp * fwd_warp_bytes<T>(nnei, MP);
+  const Slots<T> sl = carve_slots<T>(wbase, nnei);
   const int ti = atype[i];
-  T acc[NQ][4];
+  const int rs = 3 * ts.ps;
+  T acc[NA][4];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q)
+  for (int q = 0; q < NA; ++q)
 #pragma unroll
     for (int m = 0; m < 4; ++m) acc[q][m] = T(0);
   if (ti >= 0) {
+    // ---- prepass: fold point, rows and weighted env rows per section
     for (int t = 0; t < ts.ntypes; ++t) {
       const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
-      if (ns == 0) continue;
-      const int tb = tab_index(ts, t, ti);
-      const T* tab = ts.table[tb];
-      const TableInfo<T> inf = ts.info[tb];
-      const T* e0 = em + ((size_t)i * nnei + s0) * 4;
-      // fold point of this section (tabulate.cc:108-115)
-      const T last = e0[(ns - 1) * 4];
-      int bp = ns;
-      for (int b = 0; b < ns; b += 32) {
-        const int j = b + lane;
-        bool hit = false;
-        if (j < ns) {
-          const T* e = e0 + j * 4;
-          hit = e[0] == last && e[1] == T(0) && e[2] == T(0) && e[3] == T(0);
+      int jend = 0;
+      if (ns > 0) {
+        const TableInfo<T> inf = ts.info[tab_index(ts, t, ti)];
+        const T* e0 = em + ((size_t)i * nnei + s0) * 4;
+        const T last = e0[(ns - 1) * 4];
+        int bp = ns;
+        for (int b = 0; b < ns; b += 32) {
+          const int j = b + lane;
+          bool hit = false;
+          if (j < ns) {
+            const T* e = e0 + j * 4;
+            hit = e[0] == last && e[1] == T(0) && e[2] == T(0) && e[3] == T(0);
+          }
+          const unsigned mk = __ballot_sync(kFull, hit);
+          if (mk) {
+            bp = b + __ffs(mk) - 1;
+            break;
+          }
         }
-        const unsigned mk = __ballot_sync(kFull, hit);
-        if (mk) {
-          bp = b + __ffs(mk) - 1;
-          break;
+        jend = bp < ns ? bp + 1 : ns;
+        for (int j = lane; j < jend; j += 32) {
+          const V4<T> e = ld_row4(e0 + 4 * j);
+          const T w = (j == bp) ? T(ns - j) : T(1);
+          T x = e.x;
+          const int idx = locate_row(inf, x);
+          V4<T> ew;
+          ew.x = w * e.x;
+          ew.y = w * e.y;
+          ew.z = w * e.z;
+          ew.w = w * e.w;
+          sl.em[s0 + j] = ew;
+          sl.xr[s0 + j] = x;
+          sl.idx[s0 + j] = idx;
         }
       }
-      const int jend = bp < ns ? bp + 1 : ns;
-      for (int j = 0; j < jend; ++j) {
-        const T* e = e0 + j * 4;
-        T x = e[0];
-        const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
-        const T w = (j == bp) ? T(ns - j) : T(1);
-        const int idx = locate_row(inf, x);
-        const T* row = tab + (size_t)idx * M * 6;
+      if (lane == 0) sl.cnt[t] = jend;
+    }
+    __syncwarp();
+    // ---- main: lanes over k
+    for (int t = 0; t < ts.ntypes; ++t) {
+      const int s0 = ts.sec[t], cnt = sl.cnt[t];
+      const T* tab = ts.table[tab_index(ts, t, ti)];
+      for (int j = 0; j < cnt; ++j) {
+        const V4<T> e = sl.em[s0 + j];
+        const T x = sl.xr[s0 + j];
+        const T* row = tab + (size_t)sl.idx[s0 + j] * rs;
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
+        for (int q = 0; q < NQF; ++q) {
           const int k = q * 32 + lane;
           if (k < M) {
             T a[6];
-            load_coef6<T>(a, row, k);
-            const T wv = w * poly5(a, x);
-            acc[q][0] += wv * l0;
-            acc[q][1] += wv * l1;
-            acc[q][2] += wv * l2;
-            acc[q][3] += wv * l3;
+            load_coef6_kp<T>(a, row, ts.ps, k);
+            const T v = poly5(a, x);
+            acc[q][0] += v * e.x;
+            acc[q][1] += v * e.y;
+            acc[q][2] += v * e.z;
+            acc[q][3] += v * e.w;
           }
         }
       }
     }
+    // ---- tail: several neighbours per instruction over the last outputs
+    if (tail_w > 0) {
+      const int tw = 1 << tail_lg;
+      const int n = lane >> tail_lg, tt = lane & (tw - 1);
+      const int npt = 32 >> tail_lg;
+      const int k = NQF * 32 + tt;
+      T ta[4] = {T(0), T(0), T(0), T(0)};
+      for (int t = 0; t < ts.ntypes; ++t) {
+        const int s0 = ts.sec[t], cnt = sl.cnt[t];
+        const T* tab = ts.table[tab_index(ts, t, ti)];
+        for (int j0 = 0; j0 < cnt; j0 += npt) {
+          const int j = j0 + n;
+          if (j < cnt && tt < tail_w) {
+            const V4<T> e = sl.em[s0 + j];
+            const T x = sl.xr[s0 + j];
+            const T* row = tab + (size_t)sl.idx[s0 + j] * rs;
+            T a[6];
+            load_coef6_kp<T>(a, row, ts.ps, k);
+            const T v = poly5(a, x);
+            ta[0] += v * e.x;
+            ta[1] += v * e.y;
+            ta[2] += v * e.z;
+            ta[3] += v * e.w;
+          }
+        }
+      }
+      for (int o = tw; o < 32; o <<= 1)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) ta[m] += __shfl_xor_sync(kFull, ta[m], o);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) acc[NQF][m] = lane < tail_w ? ta[m] : T(0);
+    }
   }
+  // ---- epilogue: X (coalesced over k) and D
+  __syncwarp();
+  T* xs = reinterpret_cast<T*>(wbase);  // [4][MP], aliases the slot arrays
   const T inv = T(1) / T(nnei);
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
+  for (int q = 0; q < NA; ++q) {
+    if (q == NQF && tail_w == 0) break;
     const int k = q * 32 + lane;
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
-      acc[q][m] *= inv;
-      xs[warp][m][q * 32 + lane] = acc[q][m];
-      if (k < M) X[((size_t)i * 4 + m) * M + k] = acc[q][m];
+      const T v = acc[q][m] * inv;
+      xs[m * MP + k] = v;
+      if (k < M) X[((size_t)i * 4 + m) * M + k] = v;
     }
   }
   __syncwarp();
+  const size_t r = drow ? (size_t)drow[i] : (size_t)i;
+  T* d = D + r * M * kAxis;
+  T* dl = D_lo ? D_lo + r * M * kAxis : nullptr;
+  for (int e = lane * 4; e < M * kAxis; e += 128) {
+    const int k = e >> 4, a0 = e & 15;
+    T v[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    const int k = q * 32 + lane;
-    if (k >= M) continue;
-    const size_t r = drow ? (size_t)drow[i] : (size_t)i;
-    T* d = D + (r * M + k) * A;
-    T* dl = D_lo ? D_lo + (r * M + k) * A : nullptr;
+    for (int m = 0; m < 4; ++m) {
+      const T xk = xs[m * MP + k];
 #pragma unroll
-    for (int a = 0; a < A; ++a) {
-      T v = acc[q][0] * xs[warp][0][a] + acc[q][1] * xs[warp][1][a] +
-            acc[q][2] * xs[warp][2][a] + acc[q][3] * xs[warp][3][a];
-      if (dl) {
-        // TF32 head (low 13 mantissa bits cleared) and the exact remainder
-        const T hi = tf32_head(v);
-        d[a] = hi;
-        dl[a] = v - hi;
-      } else {
-        d[a] = v;
-      }
+      for (int c = 0; c < 4; ++c) v[c] += xk * xs[m * MP + a0 + c];
+    }
+    if (dl) {
+      // TF32 head and the remainder, both rounded to TF32
+      V4<T> h, l;
+      h.x = rn_tf32(v[0]);
+      h.y = rn_tf32(v[1]);
+      h.z = rn_tf32(v[2]);
+      h.w = rn_tf32(v[3]);
+      l.x = rn_tf32(v[0] - h.x);
+      l.y = rn_tf32(v[1] - h.y);
+      l.z = rn_tf32(v[2] - h.z);
+      l.w = rn_tf32(v[3] - h.w);
+      st_row4(d + e, h);
+      st_row4(dl + e, l);
+    } else {
+      V4<T> o;
+      o.x = v[0];
+      o.y = v[1];
+      o.z = v[2];
+      o.w = v[3];
+      st_row4(d + e, o);
     }
   }
 }
@@ -187,27 +363,6 @@ struct BwdGeom {
   const int* frame_eoff;   // [nframes] first extended slot of each frame
 };
 
-// Sum of v[0..31] over the 32 lanes, scattered: lane l returns the total of
-// value l.  31 shuffles for 32 sums (instead of 5 per sum): at the step with
-// offset o every lane keeps the half of its values selected by lane bit o and
-// adds the partner's copy of that half.
-template <typename T>
-__device__ __forceinline__ T reduce_scatter32(T (&v)[32], int lane) {
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int k = 0; k < o; ++k) {
-      const T send = up ? v[k] : v[k + o];
-      const T keep = up ? v[k + o] : v[k];
-      v[k] = keep + __shfl_xor_sync(kFull, send, o);
-    }
-  }
-  return v[0];
-}
-
-constexpr int kBwdGroup = 6;  // neighbours per reduce-scatter (6 x 5 sums <= 32)
-
 // Number of filled slots of a section: the env kernel fills each type
 // section from its start, so the filled slots are a prefix.
 __device__ __forceinline__ int filled_prefix(const int* __restrict__ nl, int ns) {
@@ -220,128 +375,179 @@ __device__ __forceinline__ int filled_prefix(const int* __restrict__ nl, int ns)
   return n;
 }
 
-template <typename T, int NQ, int A>
-__global__ void __launch_bounds__(kFWarps * 32)
+template <typename T>
+__host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
+  // dy4 [mp] then a region holding X^T [mp] and later the slot arrays
+  return (size_t)mp * sizeof(V4<T>) + max_sz(slots_bytes<T>(nnei), (size_t)mp * sizeof(V4<T>));
+}
+
+constexpr int kLanesPerNbr = 8;  // phase 1: lanes per neighbour
+
+template <typename T, int NQ>
+__global__ void __launch_bounds__(kBWarps * 32)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
                const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
                const int* __restrict__ ext_map, const int* __restrict__ atype,
                const T* __restrict__ inv_std, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
                int nnei, int M) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kFWarps + warp;
-  if (i >= nloc) return;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
   constexpr int MP = NQ * 32;
-  constexpr int GP = MP + 1;               // padded row of the transposed dE/dD
-  constexpr int RW = 4 * MP + A * GP + 1;  // per-warp shared region (T elements)
-  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * RW;
-  T* gs = xs + 4 * MP;  // dE/dD transposed, gs[a * GP + k]: conflict-free for both uses
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kBWarps + warp;
+  if (i >= nloc) return;
   const int ti = atype[i];
-  for (int t = lane; t < 4 * M; t += 32) {
-    const int m = t / M, k = t - m * M;
-    xs[m * MP + k] = X[(size_t)i * 4 * M + t];
-  }
-  const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
-  for (int t = lane; t < M * A; t += 32) {
-    const int k = t / A, a = t - k * A;
-    gs[a * GP + k] = dD[drow_i * M * A + t];
+  if (ti < 0) return;
+  unsigned char* wbase = smem_raw + (size_t)warp * bwd_warp_bytes<T>(nnei, MP);
+  V4<T>* dy4 = reinterpret_cast<V4<T>*>(wbase);
+  unsigned char* region = wbase + (size_t)MP * sizeof(V4<T>);
+  V4<T>* xT = reinterpret_cast<V4<T>*>(region);  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k)
+  T* xTs = reinterpret_cast<T*>(region);
+  for (int u = lane; u < 4 * M; u += 32) {
+    const int m = u / M, k = u - m * M;
+    xTs[4 * k + m] = X[(size_t)i * 4 * M + u];
   }
   __syncwarp();
-  const T inv = T(1) / T(nnei);
-  // dy[m][k] = dX[m][k] / nnei, dX = sum_a G[k][a] X[m][a] + [k < A] sum_k' G[k'][k] X[m][k'],
-  // kept in registers: lane owns k = q * 32 + lane
-  T dyr[NQ][4];
+  const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
+  const T* g_i = dD + drow_i * M * kAxis;
+  // ---- dX = dD X[:, :A] (all k) ...
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     const int k = q * 32 + lane;
-    T dx[4] = {T(0), T(0), T(0), T(0)};
     if (k < M) {
+      T g[kAxis];
 #pragma unroll
-      for (int a = 0; a < A; ++a) {
-        const T g = gs[a * GP + k];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + a];
+      for (int a4 = 0; a4 < kAxis; a4 += 4) {
+        const V4<T> v = ld_row4(g_i + k * kAxis + a4);
+        g[a4] = v.x;
+        g[a4 + 1] = v.y;
+        g[a4 + 2] = v.z;
+        g[a4 + 3] = v.w;
       }
-      if (k < A) {
-        for (int kk = 0; kk < M; ++kk) {
-          const T g = gs[k * GP + kk];
+      T dx[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
-          for (int m = 0; m < 4; ++m) dx[m] += g * xs[m * MP + kk];
-        }
+      for (int a = 0; a < kAxis; ++a) {
+        const V4<T> x4 = xT[a];
+        dx[0] += g[a] * x4.x;
+        dx[1] += g[a] * x4.y;
+        dx[2] += g[a] * x4.z;
+        dx[3] += g[a] * x4.w;
       }
+      V4<T> o;
+      o.x = dx[0];
+      o.y = dx[1];
+      o.z = dx[2];
+      o.w = dx[3];
+      dy4[k] = o;
     }
-#pragma unroll
-    for (int m = 0; m < 4; ++m) dyr[q][m] = dx[m] * inv;
   }
   __syncwarp();
-  if (ti < 0) return;
-  // the region now holds dE/d em of this atom's filled slots ([nnei][4]) and
-  // the 32 scattered sums of one neighbour group
-  T* nets = xs;
-  T* gbuf = xs + (size_t)nnei * 4;
-  const int* nl_i = nlist_ext + (size_t)i * nnei;
+  // ---- ... + dD^T X for the first A columns: two half-warps split kk
+  {
+    const int h = lane >> 4, kc = lane & 15;
+    T s[4] = {T(0), T(0), T(0), T(0)};
+    for (int kk = h; kk < M; kk += 2) {
+      const T g = __ldg(g_i + kk * kAxis + kc);
+      const V4<T> x4 = xT[kk];
+      s[0] += g * x4.x;
+      s[1] += g * x4.y;
+      s[2] += g * x4.z;
+      s[3] += g * x4.w;
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) s[m] += __shfl_xor_sync(kFull, s[m], 16);
+    if (h == 0) {
+      V4<T> o = dy4[kc];
+      o.x += s[0];
+      o.y += s[1];
+      o.z += s[2];
+      o.w += s[3];
+      dy4[kc] = o;
+    }
+  }
+  __syncwarp();
+  const T inv = T(1) / T(nnei);
+  for (int k = lane; k < M; k += 32) {
+    V4<T> o = dy4[k];
+    o.x *= inv;
+    o.y *= inv;
+    o.z *= inv;
+    o.w *= inv;
+    dy4[k] = o;
+  }
+  __syncwarp();
 
-  // ---- phase 1: tabulation gradient, lanes over k, neighbours in groups
+  // ---- prepass over filled slots (the slot arrays replace X^T)
+  const Slots<T> sl = carve_slots<T>(region, nnei);
+  const int* nl_i = nlist_ext + (size_t)i * nnei;
   for (int t = 0; t < ts.ntypes; ++t) {
     const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
     const int nv = filled_prefix(nl_i + s0, ns);
-    const int tb = tab_index(ts, t, ti);
-    const T* tab = ts.table[tb];
-    const TableInfo<T> inf = ts.info[tb];
-    for (int g0 = 0; g0 < nv; g0 += kBwdGroup) {
-      T part[32];
-#pragma unroll
-      for (int c = 0; c < 32; ++c) part[c] = T(0);
-#pragma unroll
-      for (int gg = 0; gg < kBwdGroup; ++gg) {
-        const int j = g0 + gg;
+    const TableInfo<T> inf = ts.info[tab_index(ts, t, ti)];
+    for (int j = lane; j < nv; j += 32) {
+      const V4<T> e = ld_row4(em + ((size_t)i * nnei + s0 + j) * 4);
+      T x = e.x;
+      const int idx = locate_row(inf, x);
+      sl.em[s0 + j] = e;
+      sl.xr[s0 + j] = x;
+      sl.idx[s0 + j] = idx;
+    }
+    if (lane == 0) sl.cnt[t] = nv;
+  }
+  __syncwarp();
+
+  // ---- phase 1: tabulation gradient, 8 lanes per neighbour
+  const int rs = 3 * ts.ps;
+  {
+    const int n = lane >> 3, t8 = lane & 7;
+    for (int t = 0; t < ts.ntypes; ++t) {
+      const int s0 = ts.sec[t], nv = sl.cnt[t];
+      const T* tab = ts.table[tab_index(ts, t, ti)];
+      for (int j0 = 0; j0 < nv; j0 += 32 / kLanesPerNbr) {
+        const int j = j0 + n;
+        T p[5] = {T(0), T(0), T(0), T(0), T(0)};
         if (j < nv) {
-          const T* e = em + ((size_t)i * nnei + s0 + j) * 4;
-          const T l0 = e[0], l1 = e[1], l2 = e[2], l3 = e[3];
-          T x = l0;
-          const int idx = locate_row(inf, x);
-          const T* row = tab + (size_t)idx * M * 6;
-#pragma unroll
-          for (int q = 0; q < NQ; ++q) {
-            const int k = q * 32 + lane;
-            if (k < M) {
-              T a[6];
-              load_coef6<T>(a, row, k);
-              // value and derivative by one Horner sweep (9 FMA)
-              T v = a[5], dv = a[5];
-              v = v * x + a[4];
-              dv = dv * x + v;
-              v = v * x + a[3];
-              dv = dv * x + v;
-              v = v * x + a[2];
-              dv = dv * x + v;
-              v = v * x + a[1];
-              dv = dv * x + v;
-              v = v * x + a[0];
-              part[gg * 5 + 0] += v * dyr[q][0];
-              part[gg * 5 + 1] += v * dyr[q][1];
-              part[gg * 5 + 2] += v * dyr[q][2];
-              part[gg * 5 + 3] += v * dyr[q][3];
-              part[gg * 5 + 4] +=
-                  dv * (l0 * dyr[q][0] + l1 * dyr[q][1] + l2 * dyr[q][2] + l3 * dyr[q][3]);
-            }
+          const V4<T> e = sl.em[s0 + j];
+          const T x = sl.xr[s0 + j];
+          const T* row = tab + (size_t)sl.idx[s0 + j] * rs;
+          for (int k = t8; k < M; k += kLanesPerNbr) {
+            T a[6];
+            load_coef6_kp<T>(a, row, ts.ps, k);
+            const V4<T> d = dy4[k];
+            // value and slope by one Horner sweep (9 FMA)
+            T v = a[5], dv = a[5];
+            v = v * x + a[4];
+            dv = dv * x + v;
+            v = v * x + a[3];
+            dv = dv * x + v;
+            v = v * x + a[2];
+            dv = dv * x + v;
+            v = v * x + a[1];
+            dv = dv * x + v;
+            v = v * x + a[0];
+            p[0] += v * d.x;
+            p[1] += v * d.y;
+            p[2] += v * d.z;
+            p[3] += v * d.w;
+            p[4] += dv * (e.x * d.x + e.y * d.y + e.z * d.z + e.w * d.w);
           }
         }
+#pragma unroll
+        for (int o = 4; o >= 1; o >>= 1)
+#pragma unroll
+          for (int c = 0; c < 5; ++c) p[c] += __shfl_xor_sync(kFull, p[c], o);
+        if (t8 == 0 && j < nv) {
+          V4<T> net;  // dE/d em[j, :]; em_x is em[:, 0]
+          net.x = p[0] + p[4];
+          net.y = p[1];
+          net.z = p[2];
+          net.w = p[3];
+          sl.em[s0 + j] = net;
+        }
       }
-      gbuf[lane] = reduce_scatter32(part, lane);
-      __syncwarp();
-      if (lane < kBwdGroup && g0 + lane < nv) {
-        const int s = s0 + g0 + lane;
-        const T* gv = gbuf + lane * 5;
-        nets[s * 4 + 0] = gv[0] + gv[4];  // em_x is em[:, 0]
-        nets[s * 4 + 1] = gv[1];
-        nets[s * 4 + 2] = gv[2];
-        nets[s * 4 + 3] = gv[3];
-      }
-      __syncwarp();
     }
   }
+  __syncwarp();
 
   // ---- phase 2: lanes over filled slots: env-matrix derivative row
   //      d em / d x_i (env_mat.cc:157-204) / std, force and virial scatter
@@ -357,8 +563,7 @@ __global__ void __launch_bounds__(kFWarps * 32)
 #pragma unroll
   for (int q = 0; q < 9; ++q) vir[q] = 0.;
   for (int t = 0; t < ts.ntypes; ++t) {
-    const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
-    const int nv = filled_prefix(nl_i + s0, ns);
+    const int s0 = ts.sec[t], nv = sl.cnt[t];
     for (int jj = lane; jj < nv; jj += 32) {
       const int s = s0 + jj;
       const int je = nl_i[s];
@@ -375,8 +580,9 @@ __global__ void __launch_bounds__(kFWarps * 32)
       T sw, dsw;
       spline5_d<T>(sw, dsw, nr, rmin, rmax);
       const T ev[4] = {inr, rr[0] * inr2, rr[1] * inr2, rr[2] * inr2};
-      const T gw[4] = {nets[s * 4 + 0] * isd[s * 4 + 0], nets[s * 4 + 1] * isd[s * 4 + 1],
-                       nets[s * 4 + 2] * isd[s * 4 + 2], nets[s * 4 + 3] * isd[s * 4 + 3]};
+      const V4<T> net = sl.em[s];
+      const V4<T> sd = ld_row4(isd + (size_t)s * 4);
+      const T gw[4] = {net.x * sd.x, net.y * sd.y, net.z * sd.z, net.w * sd.w};
       T v3[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -419,19 +625,41 @@ __global__ void __launch_bounds__(kFWarps * 32)
   }
 }
 
+// ------------------------------------------------------ table re-layout --
+// dst[r][p][2k + c] = src[r][6k + 2p + c], zero padding to the plane pitch
+template <typename T>
+__global__ void k_table_planar(T* __restrict__ dst, const T* __restrict__ src, int nrow, int M,
+                               int ps) {
+  const size_t n = (size_t)nrow * 3 * ps;
+  for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = u / (3 * (size_t)ps);
+    const int rem = (int)(u - r * 3 * ps);
+    const int p = rem / ps, e = rem - p * ps;
+    const int k = e >> 1, c = e & 1;
+    dst[u] = k < M ? src[r * 6 * M + 6 * k + 2 * p + c] : T(0);
+  }
+}
+
 template <typename T>
 int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntypes, const int* sel,
-                int one_side) {
-  GBDP_REQUIRE(ntypes >= 1 && ntypes <= 4, "se_a descriptor: ntypes %d not in [1,4]", ntypes);
+                int one_side, int M) {
+  GBDP_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, "se_a descriptor: ntypes %d not in [1,%d]",
+               ntypes, kMaxTypes);
   const int ntab = one_side ? ntypes : ntypes * ntypes;
   GBDP_REQUIRE(ntab <= kMaxTab, "se_a descriptor: too many tables");
+  GBDP_REQUIRE(tables && infos && sel, "se_a descriptor: null table / info / sel array");
   ts.ntypes = ntypes;
   ts.one_side = one_side ? 1 : 0;
+  ts.ps = kp_pitch<T>(M);
   ts.sec[0] = 0;
-  for (int t = 0; t < ntypes; ++t) ts.sec[t + 1] = ts.sec[t] + sel[t];
+  for (int t = 0; t < ntypes; ++t) {
+    GBDP_REQUIRE(sel[t] >= 0, "se_a descriptor: sel[%d] = %d", t, sel[t]);
+    ts.sec[t + 1] = ts.sec[t] + sel[t];
+  }
   for (int k = 0; k < ntab; ++k) {
-    GBDP_REQUIRE(tables[k] != nullptr && ((uintptr_t)tables[k] & 15) == 0,
-                 "se_a descriptor: table %d null or not 16-byte aligned", k);
+    GBDP_REQUIRE(tables[k] != nullptr && ((uintptr_t)tables[k] & 127) == 0,
+                 "se_a descriptor: table %d null or not 128-byte aligned", k);
     ts.table[k] = tables[k];
     ts.info[k] = make_table_info(infos + 6 * k);
   }
@@ -439,29 +667,88 @@ int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntype
 }
 
 template <typename T>
+int check_shapes(int M, int A, int nnei) {
+  GBDP_REQUIRE(M >= kAxis && M <= 128, "se_a descriptor: neuron[-1] %d not in [%d,128]", M,
+               kAxis);
+  GBDP_REQUIRE(A == kAxis, "se_a descriptor: axis_neuron %d (this build supports %d)", A, kAxis);
+  GBDP_REQUIRE(nnei >= 1 && nnei <= 4096, "se_a descriptor: nnei %d not in [1,4096]", nnei);
+  return GBDP_OK;
+}
+
+template <typename T, int NQF>
+void launch_fwd(dim3 grid, size_t smem, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
+                const int* atype, const int* drow, const TabSet<T>& ts, int nloc, int nnei, int M,
+                int tail_w, int tail_lg) {
+  auto kern = k_desc_fwd<T, NQF>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<grid, kFWarps * 32, smem, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                                         tail_lg);
+}
+
+template <typename T>
 int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow,
-             const T* const* tables,
-             const T* infos, int ntypes, const int* sel, int one_side, int nloc, int M, int A,
-             cudaStream_t st) {
+             const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
+             int nloc, int M, int A, cudaStream_t st) {
   TabSet<T> ts;
-  int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side);
+  int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side, M);
   if (rc) return rc;
-  GBDP_REQUIRE(M >= 1 && M <= 128, "se_a descriptor: neuron[-1] %d not in [1,128]", M);
-  GBDP_REQUIRE(A == 16, "se_a descriptor: axis_neuron %d (this build supports 16)", A);
-  if (nloc == 0) return GBDP_OK;
   const int nnei = ts.sec[ntypes];
-  const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
-  const int nq = (M + 31) / 32;
-  if (nq == 4)
-    k_desc_fwd<T, 4, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
-  else if (nq == 3)
-    k_desc_fwd<T, 3, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
-  else if (nq == 2)
-    k_desc_fwd<T, 2, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
-  else
-    k_desc_fwd<T, 1, 16><<<grid, block, 0, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M);
+  rc = check_shapes<T>(M, A, nnei);
+  if (rc) return rc;
+  if (nloc == 0) return GBDP_OK;
+  GBDP_REQUIRE(X && D && em && atype, "se_a descriptor fwd: null argument");
+  GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && ((uintptr_t)D & 15) == 0 &&
+                   (!D_lo || ((uintptr_t)D_lo & 15) == 0),
+               "se_a descriptor fwd: em / D must be 16-byte aligned");
+  // outputs past the last full 32-chunk: at most 16 of them run as a tail
+  const int w = M & 31;
+  const int nqf = (w == 0 || w > 16) ? (M + 31) / 32 : M / 32;
+  const int tail_w = (w == 0 || w > 16) ? 0 : w;
+  int tail_lg = 0;
+  while ((1 << tail_lg) < tail_w) ++tail_lg;
+  const int mp = (nqf + (tail_w > 0 ? 1 : 0)) * 32;
+  const size_t smem = (size_t)kFWarps * fwd_warp_bytes<T>(nnei, mp);
+  GBDP_REQUIRE(smem <= 200 * 1024, "se_a descriptor fwd: nnei %d needs %zu bytes of shared memory",
+               nnei, smem);
+  const dim3 grid((nloc + kFWarps - 1) / kFWarps);
+  switch (nqf) {
+    case 0:
+      launch_fwd<T, 0>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                       tail_lg);
+      break;
+    case 1:
+      launch_fwd<T, 1>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                       tail_lg);
+      break;
+    case 2:
+      launch_fwd<T, 2>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                       tail_lg);
+      break;
+    case 3:
+      launch_fwd<T, 3>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                       tail_lg);
+      break;
+    default:
+      launch_fwd<T, 4>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                       tail_lg);
+      break;
+  }
   GBDP_CHECK_LAUNCH("se_a_descriptor_fwd");
   return GBDP_OK;
+}
+
+template <typename T, int NQ>
+void launch_bwd(dim3 grid, size_t smem, cudaStream_t st, T* force, double* vir_acc, const T* X,
+                const T* dD, const int* drow, const T* em, const int* nlist_ext,
+                const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
+                BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
+  auto kern = k_desc_bwd<T, NQ>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<grid, kBWarps * 32, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                                         ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei,
+                                         M);
 }
 
 template <typename T>
@@ -471,42 +758,61 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
              float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st) {
   TabSet<T> ts;
-  int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side);
+  int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side, M);
   if (rc) return rc;
   GBDP_REQUIRE(force && vir_acc && nframes >= 1, "se_a descriptor bwd: null output / nframes");
+  const int nnei = ts.sec[ntypes];
+  rc = check_shapes<T>(M, A, nnei);
+  if (rc) return rc;
   cudaMemsetAsync(force, 0, sizeof(T) * 3 * (size_t)nloc, st);
   cudaMemsetAsync(vir_acc, 0, sizeof(double) * 9 * (size_t)nframes, st);
-  GBDP_REQUIRE(M >= 1 && M <= 128, "se_a descriptor: neuron[-1] %d not in [1,128]", M);
-  GBDP_REQUIRE(A == 16, "se_a descriptor: axis_neuron %d (this build supports 16)", A);
   if (nloc == 0) return GBDP_OK;
-  const int nnei = ts.sec[ntypes];
+  GBDP_REQUIRE(X && dD && em && nlist_ext && ext_coord && ext_map && atype && inv_std &&
+                   atom_frame && frame_aoff && frame_eoff,
+               "se_a descriptor bwd: null argument");
+  GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && ((uintptr_t)dD & 15) == 0 &&
+                   ((uintptr_t)inv_std & 15) == 0,
+               "se_a descriptor bwd: em / dE_dD / inv_std must be 16-byte aligned");
   BwdGeom geo{atom_frame, frame_aoff, frame_eoff};
   const int nq = (M + 31) / 32;
-  const int MP = nq * 32;
-  const int RW = 4 * MP + 16 * (MP + 1) + 1;
-  const size_t smem = (size_t)kFWarps * RW * sizeof(T);
-  GBDP_REQUIRE(nnei * 4 + 32 <= RW, "se_a descriptor bwd: nnei %d too large for neuron[-1] %d",
-               nnei, M);
-  const dim3 grid((nloc + kFWarps - 1) / kFWarps), block(kFWarps * 32);
-#define GBDP_LAUNCH_BWD(NQV)                                                                   \
-  {                                                                                            \
-    auto kern = k_desc_bwd<T, NQV, 16>;                                                        \
-    if (smem > 48 * 1024)                                                                      \
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
-    kern<<<grid, block, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,     \
-                                    ext_map, atype, inv_std, geo, ts, (T)rcut_smth, (T)rcut,   \
-                                    nloc, nnei, M);                                            \
+  const size_t smem = (size_t)kBWarps * bwd_warp_bytes<T>(nnei, nq * 32);
+  GBDP_REQUIRE(smem <= 200 * 1024, "se_a descriptor bwd: nnei %d needs %zu bytes of shared memory",
+               nnei, smem);
+  const dim3 grid((nloc + kBWarps - 1) / kBWarps);
+  const T rmin = (T)rcut_smth, rmax = (T)rcut;
+  switch (nq) {
+    case 1:
+      launch_bwd<T, 1>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      break;
+    case 2:
+      launch_bwd<T, 2>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      break;
+    case 3:
+      launch_bwd<T, 3>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      break;
+    default:
+      launch_bwd<T, 4>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      break;
   }
-  if (nq == 4)
-    GBDP_LAUNCH_BWD(4)
-  else if (nq == 3)
-    GBDP_LAUNCH_BWD(3)
-  else if (nq == 2)
-    GBDP_LAUNCH_BWD(2)
-  else
-    GBDP_LAUNCH_BWD(1)
-#undef GBDP_LAUNCH_BWD
   GBDP_CHECK_LAUNCH("se_a_descriptor_bwd");
+  return GBDP_OK;
+}
+
+template <typename T>
+int table_planar(T* dst, const T* src, int nrow, int M, cudaStream_t st) {
+  GBDP_REQUIRE(M >= 1 && M <= 4096 && nrow >= 0, "table_to_planar: nrow %d, M %d", nrow, M);
+  if (nrow == 0) return GBDP_OK;
+  GBDP_REQUIRE(dst && src, "table_to_planar: null pointer");
+  GBDP_REQUIRE(((uintptr_t)dst & 127) == 0, "table_to_planar: dst not 128-byte aligned");
+  const int ps = kp_pitch<T>(M);
+  const size_t n = (size_t)nrow * 3 * ps;
+  const unsigned blocks = (unsigned)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
+  k_table_planar<T><<<blocks, 256, 0, st>>>(dst, src, nrow, M, ps);
+  GBDP_CHECK_LAUNCH("table_to_planar");
   return GBDP_OK;
 }
 
@@ -515,14 +821,31 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
 
 using namespace gbdp;
 
+extern "C" size_t gbdp_table_planar_row_elems(int last_layer_size, int elem_bytes) {
+  if (last_layer_size < 1) return 0;
+  if (elem_bytes == 4) return 3 * (size_t)kp_pitch<float>(last_layer_size);
+  if (elem_bytes == 8) return 3 * (size_t)kp_pitch<double>(last_layer_size);
+  return 0;
+}
+
+extern "C" int gbdp_table_to_planar_f32(float* dst, const float* src, int nrow,
+                                        int last_layer_size, gbdp_stream stream) {
+  return table_planar<float>(dst, src, nrow, last_layer_size, (cudaStream_t)stream);
+}
+
+extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow,
+                                        int last_layer_size, gbdp_stream stream) {
+  return table_planar<double>(dst, src, nrow, last_layer_size, (cudaStream_t)stream);
+}
+
 #define GBDP_FUSED_ENTRY(T, SFX)                                                                \
   extern "C" int gbdp_se_a_descriptor_fwd_##SFX(                                                \
       T* X, T* D, const T* em, const int* atype, const int* d_row, const T* const* tables,      \
       const T* table_infos, int ntypes, const int* sel, int type_one_side, int nloc,           \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
     return desc_fwd<T>(X, D, nullptr, em, atype, d_row, tables, table_infos, ntypes, sel,       \
-                       type_one_side,                                                          \
-                       nloc, last_layer_size, axis_neuron, (cudaStream_t)stream);              \
+                       type_one_side, nloc, last_layer_size, axis_neuron,                      \
+                       (cudaStream_t)stream);                                                   \
   }                                                                                             \
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
       T* force, double* virial_acc, const T* X, const T* dE_dD, const int* d_row, const T* em, \
@@ -532,10 +855,9 @@ using namespace gbdp;
       const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
     return desc_bwd<T>(force, virial_acc, X, dE_dD, d_row, em, nlist_ext, ext_coord, ext_map,  \
-                       atype,                                                                  \
-                       inv_std, atom_frame, frame_atom_off, frame_ext_off, tables, table_infos,    \
-                       ntypes, sel, type_one_side, rcut_smth, rcut, nloc, nframes,             \
-                       last_layer_size, axis_neuron, (cudaStream_t)stream);                    \
+                       atype, inv_std, atom_frame, frame_atom_off, frame_ext_off, tables,      \
+                       table_infos, ntypes, sel, type_one_side, rcut_smth, rcut, nloc,         \
+                       nframes, last_layer_size, axis_neuron, (cudaStream_t)stream);           \
   }
 
 GBDP_FUSED_ENTRY(float, f32)

@@ -84,7 +84,9 @@ class SeAModel:
             self.table_infos = np.asarray(table_infos, np.float64)
             self.table_info_t = [torch.tensor(i, dtype=dtype) for i in self.table_infos]  # CPU
             ct = ctypes.c_double if dtype == torch.float64 else ctypes.c_float
-            self._tab_ptrs = (_P * len(self.tables))(*[t.data_ptr() for t in self.tables])
+            # the fused kernels read a k-planar copy of each table
+            self.tables_kp = [self._planar(t) for t in self.tables]
+            self._tab_ptrs = (_P * len(self.tables_kp))(*[t.data_ptr() for t in self.tables_kp])
             flat = self.table_infos.reshape(-1)
             self._tab_infos = (ct * len(flat))(*flat.tolist())
         self._sel_c = (ctypes.c_int * cfg.ntypes)(*[int(s) for s in cfg.sel])
@@ -125,6 +127,20 @@ class SeAModel:
                 self._fit_c.append((nh, widths, wp, bp, ip, wout, float(bf[0])))
         self._sfx = L.sfx(dtype)
         self._lib = L.load()
+
+    def _planar(self, table: torch.Tensor) -> torch.Tensor:
+        lib = L.load()
+        nrow, w6 = table.shape
+        m = w6 // 6
+        re = lib.gbdp_table_planar_row_elems(m, table.element_size())
+        dst = torch.empty(nrow * re, dtype=table.dtype, device=table.device)
+        if dst.data_ptr() % 128:
+            raise RuntimeError("planar table allocation is not 128-byte aligned")
+        stream = torch.cuda.current_stream(table.device).cuda_stream
+        fn = lib.gbdp_table_to_planar_f64 if table.dtype == torch.float64 else \
+            lib.gbdp_table_to_planar_f32
+        L.check(fn(dst.data_ptr(), table.data_ptr(), nrow, m, stream), "table_to_planar")
+        return dst
 
     # ------------------------------------------------------------- batches --
     def batch(self, atype_per_frame, boxes, max_cand: int = 0) -> "Batch":
@@ -328,11 +344,18 @@ class SeAModel:
         return E, torch.cat(forces), torch.stack(virs).to(torch.float64)
 
 
+def _rn_tf32(x: torch.Tensor) -> torch.Tensor:
+    """x rounded to TF32 (10 explicit mantissa bits): to nearest, ties away
+    from zero, on the magnitude bits of the FP32 pattern."""
+    return ((x.contiguous().view(torch.int32) + 0x1000) & -8192).view(torch.float32)
+
+
 def _split_tf32(x: torch.Tensor):
-    """x = hi + lo with hi exactly representable in TF32 (10 explicit
-    mantissa bits, low 13 bits cleared) and lo the remainder."""
-    hi = (x.contiguous().view(torch.int32) & -8192).view(torch.float32)
-    return hi, x - hi
+    """x ~= hi + lo, hi = x rounded to TF32 and lo = (x - hi) rounded to
+    TF32, so that both are exact tensor-core operands and
+    |x - hi - lo| <= 2^-23 |x|."""
+    hi = _rn_tf32(x)
+    return hi, _rn_tf32(x - hi)
 
 
 def energy_std_loss(E, F, V, E_ref, F_ref, V_ref, natoms: int, pref_e=0.02, pref_f=1000.0,

@@ -271,7 +271,9 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * deepmd/pt/model/descriptor/se_a.py:786-866, tables as bound through
  * deepmd::tabulate_fusion_se_a).  tables: HOST array of device table
  * pointers, one per embedding net (ntypes nets if type_one_side, else
- * ntypes^2 indexed tj * ntypes + ti); table_infos: HOST [n_tables * 6];
+ * ntypes^2 indexed tj * ntypes + ti), each in the k-planar layout written
+ * by gbdp_table_to_planar_* and 128-byte aligned; table_infos: HOST
+ * [n_tables * 6];
  * sel: HOST [ntypes].  em comes from gbdp_prod_env_mat_a_*.  d_row (device,
  * may be NULL for the identity) gives the row of D / dE_dD that belongs to
  * atom i, so that a caller can keep each type's rows contiguous.
@@ -282,6 +284,19 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * semantics); inv_std [ntypes, nnei * 4] is 1 / dstd.  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
  * are device arrays describing the packed batch (see gbdp_nbr_frame).
  * ---------------------------------------------------------------------- */
+/* The fused descriptor kernels read the tables of tabulate_fusion_se_a
+ * ([nspline, 6 M], coefficient-minor, as above) in a k-planar copy: row r
+ * holds 3 planes of pitch P elements (P = 2 M rounded up to 128 bytes),
+ * plane p the pairs (a_2p, a_2p+1) of output k at 2 k, so that consecutive
+ * k are adjacent in memory.  No reference counterpart: a layout choice of
+ * this library.  row_elems = 3 P for the element size (4 or 8 bytes); dst
+ * holds nrow * row_elems elements, 128-byte aligned; src and dst device. */
+GBDP_API size_t gbdp_table_planar_row_elems(int last_layer_size, int elem_bytes);
+GBDP_API int gbdp_table_to_planar_f32(float* dst, const float* src, int nrow,
+                                      int last_layer_size, gbdp_stream stream);
+GBDP_API int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow,
+                                      int last_layer_size, gbdp_stream stream);
+
 GBDP_API int gbdp_se_a_descriptor_fwd_f32(float* X, float* D, const float* em, const int* atype,
                                           const int* d_row, const float* const* tables, const float* table_infos,
                                           int ntypes, const int* sel, int type_one_side,
@@ -331,8 +346,8 @@ GBDP_API int gbdp_fitting_fwd_bwd_f32(float* e, float* dD, const float* D, int n
                                       gbdp_stream stream);
 
 /* As gbdp_se_a_descriptor_fwd_f32, but D is written split for the tensor-
- * core fitting: D_hi = D with the low 13 mantissa bits cleared, D_lo =
- * D - D_hi (exact). */
+ * core fitting: D_hi = D rounded to TF32 (10 explicit mantissa bits, to
+ * nearest), D_lo = (D - D_hi) rounded to TF32. */
 GBDP_API int gbdp_se_a_descriptor_fwd_split_f32(
     float* X, float* D_hi, float* D_lo, const float* em, const int* atype, const int* d_row,
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
@@ -345,8 +360,9 @@ GBDP_API int gbdp_se_a_descriptor_fwd_split_f32(
  * Rows are grouped by atom type: type t owns rows [row_off[t],
  * row_off[t] + nrows[t]) of every activation, row_off[t] a multiple of 128,
  * row_off[ntypes] the padded total (also a multiple of 128).  D is given
- * split (D_hi with the low 13 mantissa bits cleared, D_lo = D - D_hi), as
- * gbdp_se_a_descriptor_fwd_split_f32 writes it.  Per type (device pointers):
+ * split (D_hi = D rounded to TF32, D_lo = (D - D_hi) rounded to TF32), as
+ * gbdp_se_a_descriptor_fwd_split_f32 writes it; the weights are split the
+ * same way.  Per type (device pointers):
  * w_hi/w_lo[l] = W_l [in, out] and wt_hi/wt_lo[l] = W_l^T [out, in], split;
  * b[l]; idt[l] (NULL for layer 0); w_out [240]; b_out on the host.
  * Outputs: e [rows] per-row energy (0 on padding rows), dE_dD [rows, 1600].

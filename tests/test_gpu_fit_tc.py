@@ -2,8 +2,9 @@
 cuBLAS FP32 path on the same descriptor rows, and the fused step with it
 against the FP64 composite.
 
-Stated tolerances: per-atom energy and dE/dD within 2e-6 relative to the
-largest magnitude (FP32-level split product); forces <= 1e-5 eV/A vs FP64."""
+Stated tolerances: per-atom energy and dE/dD within 5e-6 relative to the
+largest magnitude (split products with short tensor-core accumulation
+chains); forces <= 1e-5 eV/A vs FP64."""
 
 import importlib
 
@@ -46,8 +47,10 @@ def test_tc_fitting_matches_fp32_gemm(setup):
         assert n_t == n_r
         e_tc, e_ref = bt.ae[s_t:s_t + n_t], br.ae[s_r:s_r + n_r]
         g_tc, g_ref = bt.dD[s_t:s_t + n_t], br.dD[s_r:s_r + n_r]
-        assert torch.allclose(e_tc, e_ref, atol=2e-6 * float(e_ref.abs().max()), rtol=0)
-        assert torch.allclose(g_tc, g_ref, atol=2e-6 * float(g_ref.abs().max()), rtol=0)
+        err_e = float((e_tc - e_ref).abs().max()) / float(e_ref.abs().max())
+        err_g = float((g_tc - g_ref).abs().max()) / float(g_ref.abs().max())
+        print(f"type {t}: relative max error e {err_e:.3e}, dE/dD {err_g:.3e}")
+        assert err_e <= 5e-6 and err_g <= 5e-6, (t, err_e, err_g)
         if t == 0:  # padding rows of the first block carry no energy
             assert float(bt.ae[s_t + n_t:bt.type_rows[1][0]].abs().max()) == 0.0
 

@@ -156,3 +156,32 @@ def test_cpu_tensors_fail_loudly():
     with pytest.raises(RuntimeError, match="CUDA tensors only"):
         torch.ops.deepmd.tabulate_fusion_se_a(table, info, torch.zeros(2, 4, dtype=torch.float64),
                                               torch.zeros(2, 4, 4, dtype=torch.float64), 8)
+
+
+@pytest.mark.parametrize("dtype,m", [(torch.float32, 100), (torch.float32, 37), (torch.float64, 100),
+                                     (torch.float64, 16)])
+def test_table_to_planar_layout(gb, dtype, m):
+    """gbdp_table_to_planar_*: element (r, 2p + c, k) of the [nrow, 6 M]
+    coefficient-minor table lands at r * row_elems + p * P + 2 k + c, with
+    zero padding up to the plane pitch P (2 M rounded up to 128 bytes)."""
+    import ctypes
+
+    L = gb._lib
+    lib = L.load()
+    nrow = 7
+    rng = np.random.default_rng(3)
+    src_np = rng.standard_normal((nrow, 6 * m))
+    src = torch.tensor(src_np, dtype=dtype, device=DEV)
+    esz = src.element_size()
+    re = lib.gbdp_table_planar_row_elems(m, esz)
+    pitch = re // 3
+    assert pitch * esz % 128 == 0 and pitch >= 2 * m
+    dst = torch.full((nrow * re,), 7.0, dtype=dtype, device=DEV)
+    fn = lib.gbdp_table_to_planar_f64 if dtype == torch.float64 else lib.gbdp_table_to_planar_f32
+    L.check(fn(dst.data_ptr(), src.data_ptr(), nrow, m, None), "table_to_planar")
+    torch.cuda.synchronize()
+    got = dst.cpu().numpy().reshape(nrow, 3, pitch)
+    exp = np.zeros((nrow, 3, pitch))
+    co = src_np.reshape(nrow, m, 3, 2)  # [r, k, p, c]
+    exp[:, :, :2 * m] = co.transpose(0, 2, 1, 3).reshape(nrow, 3, 2 * m)
+    np.testing.assert_array_equal(got, exp.astype(got.dtype))

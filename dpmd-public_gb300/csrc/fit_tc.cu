@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -34,43 +35,53 @@
 namespace gbdp {
 namespace {
 
-constexpr int TBM = 128, TBN = 80, TBK = 32, TSTAGES = 4;
+constexpr int TBM = 128, TBN = 80, TBK = 32;
 constexpr int A_TILE = TBM * TBK * 4;                // 16 KiB
 constexpr int B_TILE = TBN * TBK * 4;                // 10 KiB
 constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;       // 52 KiB
-constexpr int NACC = 3;                              // main accumulators
 constexpr uint32_t ACC_COLS = 128;                   // TMEM columns per accumulator (>= TBN)
-constexpr int TMEM_COLS = 512;                       // NACC main + 1 cross-term accumulator
-constexpr int TC_SMEM = TSTAGES * STAGE + 1024 + 256;  // + alignment slack + barriers
+// Two configurations: long K (the 1600-wide layer) with 4 pipeline stages
+// and 3 main accumulators (one CTA per SM: 214 KB shared, 512 TMEM
+// columns); short K (<= 256) with 2 stages and 1 main accumulator, so that
+// two CTAs share an SM (105 KB shared, 256 TMEM columns each) and one's
+// epilogue overlaps the other's main loop.
+constexpr int tc_smem(int stages) { return stages * STAGE + 1024 + 256; }
 constexpr int FIT_W = 240;                           // hidden width this kernel serves
 constexpr int FIT_D = 1600;                          // descriptor width this kernel serves
 
 struct TcMaps {
   CUtensorMap a_hi, a_lo;
   CUtensorMap b_hi[2], b_lo[2];
+  CUtensorMap in[2];   // per-row epilogue inputs, boxes of 16 columns x 32 rows
+  CUtensorMap out[3];  // epilogue outputs (o0, hi, lo), same boxes
 };
+
+// Epilogue staging per warp (in the pipeline buffers, free once the last
+// MMA has completed): two input chunks and two output chunks in flight,
+// each array chunk 32 rows x 16 floats (2 KiB, rows of 64 B, 64-byte TMA
+// swizzle).
+constexpr int EPI_CHUNK = 32 * 16;                          // floats per array chunk
+constexpr int EPI_IN_BYTES = 2 * 2 * EPI_CHUNK * 4;         // 8 KiB
+constexpr int EPI_WARP_BYTES = EPI_IN_BYTES + 2 * 3 * EPI_CHUNK * 4;  // 20 KiB
 
 enum { EPI_F1 = 0, EPI_F2, EPI_F3, EPI_B3, EPI_B2, EPI_B1 };
 
+// Per-row inputs and outputs of each epilogue kind (maps.in / maps.out):
+//   F1  out T1, H1 hi/lo        F2  in H1 hi/lo; out T2, H2 hi/lo
+//   F3  in H2 hi/lo; out GZ3 hi/lo (+ energy partials)
+//   B3  in T2; out G2, GZ2 hi/lo      B2  in T1, G2; out GZ1 hi/lo
+//   B1  out dE/dD
 struct TcEpi {
   int kind;
-  int ldo;          // leading dimension of the outputs
   int ntypes;
   int row_off[3];   // padded row block of each type; row_off[ntypes] = total rows
   int ntile_n;      // tiles along N (F3: partial energies per row)
+  int nin;          // per-row input arrays (maps.in[0..nin))
+  int out_mask;     // bit a: maps.out[a] is written
   const float* bias[2];
   const float* idt[2];
   const float* wout[2];
-  const float* tin;      // T of this layer (backward)
-  const float* prev_hi;  // skip input (forward: H_{l-1}; B2: none)
-  const float* prev_lo;
-  const float* gin;      // G_l for the skip of the backward (B2)
-  float* tout;           // T written (F1, F2)
-  float* out_hi;         // split output (next A operand)
-  float* out_lo;
-  float* gout;           // G2 (B3)
-  float* epart;          // [rows, ntile_n] partial energies (F3)
-  float* out;            // dE/dD (B1)
+  float* epart;     // [rows, ntile_n] partial energies (F3)
   int* status;
 };
 
@@ -94,6 +105,29 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   d |= (uint64_t)1 << 46;                    // descriptor version (sm_100 family)
   d |= (uint64_t)2 << 61;                    // swizzle: 128 B
   return d;
+}
+
+// bulk tensor store of one box from shared memory (bulk-group completion)
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y,
+                                             const void* src) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(x), "r"(y), "r"(smem_addr(src))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// at most one group still reading its shared-memory source
+__device__ __forceinline__ void bulk_wait_read1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 __device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
@@ -143,15 +177,45 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
   lo = rn_tf32(x - hi);
 }
 
-__device__ __forceinline__ void store16(float* p, const float* v) {
+// One thread's row (16 floats) of a [32 rows][64 B] staging chunk in the
+// TMA 64-byte swizzle: logical 16-byte piece q of row r sits at piece
+// q ^ ((r >> 1) & 3) (address bits 4-5 XOR bits 7-8; chunks 512-byte
+// aligned), so the 8 rows of a warp phase use 8 distinct bank groups.
+__device__ __forceinline__ void row_st16(float* chunk, int lane, const float* v) {
+  const int sw = (lane >> 1) & 3;
 #pragma unroll
-  for (int k = 0; k < 16; k += 4)
-    *reinterpret_cast<float4*>(p + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+  for (int q = 0; q < 4; ++q)
+    *reinterpret_cast<float4*>(chunk + lane * 16 + ((q ^ sw) << 2)) =
+        make_float4(v[q * 4], v[q * 4 + 1], v[q * 4 + 2], v[q * 4 + 3]);
+}
+__device__ __forceinline__ void row_ld16(const float* chunk, int lane, float* v) {
+  const int sw = (lane >> 1) & 3;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 u = *reinterpret_cast<const float4*>(chunk + lane * 16 + ((q ^ sw) << 2));
+    v[q * 4] = u.x;
+    v[q * 4 + 1] = u.y;
+    v[q * 4 + 2] = u.z;
+    v[q * 4 + 3] = u.w;
+  }
+}
+// 16 per-column parameters (64-byte aligned)
+__device__ __forceinline__ void col_ld16(const float* p, float* v) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 u = __ldg(reinterpret_cast<const float4*>(p) + q);
+    v[q * 4] = u.x;
+    v[q * 4 + 1] = u.y;
+    v[q * 4 + 2] = u.z;
+    v[q * 4 + 3] = u.w;
+  }
 }
 
 // ------------------------------------------------------------- kernel --
+template <int TSTAGES, int NACC>
 __global__ void __launch_bounds__(128, 1)
-    k_fit_tc(const __grid_constant__ TcMaps maps, const TcEpi ep, int K) {
+    k_fit_tc(const __grid_constant__ TcMaps maps, const __grid_constant__ TcEpi ep, int K) {
+  constexpr int TMEM_COLS = (NACC + 1) * (int)ACC_COLS;  // NACC main + 1 cross-term
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -159,8 +223,11 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* empty = full + TSTAGES;
   uint64_t* tfull = empty + TSTAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfull + 1);
+  uint64_t* inbar = tfull + 2;  // [4 warps][2 buffers]: epilogue input chunks
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row0 = blockIdx.x * TBM, n0 = blockIdx.y * TBN;
+  // N tiles of one row block are adjacent in launch order: A is read from
+  // DRAM once and re-read from L2
+  const int row0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
   int t = 0;
   while (t + 1 < ep.ntypes && row0 >= ep.row_off[t + 1]) ++t;
   const int nkb = (K + TBK - 1) / TBK;
@@ -171,6 +238,7 @@ __global__ void __launch_bounds__(128, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
+    for (int b = 0; b < 8; ++b) mbar_init(&inbar[b], 1);
     fence_mbar_init();
   }
   if (warp == 0) {
@@ -228,15 +296,41 @@ __global__ void __launch_bounds__(128, 1)
   }
   __syncwarp();
 
-  // ---- epilogue: warp w owns rows 32w..32w+31 of the tile (TMEM lanes)
-  const bool got = mbar_wait_bounded(tfull, 0, ep.status);
+  // ---- epilogue: warp w owns rows 32w..32w+31 of the tile (TMEM lanes);
+  //      per-row inputs arrive by TMA, outputs leave by TMA bulk stores
+  // lanes poll on their own: agree on the outcome before any warp-wide op
+  const bool got = __all_sync(kFull, mbar_wait_bounded(tfull, 0, ep.status));
   tc_fence_after();
-  const int r = row0 + warp * 32 + lane;
-  const int ld = ep.ldo;
   float esum = 0.f;
   if (got) {
+    static_assert(4 * EPI_WARP_BYTES <= 2 * STAGE, "epilogue staging exceeds the stage buffers");
+    unsigned char* wsm = smem + warp * EPI_WARP_BYTES;
+    float* inb = reinterpret_cast<float*>(wsm);                  // [2 buf][2 arr][chunk]
+    float* outb = reinterpret_cast<float*>(wsm + EPI_IN_BYTES);  // [2 buf][3 arr][chunk]
+    uint64_t* ib = inbar + warp * 2;
+    const int yrow = row0 + warp * 32;
+    const int nin = ep.nin;
+    constexpr int NCH = TBN / 16;
+    int in_issued = nin > 0 ? 1 : 0, in_done = 0;  // input chunks issued / received
+    if (lane == 0 && nin > 0) {
+      mbar_expect_tx(&ib[0], nin * EPI_CHUNK * 4);
+      for (int a = 0; a < nin; ++a) tma_2d(inb + a * EPI_CHUNK, &maps.in[a], n0, yrow, &ib[0]);
+    }
 #pragma unroll 1
-    for (int c0 = 0; c0 < TBN; c0 += 16) {
+    for (int ci = 0; ci < NCH; ++ci) {
+      const int c0 = ci * 16, buf = ci & 1;
+      if (ci + 1 < NCH && nin > 0) {
+        // the other input buffer was last read in chunk ci - 1
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          mbar_expect_tx(&ib[buf ^ 1], nin * EPI_CHUNK * 4);
+          for (int a = 0; a < nin; ++a)
+            tma_2d(inb + ((buf ^ 1) * 2 + a) * EPI_CHUNK, &maps.in[a], n0 + c0 + 16, yrow,
+                   &ib[buf ^ 1]);
+        }
+        ++in_issued;
+      }
       float v[16], w[16];
       const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       tmem_ld16(ta, v);
@@ -248,47 +342,74 @@ __global__ void __launch_bounds__(128, 1)
       tmem_ld16(ta + (uint32_t)NACC * ACC_COLS, w);
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] += w[k];
-      const int c = n0 + c0;
-      const size_t o = (size_t)r * ld + c;
-      if (ep.kind == EPI_B1) {
-        store16(ep.out + o, v);
-        continue;
+      float x0[16], x1[16];
+      if (nin > 0) {
+        if (!__all_sync(kFull, mbar_wait_bounded(&ib[buf], (unsigned)(ci >> 1) & 1u, ep.status)))
+          break;
+        ++in_done;
+        row_ld16(inb + (buf * 2) * EPI_CHUNK, lane, x0);
+        if (nin > 1) row_ld16(inb + (buf * 2 + 1) * EPI_CHUNK, lane, x1);
       }
-      float hi[16], lo[16];
-      if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
-        const float* b = ep.bias[t];
-        const float* idt = ep.idt[t];
+      const int c = n0 + c0;
+      float o0[16], hi[16], lo[16];
+      if (ep.kind == EPI_B1) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) o0[k] = v[k];
+      } else if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
+        float bb[16], id[16], wo[16];
+        col_ld16(ep.bias[t] + c, bb);
+        if (ep.kind != EPI_F1) col_ld16(ep.idt[t] + c, id);
+        if (ep.kind == EPI_F3) col_ld16(ep.wout[t] + c, wo);
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-          const float tt = tanhf(v[k] + b[c + k]);
+          const float tt = tanhf(v[k] + bb[k]);
           float h = tt;
-          if (ep.kind != EPI_F1) h = tt * idt[c + k] + (ep.prev_hi[o + k] + ep.prev_lo[o + k]);
+          if (ep.kind != EPI_F1) h = tt * id[k] + (x0[k] + x1[k]);
           if (ep.kind == EPI_F3) {
-            const float wo = ep.wout[t][c + k];
-            esum += h * wo;
-            split_tf32(wo * idt[c + k] * (1.f - tt * tt), hi[k], lo[k]);  // GZ3
+            esum += h * wo[k];
+            split_tf32(wo[k] * id[k] * (1.f - tt * tt), hi[k], lo[k]);  // GZ3
           } else {
             split_tf32(h, hi[k], lo[k]);
           }
-          v[k] = tt;
+          o0[k] = tt;
         }
-        if (ep.kind != EPI_F3) store16(ep.tout + o, v);
-      } else {  // B3, B2
-        const float* idt = ep.kind == EPI_B3 ? ep.idt[t] : nullptr;
+      } else {  // B3: x0 = T2; B2: x0 = T1, x1 = G2
+        float id[16], wo[16];
+        if (ep.kind == EPI_B3) {
+          col_ld16(ep.idt[t] + c, id);
+          col_ld16(ep.wout[t] + c, wo);
+        }
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-          float g = v[k] + (ep.kind == EPI_B3 ? ep.wout[t][c + k] : ep.gin[o + k]);
-          if (ep.kind == EPI_B3) v[k] = g;
-          const float tt = ep.tin[o + k];
-          float gz = (idt ? g * idt[c + k] : g) * (1.f - tt * tt);
+          const float g = v[k] + (ep.kind == EPI_B3 ? wo[k] : x1[k]);
+          o0[k] = g;
+          const float tt = x0[k];
+          const float gz = (ep.kind == EPI_B3 ? g * id[k] : g) * (1.f - tt * tt);
           split_tf32(gz, hi[k], lo[k]);
         }
-        if (ep.kind == EPI_B3) store16(ep.gout + o, v);
       }
-      store16(ep.out_hi + o, hi);
-      store16(ep.out_lo + o, lo);
+      // the output buffer was last used by the stores of chunk ci - 2
+      if (lane == 0 && ci >= 2) bulk_wait_read1();
+      __syncwarp();
+      float* ob = outb + buf * 3 * EPI_CHUNK;
+      if (ep.out_mask & 1) row_st16(ob, lane, o0);
+      if (ep.out_mask & 2) row_st16(ob + EPI_CHUNK, lane, hi);
+      if (ep.out_mask & 4) row_st16(ob + 2 * EPI_CHUNK, lane, lo);
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        for (int a = 0; a < 3; ++a)
+          if (ep.out_mask & (1 << a)) tma_store_2d(&maps.out[a], c, yrow, ob + a * EPI_CHUNK);
+        bulk_commit();
+      }
     }
-    if (ep.kind == EPI_F3) ep.epart[(size_t)r * ep.ntile_n + blockIdx.y] = esum;
+    if (lane == 0) {
+      bulk_wait_all();
+      // after a timeout: no input chunk may land once the CTA has exited
+      for (int ch = in_done; ch < in_issued; ++ch)
+        mbar_wait_bounded(&ib[ch & 1], (unsigned)(ch >> 1) & 1u, ep.status);
+    }
+    if (ep.kind == EPI_F3) ep.epart[(size_t)(yrow + lane) * ep.ntile_n + blockIdx.x] = esum;
   }
   // ---- drain: no bulk copy of this CTA may land after it exits
   if (warp == 0 && lane == 0) {
@@ -344,20 +465,32 @@ int get_encode() {
   return GBDP_OK;
 }
 
-// [rows, cols] fp32 row-major, boxes of 32 columns x box_rows rows, 128 B swizzle
-int make_map(CUtensorMap* m, const float* base, long rows, long cols, int box_rows) {
-  GBDP_REQUIRE(((uintptr_t)base & 15) == 0, "fit_tc: operand not 16-byte aligned");
+// [rows, cols] fp32 row-major in boxes of box_x columns x box_y rows
+int make_map_box(CUtensorMap* m, const float* base, long rows, long cols, int box_x, int box_y,
+                 CUtensorMapSwizzle swz) {
+  GBDP_REQUIRE(base != nullptr && ((uintptr_t)base & 15) == 0,
+               "fit_tc: operand null or not 16-byte aligned");
   GBDP_REQUIRE((cols * 4) % 16 == 0, "fit_tc: row pitch not a multiple of 16 bytes");
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
-  cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
-                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   GBDP_REQUIRE(r == CUDA_SUCCESS, "fit_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
   return GBDP_OK;
+}
+
+// MMA operand: boxes of 32 columns (128 B) x box_rows rows, 128 B swizzle
+int make_map(CUtensorMap* m, const float* base, long rows, long cols, int box_rows) {
+  return make_map_box(m, base, rows, cols, TBK, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
+// epilogue row array: boxes of 16 columns x 32 rows (one warp's chunk),
+// 64-byte swizzle (matching row_st16 / row_ld16)
+int make_epi_map(CUtensorMap* m, const float* base, long rows, long cols) {
+  return make_map_box(m, base, rows, cols, 16, 32, CU_TENSOR_MAP_SWIZZLE_64B);
 }
 
 size_t a256t(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -433,31 +566,44 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
   int* status = reinterpret_cast<int*>(static_cast<char*>(workspace) + ws.bytes);
   cudaStream_t st = (cudaStream_t)stream;
   cudaMemsetAsync(status, 0, sizeof(int) * 4, st);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(k_fit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    attr_done = true;
-  }
+  cudaFuncSetAttribute(k_fit_tc<4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(4));
+  cudaFuncSetAttribute(k_fit_tc<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(2));
+  GBDP_REQUIRE(rows / TBM <= 65535, "fit_tc: %ld rows exceed the grid limit", rows);
   TcEpi base{};
   base.ntypes = ntypes;
   for (int t = 0; t <= ntypes; ++t) base.row_off[t] = row_off[t];
   base.status = status;
-  base.ldo = FIT_W;
   base.ntile_n = FIT_W / TBN;
-  for (int t = 0; t < ntypes; ++t) base.wout[t] = nets[t].w_out;
+  for (int t = 0; t < ntypes; ++t) {
+    base.wout[t] = nets[t].w_out;
+    const float* cols[4] = {nets[t].w_out, nets[t].b[0], nets[t].b[1], nets[t].b[2]};
+    for (const float* p : cols)
+      GBDP_REQUIRE(((uintptr_t)p & 15) == 0, "fit_tc: bias / w_out not 16-byte aligned");
+    GBDP_REQUIRE(((uintptr_t)nets[t].idt[1] & 15) == 0 && ((uintptr_t)nets[t].idt[2] & 15) == 0,
+                 "fit_tc: idt not 16-byte aligned");
+  }
   struct Step {
     int kind;
     const float *a_hi, *a_lo;
     int K, N, layer;
     bool fwd;
+    const float* in[2];
+    float* out[3];
   };
   const Step steps[6] = {
-      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true},     {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true},
-      {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true}, {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false},
-      {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false},
-      {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false}};
+      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}},
+      {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.h1h, ws.h1l}, {ws.t2, ws.h2h, ws.h2l}},
+      {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true, {ws.h2h, ws.h2l},
+       {nullptr, ws.gz3h, ws.gz3l}},
+      {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false, {ws.t2, nullptr},
+       {ws.g2, ws.gz2h, ws.gz2l}},
+      {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false, {ws.t1, ws.g2},
+       {nullptr, ws.gz1h, ws.gz1l}},
+      {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false, {nullptr, nullptr},
+       {dE_dD, nullptr, nullptr}}};
   for (const Step& sp : steps) {
     TcMaps maps;
+    memset(&maps, 0, sizeof(maps));
     rc = make_map(&maps.a_hi, sp.a_hi, rows, sp.K, TBM);
     if (!rc) rc = make_map(&maps.a_lo, sp.a_lo, rows, sp.K, TBM);
     for (int t = 0; t < 2 && !rc; ++t) {
@@ -468,38 +614,34 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
       rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, TBN);
       if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, TBN);
     }
-    if (rc) return rc;
     TcEpi ep = base;
     ep.kind = sp.kind;
-    ep.ldo = sp.N;
+    ep.nin = 0;
+    ep.out_mask = 0;
+    // per-row inputs and outputs are [rows, N] arrays, N = this layer's width
+    for (int a = 0; a < 2 && !rc; ++a)
+      if (sp.in[a]) {
+        rc = make_epi_map(&maps.in[a], sp.in[a], rows, sp.N);
+        ep.nin = a + 1;
+      }
+    for (int a = 0; a < 3 && !rc; ++a)
+      if (sp.out[a]) {
+        rc = make_epi_map(&maps.out[a], sp.out[a], rows, sp.N);
+        ep.out_mask |= 1 << a;
+      }
+    if (rc) return rc;
     for (int t = 0; t < ntypes; ++t) {
       ep.bias[t] = nets[t].b[sp.layer];
       ep.idt[t] = nets[t].idt[sp.layer];
     }
-    switch (sp.kind) {
-      case EPI_F1:
-        ep.tout = ws.t1, ep.out_hi = ws.h1h, ep.out_lo = ws.h1l;
-        break;
-      case EPI_F2:
-        ep.tout = ws.t2, ep.prev_hi = ws.h1h, ep.prev_lo = ws.h1l, ep.out_hi = ws.h2h,
-        ep.out_lo = ws.h2l;
-        break;
-      case EPI_F3:
-        ep.prev_hi = ws.h2h, ep.prev_lo = ws.h2l, ep.out_hi = ws.gz3h, ep.out_lo = ws.gz3l,
-        ep.epart = ws.epart;
-        break;
-      case EPI_B3:
-        for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
-        ep.tin = ws.t2, ep.gout = ws.g2, ep.out_hi = ws.gz2h, ep.out_lo = ws.gz2l;
-        break;
-      case EPI_B2:
-        ep.tin = ws.t1, ep.gin = ws.g2, ep.out_hi = ws.gz1h, ep.out_lo = ws.gz1l;
-        break;
-      default:
-        ep.out = dE_dD;
-    }
-    const dim3 grid((unsigned)(rows / TBM), (unsigned)(sp.N / TBN));
-    k_fit_tc<<<grid, 128, TC_SMEM, st>>>(maps, ep, sp.K);
+    if (sp.kind == EPI_B3)
+      for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
+    if (sp.kind == EPI_F3) ep.epart = ws.epart;
+    const dim3 grid((unsigned)(sp.N / TBN), (unsigned)(rows / TBM));
+    if (sp.K > 256)
+      k_fit_tc<4, 3><<<grid, 128, tc_smem(4), st>>>(maps, ep, sp.K);
+    else
+      k_fit_tc<2, 1><<<grid, 128, tc_smem(2), st>>>(maps, ep, sp.K);
     GBDP_CHECK_LAUNCH("fit_tc gemm");
   }
   TcRows rw{};

@@ -85,13 +85,29 @@ struct Vec<double> {
 template <typename T>
 using V4 = typename Vec<T>::v4;
 
+// L1 policy.  The table rows are the only data the kernels re-read across
+// atoms; everything per atom (env rows, X, dE/dD) streams through once or
+// twice.  Table loads carry L1::evict_last, per-atom rows L1::no_allocate
+// (read once) or L1::evict_first (read twice), so that the hot band of
+// table rows stays resident in L1.
+__device__ __forceinline__ float2 ld_tab2(const float2* p) {
+  float2 v;
+  asm("ld.global.nc.L1::evict_last.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double2 ld_tab2(const double2* p) {
+  double2 v;
+  asm("ld.global.nc.L1::evict_last.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
+
 // the six coefficients of output k from a k-planar row
 template <typename T>
 __device__ __forceinline__ void load_coef6_kp(T* a, const T* __restrict__ row, int ps, int k) {
   using P = typename Vec<T>::v2;
-  const P u = __ldg(reinterpret_cast<const P*>(row) + k);
-  const P v = __ldg(reinterpret_cast<const P*>(row + ps) + k);
-  const P w = __ldg(reinterpret_cast<const P*>(row + 2 * ps) + k);
+  const P u = ld_tab2(reinterpret_cast<const P*>(row) + k);
+  const P v = ld_tab2(reinterpret_cast<const P*>(row + ps) + k);
+  const P w = ld_tab2(reinterpret_cast<const P*>(row + 2 * ps) + k);
   a[0] = u.x;
   a[1] = u.y;
   a[2] = v.x;
@@ -100,7 +116,57 @@ __device__ __forceinline__ void load_coef6_kp(T* a, const T* __restrict__ row, i
   a[5] = w.y;
 }
 
-// one env row (4 values, 16-byte aligned for float, 32 for double)
+// one row of 4 values (16-byte aligned), not allocated in L1
+__device__ __forceinline__ float4 ld_stream4(const float* p) {
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ dbl4 ld_stream4(const double* p) {
+  dbl4 v;
+  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v.z), "=d"(v.w) : "l"(p + 2));
+  return v;
+}
+__device__ __forceinline__ float ld_stream(const float* p) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_stream(const double* p) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// a row of 4 values read twice by the same warp: first out of L1
+__device__ __forceinline__ float4 ld_first4(const float* p) {
+  float4 v;
+  asm("ld.global.nc.L1::evict_first.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ dbl4 ld_first4(const double* p) {
+  dbl4 v;
+  asm("ld.global.nc.L1::evict_first.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  asm("ld.global.nc.L1::evict_first.v2.f64 {%0, %1}, [%2];" : "=d"(v.z), "=d"(v.w) : "l"(p + 2));
+  return v;
+}
+__device__ __forceinline__ float ld_first(const float* p) {
+  float v;
+  asm("ld.global.nc.L1::evict_first.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_first(const double* p) {
+  double v;
+  asm("ld.global.nc.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// one row of 4 values through the default path (16-byte aligned)
 __device__ __forceinline__ float4 ld_row4(const float* p) {
   return __ldg(reinterpret_cast<const float4*>(p));
 }
@@ -194,35 +260,37 @@ __global__ void __launch_bounds__(kFWarps * 32)
         const TableInfo<T> inf = ts.info[tab_index(ts, t, ti)];
         const T* e0 = em + ((size_t)i * nnei + s0) * 4;
         const T last = e0[(ns - 1) * 4];
+        // every slot up to the first chunk holding the fold point is staged;
+        // the fold slot then takes the weight of the slots it stands for
         int bp = ns;
         for (int b = 0; b < ns; b += 32) {
           const int j = b + lane;
           bool hit = false;
+          V4<T> e;
           if (j < ns) {
-            const T* e = e0 + j * 4;
-            hit = e[0] == last && e[1] == T(0) && e[2] == T(0) && e[3] == T(0);
+            e = ld_stream4(e0 + 4 * j);
+            hit = e.x == last && e.y == T(0) && e.z == T(0) && e.w == T(0);
+            T x = e.x;
+            const int idx = locate_row(inf, x);
+            sl.em[s0 + j] = e;
+            sl.xr[s0 + j] = x;
+            sl.idx[s0 + j] = idx;
           }
           const unsigned mk = __ballot_sync(kFull, hit);
           if (mk) {
             bp = b + __ffs(mk) - 1;
+            if (j == bp) {
+              const T w = T(ns - bp);
+              e.x *= w;
+              e.y *= w;
+              e.z *= w;
+              e.w *= w;
+              sl.em[s0 + j] = e;
+            }
             break;
           }
         }
         jend = bp < ns ? bp + 1 : ns;
-        for (int j = lane; j < jend; j += 32) {
-          const V4<T> e = ld_row4(e0 + 4 * j);
-          const T w = (j == bp) ? T(ns - j) : T(1);
-          T x = e.x;
-          const int idx = locate_row(inf, x);
-          V4<T> ew;
-          ew.x = w * e.x;
-          ew.y = w * e.y;
-          ew.z = w * e.z;
-          ew.w = w * e.w;
-          sl.em[s0 + j] = ew;
-          sl.xr[s0 + j] = x;
-          sl.idx[s0 + j] = idx;
-        }
       }
       if (lane == 0) sl.cnt[t] = jend;
     }
@@ -405,7 +473,7 @@ __global__ void __launch_bounds__(kBWarps * 32)
   T* xTs = reinterpret_cast<T*>(region);
   for (int u = lane; u < 4 * M; u += 32) {
     const int m = u / M, k = u - m * M;
-    xTs[4 * k + m] = X[(size_t)i * 4 * M + u];
+    xTs[4 * k + m] = ld_stream(X + (size_t)i * 4 * M + u);
   }
   __syncwarp();
   const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
@@ -418,7 +486,7 @@ __global__ void __launch_bounds__(kBWarps * 32)
       T g[kAxis];
 #pragma unroll
       for (int a4 = 0; a4 < kAxis; a4 += 4) {
-        const V4<T> v = ld_row4(g_i + k * kAxis + a4);
+        const V4<T> v = ld_first4(g_i + k * kAxis + a4);
         g[a4] = v.x;
         g[a4 + 1] = v.y;
         g[a4 + 2] = v.z;
@@ -447,7 +515,7 @@ __global__ void __launch_bounds__(kBWarps * 32)
     const int h = lane >> 4, kc = lane & 15;
     T s[4] = {T(0), T(0), T(0), T(0)};
     for (int kk = h; kk < M; kk += 2) {
-      const T g = __ldg(g_i + kk * kAxis + kc);
+      const T g = ld_first(g_i + kk * kAxis + kc);
       const V4<T> x4 = xT[kk];
       s[0] += g * x4.x;
       s[1] += g * x4.y;
@@ -485,7 +553,7 @@ __global__ void __launch_bounds__(kBWarps * 32)
     const int nv = filled_prefix(nl_i + s0, ns);
     const TableInfo<T> inf = ts.info[tab_index(ts, t, ti)];
     for (int j = lane; j < nv; j += 32) {
-      const V4<T> e = ld_row4(em + ((size_t)i * nnei + s0 + j) * 4);
+      const V4<T> e = ld_stream4(em + ((size_t)i * nnei + s0 + j) * 4);
       T x = e.x;
       const int idx = locate_row(inf, x);
       sl.em[s0 + j] = e;

@@ -25,15 +25,19 @@
 //   dX        dX = dD X[:, :A] + (dD^T X) padded to M columns, dy = dX / nnei,
 //             kept in shared memory as dy4[k] = (dy_0k, dy_1k, dy_2k, dy_3k);
 //   prepass   table row / offset / env row of every filled slot;
-//   phase 1   8 lanes per neighbour, 4 neighbours per warp instruction, lanes
-//             over k within the group: value and slope of the row polynomial
-//             and the five sums dE/d em[j, 0..3] (+ the x slope term) of the
-//             tabulation gradient (tabulate.cc:158-260), reduced over the 8
-//             lanes by 3 butterfly steps;
+//   phase 1   16 lanes per neighbour, 2 neighbours per warp instruction;
+//             lane t owns outputs k = t + 16 i and keeps their dy in
+//             registers: value and slope of the row polynomial and the five
+//             sums dE/d em[j, 0..3] (+ the x slope term) of the tabulation
+//             gradient (tabulate.cc:158-260), reduced over the 16 lanes by 4
+//             butterfly steps;
 //   phase 2   lanes over filled slots: the env-matrix derivative row is
 //             recomputed from the coordinates (env_mat.cc:122-226) instead of
 //             being stored, and force / virial contributions
-//             (prod_force.cc:22-72, prod_virial.cc:22-68) are scattered.
+//             (prod_force.cc:22-72, prod_virial.cc:22-68) are scattered; the
+//             virial of the atom is summed in FP32 over its neighbours (as
+//             the reference's FPTYPE accumulation) and added to the frame's
+//             FP64 accumulator (9 atomics per atom).
 //   Padding slots carry no coordinate dependence and are skipped.
 #include "common.cuh"
 
@@ -449,10 +453,14 @@ __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
   return (size_t)mp * sizeof(V4<T>) + max_sz(slots_bytes<T>(nnei), (size_t)mp * sizeof(V4<T>));
 }
 
-constexpr int kLanesPerNbr = 8;  // phase 1: lanes per neighbour
+constexpr int kLanesPerNbr = 16;  // phase 1: lanes per neighbour
 
-template <typename T, int NQ>
-__global__ void __launch_bounds__(kBWarps * 32)
+// NK = ceil(M / 16): outputs per lane in phase 1; NQ = ceil(M / 32); U:
+// neighbours in flight per 16-lane group (measured on the 12,288-atom water
+// step: U = 1 at 7 CTAs per SM is faster than U = 2 at 6).
+constexpr int kBwdU = 1;
+template <typename T, int NQ, int NK, int U>
+__global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6) : 1)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
                const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
@@ -564,53 +572,93 @@ __global__ void __launch_bounds__(kBWarps * 32)
   }
   __syncwarp();
 
-  // ---- phase 1: tabulation gradient, 8 lanes per neighbour
+  // ---- phase 1: tabulation gradient, 16 lanes per neighbour
   const int rs = 3 * ts.ps;
   {
-    const int n = lane >> 3, t8 = lane & 7;
+    const int n = lane >> 4, t16 = lane & 15;
+    T dr[NK][4];  // dy of this lane's outputs k = t16 + 16 i
+#pragma unroll
+    for (int q = 0; q < NK; ++q) {
+      const int k = t16 + 16 * q;
+      V4<T> d;
+      if (k < M) {
+        d = dy4[k];
+      } else {
+        d.x = d.y = d.z = d.w = T(0);
+      }
+      dr[q][0] = d.x;
+      dr[q][1] = d.y;
+      dr[q][2] = d.z;
+      dr[q][3] = d.w;
+    }
+    // each 16-lane group carries U neighbours (j0 + n + 2 u) at once, so
+    // that 3 U independent table loads are in flight per output step
     for (int t = 0; t < ts.ntypes; ++t) {
       const int s0 = ts.sec[t], nv = sl.cnt[t];
       const T* tab = ts.table[tab_index(ts, t, ti)];
-      for (int j0 = 0; j0 < nv; j0 += 32 / kLanesPerNbr) {
-        const int j = j0 + n;
-        T p[5] = {T(0), T(0), T(0), T(0), T(0)};
-        if (j < nv) {
-          const V4<T> e = sl.em[s0 + j];
-          const T x = sl.xr[s0 + j];
-          const T* row = tab + (size_t)sl.idx[s0 + j] * rs;
-          for (int k = t8; k < M; k += kLanesPerNbr) {
-            T a[6];
-            load_coef6_kp<T>(a, row, ts.ps, k);
-            const V4<T> d = dy4[k];
+      for (int j0 = 0; j0 < nv; j0 += 2 * U) {
+        T p[U][5];
+        V4<T> e[U];
+        T x[U];
+        const T* row[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          // a slot past the end re-evaluates slot j0 (always filled); its
+          // sums are dropped
+          const int j = j0 + n + 2 * u;
+          const int js = j < nv ? j : j0;
+          e[u] = sl.em[s0 + js];
+          x[u] = sl.xr[s0 + js];
+          row[u] = tab + (size_t)sl.idx[s0 + js] * rs;
+#pragma unroll
+          for (int c = 0; c < 5; ++c) p[u][c] = T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < NK; ++q) {
+          const int k = t16 + 16 * q;
+          if (k >= M) break;
+          T a[U][6];
+#pragma unroll
+          for (int u = 0; u < U; ++u) load_coef6_kp<T>(a[u], row[u], ts.ps, k);
+          const T d[4] = {dr[q][0], dr[q][1], dr[q][2], dr[q][3]};
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
             // value and slope by one Horner sweep (9 FMA)
-            T v = a[5], dv = a[5];
-            v = v * x + a[4];
-            dv = dv * x + v;
-            v = v * x + a[3];
-            dv = dv * x + v;
-            v = v * x + a[2];
-            dv = dv * x + v;
-            v = v * x + a[1];
-            dv = dv * x + v;
-            v = v * x + a[0];
-            p[0] += v * d.x;
-            p[1] += v * d.y;
-            p[2] += v * d.z;
-            p[3] += v * d.w;
-            p[4] += dv * (e.x * d.x + e.y * d.y + e.z * d.z + e.w * d.w);
+            const T xu = x[u];
+            T v = a[u][5], dv = a[u][5];
+            v = v * xu + a[u][4];
+            dv = dv * xu + v;
+            v = v * xu + a[u][3];
+            dv = dv * xu + v;
+            v = v * xu + a[u][2];
+            dv = dv * xu + v;
+            v = v * xu + a[u][1];
+            dv = dv * xu + v;
+            v = v * xu + a[u][0];
+            p[u][0] += v * d[0];
+            p[u][1] += v * d[1];
+            p[u][2] += v * d[2];
+            p[u][3] += v * d[3];
+            p[u][4] += dv * (e[u].x * d[0] + e[u].y * d[1] + e[u].z * d[2] + e[u].w * d[3]);
           }
         }
 #pragma unroll
-        for (int o = 4; o >= 1; o >>= 1)
+        for (int o = 8; o >= 1; o >>= 1)
 #pragma unroll
-          for (int c = 0; c < 5; ++c) p[c] += __shfl_xor_sync(kFull, p[c], o);
-        if (t8 == 0 && j < nv) {
-          V4<T> net;  // dE/d em[j, :]; em_x is em[:, 0]
-          net.x = p[0] + p[4];
-          net.y = p[1];
-          net.z = p[2];
-          net.w = p[3];
-          sl.em[s0 + j] = net;
+          for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int c = 0; c < 5; ++c) p[u][c] += __shfl_xor_sync(kFull, p[u][c], o);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int j = j0 + n + 2 * u;
+          if (t16 == 0 && j < nv) {
+            V4<T> net;  // dE/d em[j, :]; em_x is em[:, 0]
+            net.x = p[u][0] + p[u][4];
+            net.y = p[u][1];
+            net.z = p[u][2];
+            net.w = p[u][3];
+            sl.em[s0 + j] = net;
+          }
         }
       }
     }
@@ -627,9 +675,9 @@ __global__ void __launch_bounds__(kBWarps * 32)
           zi = ext_coord[3 * (eoff + il) + 2];
   const T* isd = inv_std + (size_t)ti * nnei * 4;
   T ci[3] = {T(0), T(0), T(0)};
-  double vir[9];
+  T vir[9];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) vir[q] = 0.;
+  for (int q = 0; q < 9; ++q) vir[q] = T(0);
   for (int t = 0; t < ts.ntypes; ++t) {
     const int s0 = ts.sec[t], nv = sl.cnt[t];
     for (int jj = lane; jj < nv; jj += 32) {
@@ -674,7 +722,7 @@ __global__ void __launch_bounds__(kBWarps * 32)
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) vir[a * 3 + b] += (double)(v3[a] * rr[b]);
+        for (int b = 0; b < 3; ++b) vir[a * 3 + b] += v3[a] * rr[b];
     }
   }
   ci[0] = warp_sum(ci[0]);
@@ -688,8 +736,8 @@ __global__ void __launch_bounds__(kBWarps * 32)
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
-    const double v = warp_sum(vir[q]);
-    if (lane == 0) atomicAdd(vir_acc + f * 9 + q, v);
+    const T v = warp_sum(vir[q]);
+    if (lane == 0) atomicAdd(vir_acc + f * 9 + q, (double)v);
   }
 }
 
@@ -806,12 +854,12 @@ int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow
   return GBDP_OK;
 }
 
-template <typename T, int NQ>
+template <typename T, int NQ, int NK, int U>
 void launch_bwd(dim3 grid, size_t smem, cudaStream_t st, T* force, double* vir_acc, const T* X,
                 const T* dD, const int* drow, const T* em, const int* nlist_ext,
                 const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
                 BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
-  auto kern = k_desc_bwd<T, NQ>;
+  auto kern = k_desc_bwd<T, NQ, NK, U>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kern<<<grid, kBWarps * 32, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
@@ -848,24 +896,28 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
                nnei, smem);
   const dim3 grid((nloc + kBWarps - 1) / kBWarps);
   const T rmin = (T)rcut_smth, rmax = (T)rcut;
-  switch (nq) {
-    case 1:
-      launch_bwd<T, 1>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
-                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
-      break;
-    case 2:
-      launch_bwd<T, 2>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
-                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
-      break;
-    case 3:
-      launch_bwd<T, 3>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
-                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
-      break;
+  const int nk = (M + 15) / 16;
+#define GBDP_BWD_CASE(NKV)                                                                       \
+  case NKV:                                                                                      \
+    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU>(grid, smem, st, force, vir_acc, X, dD, drow, em,   \
+                                             nlist_ext, ext_coord, ext_map, atype, inv_std, geo, \
+                                             ts, rmin, rmax, nloc, nnei, M);                     \
+    break;
+  switch (nk) {
+    GBDP_BWD_CASE(1)
+    GBDP_BWD_CASE(2)
+    GBDP_BWD_CASE(3)
+    GBDP_BWD_CASE(4)
+    GBDP_BWD_CASE(5)
+    GBDP_BWD_CASE(6)
+    GBDP_BWD_CASE(7)
     default:
-      launch_bwd<T, 4>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
-                       ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      launch_bwd<T, 4, 8, kBwdU>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext,
+                             ext_coord, ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei,
+                             M);
       break;
   }
+#undef GBDP_BWD_CASE
   GBDP_CHECK_LAUNCH("se_a_descriptor_bwd");
   return GBDP_OK;
 }

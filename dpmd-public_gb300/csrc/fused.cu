@@ -741,6 +741,43 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
   }
 }
 
+// ------------------------------------------------------- frame energies --
+// E[f] = sum of the per-row energies of frame f, in FP64.  Rows of a frame
+// come in runs (rows are grouped by type, frames in order within a type),
+// so each warp adds one partial per run it sees: a handful of atomics per
+// warp instead of one per row.  Rows with frame -1 (padding) are skipped.
+template <typename T>
+__global__ void k_frame_energy(double* __restrict__ E, const T* __restrict__ ae,
+                               const int* __restrict__ frame_of_row, int nrows) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int f = r < nrows ? frame_of_row[r] : -1;
+  const double v = r < nrows ? (double)ae[r] : 0.;
+  unsigned todo = __ballot_sync(kFull, f >= 0);
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int lf = __shfl_sync(kFull, f, leader);
+    const bool mine = f == lf;
+    const unsigned mk = __ballot_sync(kFull, mine);
+    const double sum = warp_sum(mine ? v : 0.);
+    if (lane == leader) atomicAdd(E + lf, sum);
+    todo &= ~mk;
+  }
+}
+
+template <typename T>
+int frame_energy(double* E, const T* ae, const int* frame_of_row, int nrows, int nframes,
+                 cudaStream_t st) {
+  GBDP_REQUIRE(nrows >= 0 && nframes >= 1, "frame_energy: nrows %d, nframes %d", nrows, nframes);
+  GBDP_REQUIRE(E != nullptr, "frame_energy: null E");
+  cudaMemsetAsync(E, 0, sizeof(double) * (size_t)nframes, st);
+  if (nrows == 0) return GBDP_OK;
+  GBDP_REQUIRE(ae && frame_of_row, "frame_energy: null input");
+  k_frame_energy<T><<<(unsigned)((nrows + 255) / 256), 256, 0, st>>>(E, ae, frame_of_row, nrows);
+  GBDP_CHECK_LAUNCH("frame_energy");
+  return GBDP_OK;
+}
+
 // ------------------------------------------------------ table re-layout --
 // dst[r][p][2k + c] = src[r][6k + 2p + c], zero padding to the plane pitch
 template <typename T>
@@ -946,6 +983,16 @@ extern "C" size_t gbdp_table_planar_row_elems(int last_layer_size, int elem_byte
   if (elem_bytes == 4) return 3 * (size_t)kp_pitch<float>(last_layer_size);
   if (elem_bytes == 8) return 3 * (size_t)kp_pitch<double>(last_layer_size);
   return 0;
+}
+
+extern "C" int gbdp_frame_energy_f32(double* E, const float* ae, const int* frame_of_row,
+                                     int nrows, int nframes, gbdp_stream stream) {
+  return frame_energy<float>(E, ae, frame_of_row, nrows, nframes, (cudaStream_t)stream);
+}
+
+extern "C" int gbdp_frame_energy_f64(double* E, const double* ae, const int* frame_of_row,
+                                     int nrows, int nframes, gbdp_stream stream) {
+  return frame_energy<double>(E, ae, frame_of_row, nrows, nframes, (cudaStream_t)stream);
 }
 
 extern "C" int gbdp_table_to_planar_f32(float* dst, const float* src, int nrow,

@@ -241,8 +241,9 @@ class SeAModel:
             self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side),
             ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), n, b.nframes, M, A,
             _stream()), "se_a_descriptor_bwd")
-        b.energy.zero_()
-        b.energy.index_add_(0, b.frame_of_row, b.ae.to(torch.float64))
+        L.check(getattr(lib, f"gbdp_frame_energy_{self._sfx}")(
+            _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes,
+            _stream()), "frame_energy")
         return b.energy, b.force, b.vir
 
     def fitting_tc(self, b: "Batch"):
@@ -467,13 +468,13 @@ class Batch:
         self.type_rows = [(int(a), int(c0)) for a, c0 in zip(starts, counts)]
         self.row_off_c = (ctypes.c_int * (cfg.ntypes + 1))(*(starts + [s0]))
         drow = np.empty(len(flat), np.int64)
-        fo_row = np.zeros(s0, np.int64)
+        fo_row = np.full(s0, -1, np.int32)  # -1: padding row
         for t in range(cfg.ntypes):
             idx = np.nonzero(flat == t)[0]
             drow[idx] = starts[t] + np.arange(len(idx))
             fo_row[starts[t]:starts[t] + len(idx)] = fo[idx]
         self.drow = torch.tensor(drow, dtype=torch.int32, device=dev)
-        self.frame_of_row = torch.tensor(fo_row, dtype=torch.int64, device=dev)
+        self.frame_of_row = torch.tensor(fo_row, dtype=torch.int32, device=dev)
         n = self.nloc
         nnei = cfg.nnei
         M, A = cfg.neuron[-1], cfg.axis_neuron

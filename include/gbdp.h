@@ -325,6 +325,16 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f64(
     int ntypes, const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,
     int nframes, int last_layer_size, int axis_neuron, gbdp_stream stream);
 
+/* Frame energies of a packed batch: E [nframes] (FP64, zeroed here) = the
+ * sum of the per-row energies ae [nrows] whose frame_of_row [nrows] is the
+ * frame (rows with -1 are skipped).  Device pointers.  The energy reduction
+ * of the reference's model output (atomic energies summed per frame in the
+ * FP64 energy precision, deepmd/pt/model/model/transform_output.py:165,181). */
+GBDP_API int gbdp_frame_energy_f32(double* E, const float* ae, const int* frame_of_row, int nrows,
+                                   int nframes, gbdp_stream stream);
+GBDP_API int gbdp_frame_energy_f64(double* E, const double* ae, const int* frame_of_row,
+                                   int nrows, int nframes, gbdp_stream stream);
+
 /* ------------------------------------------------------------------------
  * Fitting net of one atom type: per-atom energy e = H_L w_out + b_out and
  * dE/dD for every row of D [n, widths[0]] (deepmd/pt/model/task/

@@ -449,8 +449,10 @@ __device__ __forceinline__ int filled_prefix(const int* __restrict__ nl, int ns)
 
 template <typename T>
 __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
-  // dy4 [mp] then a region holding X^T [mp] and later the slot arrays
-  return (size_t)mp * sizeof(V4<T>) + max_sz(slots_bytes<T>(nnei), (size_t)mp * sizeof(V4<T>));
+  // dy4 [mp] and X^T [mp] while dX is formed, then the slot arrays over them
+  // (dy is in registers by then): the smaller the footprint, the more L1 is
+  // left for table rows
+  return max_sz(slots_bytes<T>(nnei), (size_t)2 * mp * sizeof(V4<T>));
 }
 
 constexpr int kLanesPerNbr = 16;  // phase 1: lanes per neighbour
@@ -476,9 +478,8 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
   if (ti < 0) return;
   unsigned char* wbase = smem_raw + (size_t)warp * bwd_warp_bytes<T>(nnei, MP);
   V4<T>* dy4 = reinterpret_cast<V4<T>*>(wbase);
-  unsigned char* region = wbase + (size_t)MP * sizeof(V4<T>);
-  V4<T>* xT = reinterpret_cast<V4<T>*>(region);  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k)
-  T* xTs = reinterpret_cast<T*>(region);
+  V4<T>* xT = dy4 + MP;  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k)
+  T* xTs = reinterpret_cast<T*>(xT);
   for (int u = lane; u < 4 * M; u += 32) {
     const int m = u / M, k = u - m * M;
     xTs[4 * k + m] = ld_stream(X + (size_t)i * 4 * M + u);
@@ -552,9 +553,28 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
     dy4[k] = o;
   }
   __syncwarp();
+  // phase 1 mapping: 16 lanes per neighbour; lane t16 owns outputs
+  // k = t16 + 16 i and keeps their dy in registers from here on
+  const int n = lane >> 4, t16 = lane & 15;
+  T dr[NK][4];
+#pragma unroll
+  for (int q = 0; q < NK; ++q) {
+    const int k = t16 + 16 * q;
+    V4<T> d;
+    if (k < M) {
+      d = dy4[k];
+    } else {
+      d.x = d.y = d.z = d.w = T(0);
+    }
+    dr[q][0] = d.x;
+    dr[q][1] = d.y;
+    dr[q][2] = d.z;
+    dr[q][3] = d.w;
+  }
+  __syncwarp();
 
-  // ---- prepass over filled slots (the slot arrays replace X^T)
-  const Slots<T> sl = carve_slots<T>(region, nnei);
+  // ---- prepass over filled slots (the slot arrays replace dy4 and X^T)
+  const Slots<T> sl = carve_slots<T>(wbase, nnei);
   const int* nl_i = nlist_ext + (size_t)i * nnei;
   for (int t = 0; t < ts.ntypes; ++t) {
     const int s0 = ts.sec[t], ns = ts.sec[t + 1] - s0;
@@ -575,22 +595,6 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
   // ---- phase 1: tabulation gradient, 16 lanes per neighbour
   const int rs = 3 * ts.ps;
   {
-    const int n = lane >> 4, t16 = lane & 15;
-    T dr[NK][4];  // dy of this lane's outputs k = t16 + 16 i
-#pragma unroll
-    for (int q = 0; q < NK; ++q) {
-      const int k = t16 + 16 * q;
-      V4<T> d;
-      if (k < M) {
-        d = dy4[k];
-      } else {
-        d.x = d.y = d.z = d.w = T(0);
-      }
-      dr[q][0] = d.x;
-      dr[q][1] = d.y;
-      dr[q][2] = d.z;
-      dr[q][3] = d.w;
-    }
     // each 16-lane group carries U neighbours (j0 + n + 2 u) at once, so
     // that 3 U independent table loads are in flight per output step
     for (int t = 0; t < ts.ntypes; ++t) {
@@ -835,6 +839,11 @@ void launch_fwd(dim3 grid, size_t smem, cudaStream_t st, T* X, T* D, T* D_lo, co
   auto kern = k_desc_fwd<T, NQF>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the smallest shared-memory carveout that holds the resident CTAs (9 at
+  // 56 registers in FP32): the rest of the unified L1 caches table rows
+  const int per_sm = 9 * (int)(smem + 1024);
+  cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
   kern<<<grid, kFWarps * 32, smem, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
                                          tail_lg);
 }
@@ -899,6 +908,11 @@ void launch_bwd(dim3 grid, size_t smem, cudaStream_t st, T* force, double* vir_a
   auto kern = k_desc_bwd<T, NQ, NK, U>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the smallest shared-memory carveout that holds the resident CTAs: the
+  // rest of the unified L1 caches table rows
+  const int per_sm = 7 * (int)(smem + 1024);
+  cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
   kern<<<grid, kBWarps * 32, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
                                          ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei,
                                          M);

@@ -361,6 +361,11 @@ def main():
     dom = max(kt, key=lambda k: kt[k]["ms"])
     peaks = _peaks()
     roof = roofline(dom, kt[dom], nat, cfg, peaks, args.fit_mode)
+    roof_parts = {}
+    for k in kt:
+        rp = roofline(k, kt[k], nat, cfg, peaks, args.fit_mode)
+        roof_parts[k] = {x: rp[x] for x in ("kernel", "bound", "achieved", "unit", "frac",
+                                            "ms_per_launch", "launches", "traffic") if x in rp}
 
     # ---- plain (uncompressed) drop-in, eager, same frame
     mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
@@ -389,7 +394,7 @@ def main():
            "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                      "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
-           "roofline": roof, "clocks": clk.summary()}
+           "roofline": roof, "roofline_parts": roof_parts, "clocks": clk.summary()}
     if rank == 0:
         import oracle as O
         import composite
@@ -675,14 +680,16 @@ def _peaks():
 
 # algorithmic HBM bytes per local atom of each part (FP32, nnei 138, M 100,
 # A 16): inputs read once, outputs written once
-def _alg_bytes(name, cfg):
+def _alg_bytes(name, cfg, fit_mode="tc-tf32x3"):
     nn, M, A = cfg.nnei, cfg.neuron[-1], cfg.axis_neuron
     f = 4
     if name == "env_nlist":
         # coord + type in; em, nlist (local + ext) out; ghosts ~0.9 x nloc x 16 B
         return 12 + 4 + nn * 4 * f + 2 * nn * 4 + 16
     if name == "desc_fwd":
-        return nn * 4 * f + 4 * M * f + M * A * f + 4  # em in; X, D out
+        # em in; X, D out (D as TF32 hi and lo for the tensor-core fitting)
+        nd = 2 if fit_mode == "tc-tf32x3" else 1
+        return nn * 4 * f + 4 * M * f + nd * M * A * f + 4
     if name == "desc_bwd":
         # X, dE/dD, em, nlist_ext in; ~91 neighbour coords (L2) ; force out
         return 4 * M * f + M * A * f + nn * 4 * f + nn * 4 + 12
@@ -703,6 +710,11 @@ def _fit_flops(cfg):
 PART_KERNEL = {"env_nlist": "k_nlist_env (+ cell build and ghost fill)",
                "desc_fwd": "k_desc_fwd", "desc_bwd": "k_desc_bwd"}
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
+# of the 12,288-atom step (profiles/k_desc_fwd_bwd_12288.md,
+# profiles/k_fit_tc_12288.md: the six k_fit_tc launches averaged)
+NCU_TRAFFIC = {"desc_bwd": 133.1e6, "desc_fwd": 144.6e6, "fitting_gemm": 63.6e6}
+
 
 def roofline(name, t, nat, cfg, peaks, fit_mode):
     ms = t["ms"]
@@ -714,19 +726,20 @@ def roofline(name, t, nat, cfg, peaks, fit_mode):
         peak = peaks["bf16_tflops"]
         out = {"kernel": "k_fit_tc" if tc else f"cuBLAS ({fit_mode}) + k_fit_*", "bound": "tensor",
                "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-               "traffic": None, "peak_src": peaks["src"] + " (dense BF16, burst)",
+               "traffic": NCU_TRAFFIC.get(name) if tc else None,
+               "peak_src": peaks["src"] + " (dense BF16, burst)",
                "alg_flops_per_launch": flops / nl, "launches": nl, "ms_per_launch": ms / nl}
         if tc:
             # FP32 products as 3 TF32 MMAs at half the BF16 rate: 1/6 of peak
             out["ceiling_tf32x3_tflops"] = peak / 6
             out["frac_of_tf32x3_ceiling"] = ach / (peak / 6)
         return out
-    alg = _alg_bytes(name, cfg) * nat
+    alg = _alg_bytes(name, cfg, fit_mode) * nat
     ach = alg / (ms * 1e-3) / 1e9
     return {"kernel": PART_KERNEL.get(name, name), "bound": "hbm", "achieved": ach,
             "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-            "traffic": None, "peak_src": peaks["src"], "alg_bytes_per_launch": alg,
-            "launches": 1, "ms_per_launch": ms}
+            "traffic": NCU_TRAFFIC.get(name), "peak_src": peaks["src"],
+            "alg_bytes_per_launch": alg, "launches": 1, "ms_per_launch": ms}
 
 
 if __name__ == "__main__":

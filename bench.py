@@ -212,12 +212,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline")
-    ap.add_argument("--fit-mode", default="tc-tf32x3",
+    ap.add_argument("--fit-mode", default=None,
                     choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
                              "native-bf16", "tc-tf32x3"],
-                    help="fitting net: tc-tf32x3 (tcgen05 kernel, TF32 hi/lo split), torch GEMMs "
-                         "(fp32, split tf32x3, bf16) or the native call with a cuBLAS compute "
-                         "type (native-*)")
+                    help="fitting net: tc-tf32x3 (tcgen05 kernel, TF32 hi/lo split; default on "
+                         "one GPU), torch GEMMs (fp32, split tf32x3, bf16) or the native call with a "
+                         "cuBLAS compute type (native-*; native-bf16x9 is the default when "
+                         "WORLD_SIZE > 1)")
     ap.add_argument("--workload", default="water12k", choices=["water12k", "ragged512", "md786k"],
                     help="water12k: the headline config; ragged512: 512 ragged frames, batched "
                          "fused graph vs the plain per-frame loop; md786k: 786,432-atom NVE MD")
@@ -227,6 +228,10 @@ def main():
                          "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.fit_mode is None:
+        # the tensor-core fitting stages operands with TMA, which jobs on two or
+        # more GPUs keep out of: replicas there take the cuBLAS BF16x9 fitting
+        args.fit_mode = "tc-tf32x3" if _dist()[0] == 1 else "native-bf16x9"
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "ragged512":

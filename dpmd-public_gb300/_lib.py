@@ -69,6 +69,10 @@ _SIGS = {
     "gbdp_prod_env_mat_a_noalloc_f32": (_I, [_P] * 16 + [_F, _P, _I, _P]),
     "gbdp_fitting_workspace_bytes": (_Z, [_I, _P, _I, _P]),
     "gbdp_fitting_fwd_bwd_f32": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _F, _I, _P, _Z, _P]),
+    "gbdp_prod_env_mat_a_nlist_f32": (_I, [_P] * 10 + [_I, _I, _I, _I, ctypes.c_float,
+                                                        ctypes.c_float, _P, _I, _P]),
+    "gbdp_prod_env_mat_a_nlist_f64": (_I, [_P] * 10 + [_I, _I, _I, _I, ctypes.c_float,
+                                                        ctypes.c_float, _P, _I, _P]),
     "gbdp_frame_energy_f32": (_I, [_P, _P, _P, _I, _I, _P]),
     "gbdp_frame_energy_f64": (_I, [_P, _P, _P, _I, _I, _P]),
     "gbdp_table_planar_row_elems": (ctypes.c_size_t, [_I, _I]),

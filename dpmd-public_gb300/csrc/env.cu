@@ -424,6 +424,75 @@ __device__ __forceinline__ void store4<double>(double* p, double a, double b, do
   *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
 }
 
+// Env row of one slot (env_mat.cc:122-226: s(r) [1/r, x/r^2, y/r^2, z/r^2]
+// and its derivative wrt r_ij), normalised by the centre type's davg/dstd
+// (prod_env_mat.cc:84-100), stored at row o; xj == nullptr: the padding row
+// (0 - avg) / std; centre type < 0: zeros.
+template <typename T>
+__device__ __forceinline__ void env_row_store(const T* xj, T xi, T yi, T zi, int ti,
+                                              const T* av, const T* sd, int s, T rmin, T rmax,
+                                              size_t o, T* em, T* em_deriv, T* rij) {
+  T e[4] = {T(0), T(0), T(0), T(0)};
+  T dv[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) dv[q] = T(0);
+  T rr[3] = {T(0), T(0), T(0)};
+  if (xj) {
+    rr[0] = xj[0] - xi;
+    rr[1] = xj[1] - yi;
+    rr[2] = xj[2] - zi;
+    const T nr2 = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
+    const T inr = T(1) / sqrt(nr2);
+    const T nr = nr2 * inr;
+    const T inr2 = inr * inr;
+    const T inr4 = inr2 * inr2;
+    const T inr3 = inr4 * nr;
+    T sw, dsw;
+    spline5<T>(sw, dsw, nr, rmin, rmax);
+    e[0] = T(1) / nr;
+    e[1] = rr[0] / nr2;
+    e[2] = rr[1] / nr2;
+    e[3] = rr[2] / nr2;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dv[d] = rr[d] * inr3 * sw - e[0] * dsw * rr[d] * inr;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        T t = T(2) * rr[a] * rr[d] * inr4;
+        if (a == d) t -= inr2;
+        dv[3 + a * 3 + d] = t * sw - e[1 + a] * dsw * rr[d] * inr;
+      }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) e[q] *= sw;
+  }
+  T out[4];
+  if (ti >= 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[q] = (e[q] - av[s * 4 + q]) / sd[s * 4 + q];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[q] = T(0);
+  }
+  store4<T>(em + o * 4, out[0], out[1], out[2], out[3]);
+  if (em_deriv) {
+    T* dp = em_deriv + o * 12;
+#pragma unroll
+    for (int q = 0; q < 12; q += 4) {
+      if (ti >= 0)
+        store4<T>(dp + q, dv[q] / sd[s * 4 + q / 3], dv[q + 1] / sd[s * 4 + (q + 1) / 3],
+                  dv[q + 2] / sd[s * 4 + (q + 2) / 3], dv[q + 3] / sd[s * 4 + (q + 3) / 3]);
+      else
+        store4<T>(dp + q, T(0), T(0), T(0), T(0));
+    }
+  }
+  if (rij) {
+    rij[o * 3] = rr[0];
+    rij[o * 3 + 1] = rr[1];
+    rij[o * 3 + 2] = rr[2];
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kEnvWarps * 32)
     k_nlist_env(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
@@ -513,68 +582,113 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   const T* sd = stdv + (size_t)max(ti, 0) * nem;
   for (int s = lane; s < nnei; s += 32) {
     const int j = row[s];
-    T e[4] = {T(0), T(0), T(0), T(0)};
-    T dv[12];
-#pragma unroll
-    for (int q = 0; q < 12; ++q) dv[q] = T(0);
-    T rr[3] = {T(0), T(0), T(0)};
-    if (j >= 0) {
-      rr[0] = ext_coord[3 * (eoff + j)] - xi;
-      rr[1] = ext_coord[3 * (eoff + j) + 1] - yi;
-      rr[2] = ext_coord[3 * (eoff + j) + 2] - zi;
-      const T nr2 = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
-      const T inr = T(1) / sqrt(nr2);
-      const T nr = nr2 * inr;
-      const T inr2 = inr * inr;
-      const T inr4 = inr2 * inr2;
-      const T inr3 = inr4 * nr;
-      T sw, dsw;
-      spline5<T>(sw, dsw, nr, rmin, rmax);
-      e[0] = T(1) / nr;
-      e[1] = rr[0] / nr2;
-      e[2] = rr[1] / nr2;
-      e[3] = rr[2] / nr2;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) dv[d] = rr[d] * inr3 * sw - e[0] * dsw * rr[d] * inr;
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          T t = T(2) * rr[a] * rr[d] * inr4;
-          if (a == d) t -= inr2;
-          dv[3 + a * 3 + d] = t * sw - e[1 + a] * dsw * rr[d] * inr;
-        }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) e[q] *= sw;
-    }
     const size_t o = ((size_t)i * nnei + s);
-    T out[4];
-    if (ti >= 0) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) out[q] = (e[q] - av[s * 4 + q]) / sd[s * 4 + q];
-    } else {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) out[q] = T(0);
-    }
-    store4<T>(em + o * 4, out[0], out[1], out[2], out[3]);
-    if (em_deriv) {
-      T* dp = em_deriv + o * 12;
-#pragma unroll
-      for (int q = 0; q < 12; q += 4) {
-        if (ti >= 0)
-          store4<T>(dp + q, dv[q] / sd[s * 4 + q / 3], dv[q + 1] / sd[s * 4 + (q + 1) / 3],
-                    dv[q + 2] / sd[s * 4 + (q + 2) / 3], dv[q + 3] / sd[s * 4 + (q + 3) / 3]);
-        else
-          store4<T>(dp + q, T(0), T(0), T(0), T(0));
-      }
-    }
-    if (rij) {
-      rij[o * 3] = rr[0];
-      rij[o * 3 + 1] = rr[1];
-      rij[o * 3 + 2] = rr[2];
-    }
+    env_row_store<T>(j >= 0 ? ext_coord + 3 * (eoff + j) : nullptr, xi, yi, zi, ti, av, sd, s,
+                     rmin, rmax, o, em, em_deriv, rij);
     nlist[o] = j >= 0 ? ext_map[eoff + j] : -1;
     if (nlist_ext) nlist_ext[o] = j;
+  }
+}
+
+// ------------------------------------------------------ k_nlist_env_ext --
+// The neighbour list of the PyTorch forward_lower path, formatted from an
+// external candidate list (an MD engine's rcut + skin list, unsorted) as
+// deepmd/pt/model/model/make_model.py:541-598 (_format_nlist with the forced
+// sort a compressed se_e2_a asks for) and deepmd/pt/utils/nlist.py:304-337
+// (nlist_distinguish_types) do: rr = |x_i - x_j| in the coordinate type,
+// rr > rcut dropped, ascending rr (ties by list position), the nearest nnei
+// kept, then the first sel[t] of each type in that order.  One warp per
+// centre; env rows as k_nlist_env.  Indices stay in the extended space.
+template <typename T>
+__device__ __forceinline__ T dist_rn(T dx, T dy, T dz);
+template <>
+__device__ __forceinline__ float dist_rn<float>(float dx, float dy, float dz) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+template <>
+__device__ __forceinline__ double dist_rn<double>(double dx, double dy, double dz) {
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kEnvWarps * 32)
+    k_nlist_env_ext(int nloc, int nall, int nnei_in, int nwork, const T* __restrict__ ext_coord,
+                    const int* __restrict__ ext_type, const int* __restrict__ nlist_in,
+                    const T* __restrict__ avg, const T* __restrict__ stdv, SecInfo si, T rcut,
+                    T rmin, T rmax, T* __restrict__ em, T* __restrict__ em_deriv,
+                    T* __restrict__ rij, int* __restrict__ nlist, int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kEnvWarps + warp;
+  if (i >= nwork) return;
+  const int nnei = si.nnei;
+  const int cap = (nnei_in + 7) & ~7;
+  // per warp: rr [cap] (T), slot row [nnei] (int), type [cap], kept [cap]
+  const size_t per_warp = (size_t)cap * sizeof(T) + (size_t)((nnei + 3) & ~3) * 4 + 2 * (size_t)cap;
+  unsigned char* base = smem + (size_t)warp * ((per_warp + 15) & ~(size_t)15);
+  T* rr = reinterpret_cast<T*>(base);
+  int* row = reinterpret_cast<int*>(base + (size_t)cap * sizeof(T));
+  unsigned char* ctype = base + (size_t)cap * sizeof(T) + (size_t)((nnei + 3) & ~3) * 4;
+  unsigned char* kept = ctype + cap;
+  const int f = i / nloc, il = i - f * nloc;
+  const T* xf = ext_coord + (size_t)f * nall * 3;
+  const int* tf = ext_type + (size_t)f * nall;
+  const int* nl = nlist_in + (size_t)i * nnei_in;
+  const T xi = xf[3 * il], yi = xf[3 * il + 1], zi = xf[3 * il + 2];
+  const int ti = tf[il];
+  const T inf = T(1) / T(0);
+  for (int p = lane; p < nnei_in; p += 32) {
+    const int j = nl[p];
+    T d = inf;
+    int t = 0xff;
+    if (j >= nall) {
+      raise_status(status, GBDP_STATUS_BAD_INDEX);
+    } else if (j >= 0) {
+      d = dist_rn<T>(xi - xf[3 * j], yi - xf[3 * j + 1], zi - xf[3 * j + 2]);
+      if (d > rcut) d = inf;  // dropped, as rr > rcut
+      const int tj = tf[j];
+      t = (tj >= 0 && tj < si.ntypes) ? tj : 0xfe;  // 0xfe: counted, never placed
+    }
+    rr[p] = d;
+    ctype[p] = (unsigned char)t;
+  }
+  for (int s = lane; s < nnei; s += 32) row[s] = -1;
+  __syncwarp();
+  // nearest nnei over all types: rank by (rr, list position)
+  for (int p = lane; p < nnei_in; p += 32) {
+    const T d = rr[p];
+    int rank = 0;
+    if (d != inf)
+      for (int q = 0; q < nnei_in; ++q) {
+        const T e = rr[q];
+        rank += (e < d) | ((e == d) & (q < p));
+      }
+    kept[p] = (d != inf && rank < nnei) ? 1 : 0;
+  }
+  __syncwarp();
+  // section t: the first sel[t] kept neighbours of type t, in the same order
+  for (int p = lane; p < nnei_in; p += 32) {
+    if (!kept[p]) continue;
+    const int t = ctype[p];
+    if (t >= si.ntypes) continue;
+    const T d = rr[p];
+    int rank = 0;
+    for (int q = 0; q < nnei_in; ++q) {
+      const T e = rr[q];
+      rank += kept[q] & (ctype[q] == t) & ((e < d) | ((e == d) & (q < p)));
+    }
+    if (rank < si.sec[t + 1] - si.sec[t]) row[si.sec[t] + rank] = nl[p];
+  }
+  __syncwarp();
+  const int nem = nnei * 4;
+  const T* av = avg + (size_t)max(ti, 0) * nem;
+  const T* sd = stdv + (size_t)max(ti, 0) * nem;
+  for (int s = lane; s < nnei; s += 32) {
+    const int j = row[s];
+    const size_t o = ((size_t)i * nnei + s);
+    env_row_store<T>(j >= 0 ? xf + 3 * j : nullptr, xi, yi, zi, ti, av, sd, s, rmin, rmax, o, em,
+                     em_deriv, rij);
+    nlist[o] = j;
   }
 }
 
@@ -684,6 +798,49 @@ int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_co
       static_cast<const typename XsOf<T>::type*>(w.xs), ext_coord, ext_map, atype, avg, stdv, si,
       rc * rc, (T)rcut_smth, (T)rc, mc, em, em_deriv, rij, nlist, nlist_ext, w.status);
   GBDP_CHECK_LAUNCH("prod_env_mat_a");
+  return GBDP_OK;
+}
+
+template <typename T>
+int env_nlist_launch(T* em, T* em_deriv, T* rij, int* nlist, int* status, const T* ext_coord,
+                     const int* ext_type, const int* nlist_in, const T* avg, const T* stdv,
+                     int nframes, int nloc, int nall, int nnei_in, float rcut, float rcut_smth,
+                     const int* sel, int ntypes, cudaStream_t stream) {
+  GBDP_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, "prod_env_mat_a_nlist: ntypes %d out of [1,%d]",
+               ntypes, kMaxTypes);
+  GBDP_REQUIRE(nframes >= 0 && nloc >= 0 && nall >= nloc && nnei_in >= 0 && nnei_in <= 4096,
+               "prod_env_mat_a_nlist: nframes %d nloc %d nall %d nnei_in %d", nframes, nloc, nall,
+               nnei_in);
+  GBDP_REQUIRE(sel != nullptr, "prod_env_mat_a_nlist: null sel");
+  SecInfo si;
+  si.ntypes = ntypes;
+  si.sec[0] = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    GBDP_REQUIRE(sel[t] >= 0, "prod_env_mat_a_nlist: negative sel");
+    si.sec[t + 1] = si.sec[t] + sel[t];
+  }
+  si.nnei = si.sec[ntypes];
+  GBDP_REQUIRE(si.nnei > 0, "prod_env_mat_a_nlist: sum(sel) must be positive");
+  const long nwork = (long)nframes * nloc;
+  if (nwork == 0) return GBDP_OK;
+  GBDP_REQUIRE(nwork < (1l << 31), "prod_env_mat_a_nlist: too many centres");
+  GBDP_REQUIRE(em && nlist && ext_coord && ext_type && (nlist_in || nnei_in == 0) && avg && stdv,
+               "prod_env_mat_a_nlist: null required pointer");
+  GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && (!em_deriv || ((uintptr_t)em_deriv & 15) == 0),
+               "prod_env_mat_a_nlist: em / em_deriv must be 16-byte aligned");
+  if (status) cudaMemsetAsync(status, 0, sizeof(int), stream);
+  const int cap = (nnei_in + 7) & ~7;
+  const size_t per_warp = (size_t)cap * sizeof(T) + (size_t)((si.nnei + 3) & ~3) * 4 + 2 * (size_t)cap;
+  const size_t smem = (size_t)kEnvWarps * ((per_warp + 15) & ~(size_t)15);
+  GBDP_REQUIRE(smem <= 200 * 1024, "prod_env_mat_a_nlist: nnei_in %d needs too much shared memory",
+               nnei_in);
+  auto kern = k_nlist_env_ext<T>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<(unsigned)((nwork + kEnvWarps - 1) / kEnvWarps), kEnvWarps * 32, smem, stream>>>(
+      nloc, nall, nnei_in, (int)nwork, ext_coord, ext_type, nlist_in, avg, stdv, si, (T)rcut,
+      (T)rcut_smth, (T)rcut, em, em_deriv, rij, nlist, status);
+  GBDP_CHECK_LAUNCH("prod_env_mat_a_nlist");
   return GBDP_OK;
 }
 
@@ -829,6 +986,20 @@ extern "C" int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij
                             ext_nall, coord, atype, avg, std, plan, frames_dev, rcut_smth, sel,
                             ntypes, workspace, workspace_bytes, (cudaStream_t)stream);
 }
+
+#define GBDP_ENV_NLIST_ENTRY(T, SFX)                                                           \
+  extern "C" int gbdp_prod_env_mat_a_nlist_##SFX(                                              \
+      T* em, T* em_deriv, T* rij, int* nlist, int* status, const T* ext_coord,                 \
+      const int* ext_type, const int* nlist_in, const T* avg, const T* std, int nframes,       \
+      int nloc, int nall, int nnei_in, float rcut, float rcut_smth, const int* sel, int ntypes, \
+      gbdp_stream stream) {                                                                    \
+    return env_nlist_launch<T>(em, em_deriv, rij, nlist, status, ext_coord, ext_type, nlist_in, \
+                               avg, std, nframes, nloc, nall, nnei_in, rcut, rcut_smth, sel,    \
+                               ntypes, (cudaStream_t)stream);                                   \
+  }
+GBDP_ENV_NLIST_ENTRY(float, f32)
+GBDP_ENV_NLIST_ENTRY(double, f64)
+#undef GBDP_ENV_NLIST_ENTRY
 
 // ------------------------------------------------ allocation-free variant --
 // Scratch for gbdp_prod_env_mat_a_noalloc_f32: a file-scope device array, so

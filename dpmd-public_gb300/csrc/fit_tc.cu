@@ -10,7 +10,8 @@
 // kb % 3, the two small cross terms to a fourth accumulator, and the
 // epilogue adds the four in IEEE FP32.
 //
-// One kernel computes a 128 x 80 tile of C = A B for one layer; its fused
+// One kernel computes a 128-row tile of C = A B for one layer (tile widths
+// per layer in the TcCfg configurations below); its fused
 // epilogue applies the layer's activation (forward) or gradient chain
 // (backward) and writes the next GEMM's A operand already split, so the
 // whole per-type fitting net (deepmd/pt/model/task/fitting.py:734-899,
@@ -35,17 +36,35 @@
 namespace gbdp {
 namespace {
 
-constexpr int TBM = 128, TBN = 80, TBK = 32;
-constexpr int A_TILE = TBM * TBK * 4;                // 16 KiB
-constexpr int B_TILE = TBN * TBK * 4;                // 10 KiB
-constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;       // 52 KiB
-constexpr uint32_t ACC_COLS = 128;                   // TMEM columns per accumulator (>= TBN)
-// Two configurations: long K (the 1600-wide layer) with 4 pipeline stages
-// and 3 main accumulators (one CTA per SM: 214 KB shared, 512 TMEM
-// columns); short K (<= 256) with 2 stages and 1 main accumulator, so that
-// two CTAs share an SM (105 KB shared, 256 TMEM columns each) and one's
-// epilogue overlaps the other's main loop.
-constexpr int tc_smem(int stages) { return stages * STAGE + 1024 + 256; }
+constexpr int TBM = 128, TBK = 32;
+constexpr int A_TILE = TBM * TBK * 4;  // 16 KiB
+
+// Tile configurations.  The layers are too small to fill 152 SMs with wide
+// tiles, and a CTA's TMA -> MMA pipeline is latency-bound, so narrow tiles
+// with two CTAs per SM (one CTA's epilogue overlapping the other's main
+// loop) measured fastest on the 12,288-row step (128 x 240 tiles: the K-240
+// layers 28-37 us instead of 21-24 us; 128 x 160 for the 1600-wide layer:
+// 78 us instead of 75 us):
+//   CfgLongK   F1 (K 1600): 4 stages, 3 main accumulators, one CTA per SM
+//              (214 KB shared, 512 TMEM columns); the 3 accumulators keep
+//              the long chain FP32-accurate
+//   CfgShortK  K 240 layers: 2 stages, 1 main accumulator, two CTAs per SM
+//              (105 KB shared, 256 TMEM columns each)
+template <int TBN_, int STAGES_, int NACC_>
+struct TcCfg {
+  static constexpr int TBN = TBN_, STAGES = STAGES_, NACC = NACC_;
+  static constexpr int B_TILE = TBN * TBK * 4;
+  static constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;
+  static constexpr uint32_t ACC_COLS = TBN <= 128 ? 128 : 256;  // TMEM columns per accumulator
+  static constexpr int TMEM_COLS = (NACC + 1) * (int)ACC_COLS;   // NACC main + 1 cross-term
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;       // + alignment slack + barriers
+  static_assert(TBN % 16 == 0 && TBN <= 256, "tcgen05 M=128 needs N % 16 == 0, N <= 256");
+  // CTAs that fit an SM by shared memory must also fit its 512 TMEM columns
+  static_assert((228 * 1024 / SMEM) * TMEM_COLS <= 512, "TMEM over-subscribed");
+  static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
+};
+using CfgLongK = TcCfg<80, 4, 3>;
+using CfgShortK = TcCfg<80, 2, 1>;
 constexpr int FIT_W = 240;                           // hidden width this kernel serves
 constexpr int FIT_D = 1600;                          // descriptor width this kernel serves
 
@@ -212,10 +231,12 @@ __device__ __forceinline__ void col_ld16(const float* p, float* v) {
 }
 
 // ------------------------------------------------------------- kernel --
-template <int TSTAGES, int NACC>
+template <class C>
 __global__ void __launch_bounds__(128, 1)
     k_fit_tc(const __grid_constant__ TcMaps maps, const __grid_constant__ TcEpi ep, int K) {
-  constexpr int TMEM_COLS = (NACC + 1) * (int)ACC_COLS;  // NACC main + 1 cross-term
+  constexpr int TSTAGES = C::STAGES, NACC = C::NACC, TBN = C::TBN, STAGE = C::STAGE,
+                B_TILE = C::B_TILE, TMEM_COLS = C::TMEM_COLS;
+  constexpr uint32_t ACC_COLS = C::ACC_COLS;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -303,7 +324,7 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_after();
   float esum = 0.f;
   if (got) {
-    static_assert(4 * EPI_WARP_BYTES <= 2 * STAGE, "epilogue staging exceeds the stage buffers");
+    static_assert(4 * EPI_WARP_BYTES <= TSTAGES * STAGE, "epilogue staging exceeds the stage buffers");
     unsigned char* wsm = smem + warp * EPI_WARP_BYTES;
     float* inb = reinterpret_cast<float*>(wsm);                  // [2 buf][2 arr][chunk]
     float* outb = reinterpret_cast<float*>(wsm + EPI_IN_BYTES);  // [2 buf][3 arr][chunk]
@@ -523,7 +544,7 @@ TcWs carve_tc(void* base, long rows) {
   w.gz2l = take(act);
   w.gz1h = take(act);
   w.gz1l = take(act);
-  w.epart = take(sizeof(float) * (size_t)rows * (FIT_W / TBN));
+  w.epart = take(sizeof(float) * (size_t)rows * (FIT_W / 80));
   w.bytes = off;
   return w;
 }
@@ -566,14 +587,16 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
   int* status = reinterpret_cast<int*>(static_cast<char*>(workspace) + ws.bytes);
   cudaStream_t st = (cudaStream_t)stream;
   cudaMemsetAsync(status, 0, sizeof(int) * 4, st);
-  cudaFuncSetAttribute(k_fit_tc<4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(4));
-  cudaFuncSetAttribute(k_fit_tc<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(2));
+  cudaFuncSetAttribute(k_fit_tc<CfgLongK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       CfgLongK::SMEM);
+  cudaFuncSetAttribute(k_fit_tc<CfgShortK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       CfgShortK::SMEM);
   GBDP_REQUIRE(rows / TBM <= 65535, "fit_tc: %ld rows exceed the grid limit", rows);
   TcEpi base{};
   base.ntypes = ntypes;
   for (int t = 0; t <= ntypes; ++t) base.row_off[t] = row_off[t];
   base.status = status;
-  base.ntile_n = FIT_W / TBN;
+  base.ntile_n = FIT_W / CfgShortK::TBN;  // F3's N tiles
   for (int t = 0; t < ntypes; ++t) {
     base.wout[t] = nets[t].w_out;
     const float* cols[4] = {nets[t].w_out, nets[t].b[0], nets[t].b[1], nets[t].b[2]};
@@ -582,6 +605,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     GBDP_REQUIRE(((uintptr_t)nets[t].idt[1] & 15) == 0 && ((uintptr_t)nets[t].idt[2] & 15) == 0,
                  "fit_tc: idt not 16-byte aligned");
   }
+  enum { LONGK = 0, SHORTK };
   struct Step {
     int kind;
     const float *a_hi, *a_lo;
@@ -589,18 +613,24 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     bool fwd;
     const float* in[2];
     float* out[3];
+    int cfg;
   };
+  static_assert(FIT_W % CfgShortK::TBN == 0 && FIT_W % CfgLongK::TBN == 0 &&
+                    FIT_D % CfgShortK::TBN == 0,
+                "tile widths must divide the layer widths");
   const Step steps[6] = {
-      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}},
-      {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.h1h, ws.h1l}, {ws.t2, ws.h2h, ws.h2l}},
+      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l},
+       LONGK},
+      {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.h1h, ws.h1l}, {ws.t2, ws.h2h, ws.h2l},
+       SHORTK},
       {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true, {ws.h2h, ws.h2l},
-       {nullptr, ws.gz3h, ws.gz3l}},
+       {nullptr, ws.gz3h, ws.gz3l}, SHORTK},
       {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false, {ws.t2, nullptr},
-       {ws.g2, ws.gz2h, ws.gz2l}},
+       {ws.g2, ws.gz2h, ws.gz2l}, SHORTK},
       {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false, {ws.t1, ws.g2},
-       {nullptr, ws.gz1h, ws.gz1l}},
+       {nullptr, ws.gz1h, ws.gz1l}, SHORTK},
       {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false, {nullptr, nullptr},
-       {dE_dD, nullptr, nullptr}}};
+       {dE_dD, nullptr, nullptr}, SHORTK}};
   for (const Step& sp : steps) {
     TcMaps maps;
     memset(&maps, 0, sizeof(maps));
@@ -611,8 +641,9 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
       // forward B = W_l^T [out, in]; backward B = W_l [in, out]: both K-major
       const float* bh = sp.fwd ? n.wt_hi[sp.layer] : n.w_hi[sp.layer];
       const float* bl = sp.fwd ? n.wt_lo[sp.layer] : n.w_lo[sp.layer];
-      rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, TBN);
-      if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, TBN);
+      const int tbn = sp.cfg == LONGK ? CfgLongK::TBN : CfgShortK::TBN;
+      rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, tbn);
+      if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, tbn);
     }
     TcEpi ep = base;
     ep.kind = sp.kind;
@@ -637,11 +668,12 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     if (sp.kind == EPI_B3)
       for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
     if (sp.kind == EPI_F3) ep.epart = ws.epart;
-    const dim3 grid((unsigned)(sp.N / TBN), (unsigned)(rows / TBM));
-    if (sp.K > 256)
-      k_fit_tc<4, 3><<<grid, 128, tc_smem(4), st>>>(maps, ep, sp.K);
+    if (sp.cfg == LONGK)
+      k_fit_tc<CfgLongK><<<dim3(sp.N / CfgLongK::TBN, (unsigned)(rows / TBM)), 128,
+                           CfgLongK::SMEM, st>>>(maps, ep, sp.K);
     else
-      k_fit_tc<2, 1><<<grid, 128, tc_smem(2), st>>>(maps, ep, sp.K);
+      k_fit_tc<CfgShortK><<<dim3(sp.N / CfgShortK::TBN, (unsigned)(rows / TBM)), 128,
+                            CfgShortK::SMEM, st>>>(maps, ep, sp.K);
     GBDP_CHECK_LAUNCH("fit_tc gemm");
   }
   TcRows rw{};

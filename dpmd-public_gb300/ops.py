@@ -12,6 +12,9 @@ Schemas:
     (source/op/tf/prod_env_mat_multi_device.cc:11-28), ProdForceSeA
     (source/op/tf/prod_force_multi_device.cc:6-14) and ProdVirialSeA
     (source/op/tf/prod_virial_multi_device.cc:5-15).
+  * ``prod_env_mat_a_nlist`` — the same outputs from an external neighbour
+    list (the forward_lower path: extended coordinates and an unsorted
+    rcut + skin list from an MD engine), formatted as the PyTorch model does.
   * ``enable_mpi() -> Tensor`` — present because deepmd/pt/cxx_op.py probes
     it (source/op/pt/print_summary.cc:14); always false here.
 
@@ -31,6 +34,10 @@ _P = ctypes.c_void_p
 
 
 def _ptr(t: torch.Tensor | None):
+    """Device address for a library call.  The tensor must stay referenced
+    until the call has been enqueued: pass locals, never temporaries such as
+    ``x.to(dtype)``, whose memory the caching allocator may hand to the next
+    temporary before the kernel runs."""
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
@@ -97,8 +104,9 @@ def tabulate_grad(table, table_info, em_x, em, dy):
     gx = torch.empty_like(em_x)
     gm = torch.empty_like(em)
     info = _host_info(table_info, dt, table)
+    table = table.contiguous()
     fn = getattr(L.load(), f"gbdp_tabulate_fusion_se_a_grad_{L.sfx(dt)}")
-    L.check(fn(_ptr(gx), _ptr(gm), _ptr(table.contiguous()), info, _ptr(em_x), _ptr(em), _ptr(dy),
+    L.check(fn(_ptr(gx), _ptr(gm), _ptr(table), info, _ptr(em_x), _ptr(em), _ptr(dy),
                nloc, nnei, dy.shape[2], 1, _stream()), "tabulate_fusion_se_a_grad")
     return gx, gm
 
@@ -111,10 +119,12 @@ def tabulate_grad_grad(table, table_info, em_x, em, dz_dem_x, dz_dem, last_layer
     nloc, nnei = em.shape[0], em.shape[1]
     dz = torch.empty((nloc, 4, last_layer_size), dtype=dt, device=table.device)
     info = _host_info(table_info, dt, table)
+    table = table.contiguous()
+    dz_dem_x = dz_dem_x.to(dt).contiguous()
+    dz_dem = dz_dem.to(dt).contiguous()
     fn = getattr(L.load(), f"gbdp_tabulate_fusion_se_a_grad_grad_{L.sfx(dt)}")
-    L.check(fn(_ptr(dz), _ptr(table.contiguous()), info, _ptr(em_x), _ptr(em),
-               _ptr(dz_dem_x.to(dt).contiguous()), _ptr(dz_dem.to(dt).contiguous()), nloc, nnei,
-               int(last_layer_size), 1, _stream()), "tabulate_fusion_se_a_grad_grad")
+    L.check(fn(_ptr(dz), _ptr(table), info, _ptr(em_x), _ptr(em), _ptr(dz_dem_x), _ptr(dz_dem),
+               nloc, nnei, int(last_layer_size), 1, _stream()), "tabulate_fusion_se_a_grad_grad")
     return dz
 
 
@@ -289,6 +299,49 @@ def prod_env_mat_a_impl(coord, atype, natoms, box, mesh, davg, dstd, rcut_a: flo
             r.rij.reshape(nf, nloc * nnei * 3), r.nlist.reshape(nf, nloc * nnei)]
 
 
+def prod_env_mat_a_nlist_impl(coord, atype, nlist, davg, dstd, rcut: float, rcut_smth: float,
+                              sel):
+    """prod_env_mat_a from an external neighbour list (the forward_lower
+    path): coord [nf, nall * 3] or [nf, nall, 3] extended coordinates with the
+    nloc local atoms first, type [nf, nall], nlist [nf, nloc, nnei_in]
+    extended indices (-1 padding, unsorted, rcut + skin allowed).  Formats
+    the list as deepmd/pt/model/model/make_model.py:541-598 with the forced
+    sort, then deepmd/pt/utils/nlist.py:304-337, and returns the ProdEnvMatA
+    outputs (descrpt, descrpt_deriv, rij, nlist) with nlist in the extended
+    index space."""
+    _need_cuda(coord, atype, nlist, davg, dstd)
+    nf, nloc, nnei_in = (int(x) for x in nlist.shape)
+    dt = coord.dtype
+    nall = coord.reshape(nf, -1).shape[1] // 3
+    if atype.reshape(nf, -1).shape[1] != nall:
+        raise RuntimeError("type must have nall entries per frame")
+    sel = [int(x) for x in sel]
+    nnei = sum(sel)
+    dev = coord.device
+    em = torch.empty((nf, nloc * nnei * 4), dtype=dt, device=dev)
+    emd = torch.empty((nf, nloc * nnei * 12), dtype=dt, device=dev)
+    rij = torch.empty((nf, nloc * nnei * 3), dtype=dt, device=dev)
+    nl_out = torch.empty((nf, nloc * nnei), dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    sel_c = (ctypes.c_int * len(sel))(*sel)
+    # converted copies stay referenced until the launch is enqueued
+    coord = coord.contiguous()
+    atype = atype.to(torch.int32).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    davg = davg.to(dt).contiguous()
+    dstd = dstd.to(dt).contiguous()
+    fn = getattr(L.load(), f"gbdp_prod_env_mat_a_nlist_{L.sfx(dt)}")
+    L.check(fn(_ptr(em), _ptr(emd), _ptr(rij), _ptr(nl_out), _ptr(status), _ptr(coord),
+               _ptr(atype), _ptr(nlist), _ptr(davg), _ptr(dstd), nf, nloc, nall, nnei_in,
+               ctypes.c_float(rcut), ctypes.c_float(rcut_smth), sel_c, len(sel), _stream()),
+            "prod_env_mat_a_nlist")
+    st = int(status.item())
+    if st:
+        raise L.GbdpError(f"prod_env_mat_a_nlist device status {st}: "
+                          f"{L.GBDP_STATUS.get(st, '?')}")
+    return [em, emd, rij, nl_out]
+
+
 def prod_force_se_a_impl(net_deriv, in_deriv, nlist, natoms, n_a_sel: int, n_r_sel: int,
                          deterministic: bool = False):
     _need_cuda(net_deriv, in_deriv, nlist)
@@ -302,8 +355,10 @@ def prod_force_se_a_impl(net_deriv, in_deriv, nlist, natoms, n_a_sel: int, n_r_s
     wsb = int(lib.gbdp_prod_workspace_bytes(nf, nloc, nall, nnei, int(deterministic)))
     ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=net_deriv.device)
     fn = getattr(lib, f"gbdp_prod_force_a_{L.sfx(dt)}")
-    L.check(fn(_ptr(force), _ptr(net_deriv.contiguous()), _ptr(in_deriv.to(dt).contiguous()),
-               _ptr(nlist.to(torch.int32).contiguous()), nloc, nall, nnei, nf,
+    net_deriv = net_deriv.contiguous()
+    in_deriv = in_deriv.to(dt).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    L.check(fn(_ptr(force), _ptr(net_deriv), _ptr(in_deriv), _ptr(nlist), nloc, nall, nnei, nf,
                int(deterministic), _ptr(ws), ctypes.c_size_t(wsb), _stream()), "prod_force_se_a")
     return force
 
@@ -322,11 +377,13 @@ def prod_virial_se_a_impl(net_deriv, in_deriv, rij, nlist, natoms, n_a_sel: int,
     wsb = int(lib.gbdp_prod_workspace_bytes(nf, nloc, nall, nnei, int(deterministic)))
     ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=net_deriv.device)
     fn = getattr(lib, f"gbdp_prod_virial_a_{L.sfx(dt)}")
-    L.check(fn(_ptr(virial), _ptr(atom_virial), _ptr(net_deriv.contiguous()),
-               _ptr(in_deriv.to(dt).contiguous()), _ptr(rij.to(dt).contiguous()),
-               _ptr(nlist.to(torch.int32).contiguous()), nloc, nall, nnei, nf,
-               int(deterministic), _ptr(ws), ctypes.c_size_t(wsb), _stream()),
-            "prod_virial_se_a")
+    net_deriv = net_deriv.contiguous()
+    in_deriv = in_deriv.to(dt).contiguous()
+    rij = rij.to(dt).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    L.check(fn(_ptr(virial), _ptr(atom_virial), _ptr(net_deriv), _ptr(in_deriv), _ptr(rij),
+               _ptr(nlist), nloc, nall, nnei, nf, int(deterministic), _ptr(ws),
+               ctypes.c_size_t(wsb), _stream()), "prod_virial_se_a")
     return virial, atom_virial
 
 
@@ -334,8 +391,10 @@ def prod_force_grad_impl(grad, in_deriv, nlist, nloc, nnei, nf):
     dt = grad.dtype
     out = torch.empty((nf, nloc * nnei * 4), dtype=dt, device=grad.device)
     fn = getattr(L.load(), f"gbdp_prod_force_grad_a_{L.sfx(dt)}")
-    L.check(fn(_ptr(out), _ptr(grad.contiguous()), _ptr(in_deriv.contiguous()),
-               _ptr(nlist.to(torch.int32).contiguous()), nloc, nnei, nf, _stream()),
+    grad = grad.contiguous()
+    in_deriv = in_deriv.to(dt).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    L.check(fn(_ptr(out), _ptr(grad), _ptr(in_deriv), _ptr(nlist), nloc, nnei, nf, _stream()),
             "prod_force_grad_a")
     return out
 
@@ -344,8 +403,11 @@ def prod_virial_grad_impl(grad, in_deriv, rij, nlist, nloc, nnei, nf):
     dt = grad.dtype
     out = torch.empty((nf, nloc * nnei * 4), dtype=dt, device=grad.device)
     fn = getattr(L.load(), f"gbdp_prod_virial_grad_a_{L.sfx(dt)}")
-    L.check(fn(_ptr(out), _ptr(grad.contiguous()), _ptr(in_deriv.contiguous()),
-               _ptr(rij.contiguous()), _ptr(nlist.to(torch.int32).contiguous()), nloc, nnei, nf,
+    grad = grad.contiguous()
+    in_deriv = in_deriv.to(dt).contiguous()
+    rij = rij.to(dt).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    L.check(fn(_ptr(out), _ptr(grad), _ptr(in_deriv), _ptr(rij), _ptr(nlist), nloc, nnei, nf,
                _stream()), "prod_virial_grad_a")
     return out
 
@@ -421,6 +483,9 @@ def register() -> None:
     _def("prod_env_mat_a(Tensor coord, Tensor type, Tensor natoms, Tensor box, Tensor mesh, "
          "Tensor davg, Tensor dstd, float rcut_a, float rcut_r, float rcut_r_smth, int[] sel_a, "
          "int[] sel_r) -> Tensor[]", prod_env_mat_a_impl)
+    _def("prod_env_mat_a_nlist(Tensor coord, Tensor type, Tensor nlist, Tensor davg, "
+         "Tensor dstd, float rcut, float rcut_smth, int[] sel) -> Tensor[]",
+         prod_env_mat_a_nlist_impl)
     _def("prod_force_se_a(Tensor net_deriv, Tensor in_deriv, Tensor nlist, Tensor natoms, "
          "int n_a_sel, int n_r_sel) -> Tensor",
          lambda net_deriv, in_deriv, nlist, natoms, n_a_sel, n_r_sel: ProdForceFn.apply(

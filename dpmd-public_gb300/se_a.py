@@ -345,6 +345,42 @@ class SeAModel:
         return E, torch.cat(forces), torch.stack(virs).to(torch.float64)
 
 
+    def step_lower(self, ext_coord: torch.Tensor, ext_atype: torch.Tensor,
+                   nlist: torch.Tensor, mapping: torch.Tensor, nloc: int,
+                   compressed: bool = True):
+        """The forward_lower path of one frame (deepmd/pt/model/model/
+        make_model.py:334-415, called by DeepPotPT::compute): extended
+        coordinates [nall, 3] with the local atoms first, extended types,
+        an external neighbour list [nloc, nnei_in] (unsorted, rcut + skin)
+        and the extended -> local mapping.  Env matrix through
+        prod_env_mat_a_nlist, descriptor and fitting as the operator form,
+        forces on the extended atoms folded back to the local ones through
+        the mapping (communicate_extended_output,
+        deepmd/pt/model/model/transform_output.py:317-380).
+        Returns E (FP64 scalar), F [nloc, 3], virial [9] (FP64)."""
+        cfg = self.cfg
+        nnei = cfg.nnei
+        nall = ext_atype.numel()
+        em, emd, rij, nl = torch.ops.deepmd.prod_env_mat_a_nlist(
+            ext_coord.reshape(1, -1), ext_atype.reshape(1, -1), nlist.reshape(1, nloc, -1),
+            self.davg, self.dstd, cfg.rcut, cfg.rcut_smth, list(cfg.sel))
+        em = em.reshape(nloc, nnei, 4).detach().requires_grad_(True)
+        atype = ext_atype[:nloc].to(torch.int32)
+        D = self._descriptor_from_em(em, atype, compressed)
+        E_atom = torch.zeros(nloc, dtype=self.dtype, device=self.device)
+        for t in range(cfg.ntypes):
+            idx = torch.nonzero(atype == t).reshape(-1)
+            if idx.numel():
+                E_atom = E_atom.index_add(0, idx, self.fitting_energy(t, D.index_select(0, idx)))
+        net = torch.autograd.grad(E_atom.sum(), em)[0].reshape(1, -1)
+        natoms = torch.tensor([nloc, nall] + [0] * cfg.ntypes, dtype=torch.int32)
+        f_ext = prod_force_se_a_impl(net, emd, nl, natoms, nnei, 0).reshape(nall, 3)
+        vir, _ = prod_virial_se_a_impl(net, emd, rij, nl, natoms, nnei, 0)
+        F = torch.zeros((nloc, 3), dtype=self.dtype, device=self.device)
+        F.index_add_(0, mapping.to(torch.int64), f_ext)
+        return E_atom.detach().to(torch.float64).sum(), F, vir.reshape(9).to(torch.float64)
+
+
 def _rn_tf32(x: torch.Tensor) -> torch.Tensor:
     """x rounded to TF32 (10 explicit mantissa bits): to nearest, ties away
     from zero, on the magnitude bits of the FP32 pattern."""

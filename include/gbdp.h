@@ -177,6 +177,40 @@ GBDP_API int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij, 
                             int ntypes, void* workspace, size_t workspace_bytes,
                             gbdp_stream stream);
 
+/* prod_env_mat_a from an external neighbour list: the forward_lower path of
+ * the PyTorch model (an MD engine hands over extended coordinates and an
+ * unsorted rcut + skin list).  Replaces the descriptor's own formatting and
+ * env matrix there: deepmd/pt/model/model/make_model.py:541-598 (_format_nlist
+ * with the forced sort a compressed se_e2_a asks for,
+ * need_sorted_nlist_for_lower in deepmd/pt/model/descriptor/se_a.py:872-883),
+ * deepmd/pt/utils/nlist.py:304-337 (nlist_distinguish_types), then the env
+ * rows of env_mat_a_cpu (source/lib/src/env_mat.cc:122-226) normalised as
+ * prod_env_mat.cc:84-100.  Per frame f and local atom i (the first nloc
+ * extended atoms): the listed j >= 0 at rr = |x_i - x_j| (coordinate type),
+ * rr > rcut dropped, ascending rr (ties by list position), the nearest
+ * sum(sel) kept, then the first sel[t] of type t fill section t.
+ * Device inputs: ext_coord [nframes, nall, 3], ext_type [nframes, nall],
+ * nlist_in [nframes, nloc, nnei_in] (extended indices, -1 padding,
+ * nnei_in <= 4096), avg/std [ntypes, sum(sel) * 4]; sel on the host.
+ * Outputs: em [nframes * nloc, sum(sel) * 4], em_deriv (x3, may be NULL),
+ * rij (x3/4, may be NULL), nlist [nframes * nloc, sum(sel)] in the extended
+ * index space; status (device int, may be NULL) becomes
+ * GBDP_STATUS_BAD_INDEX if a listed index is >= nall. */
+GBDP_API int gbdp_prod_env_mat_a_nlist_f32(float* em, float* em_deriv, float* rij, int* nlist,
+                                           int* status, const float* ext_coord,
+                                           const int* ext_type, const int* nlist_in,
+                                           const float* avg, const float* std, int nframes,
+                                           int nloc, int nall, int nnei_in, float rcut,
+                                           float rcut_smth, const int* sel, int ntypes,
+                                           gbdp_stream stream);
+GBDP_API int gbdp_prod_env_mat_a_nlist_f64(double* em, double* em_deriv, double* rij,
+                                           int* nlist, int* status, const double* ext_coord,
+                                           const int* ext_type, const int* nlist_in,
+                                           const double* avg, const double* std, int nframes,
+                                           int nloc, int nall, int nnei_in, float rcut,
+                                           float rcut_smth, const int* sel, int ntypes,
+                                           gbdp_stream stream);
+
 /* Allocation-free variant of gbdp_prod_env_mat_a_f32 (float only).  It has
  * no counterpart in the reference.  It is for callers that cannot allocate
  * device memory at the point of the call: a host MD engine that owns all

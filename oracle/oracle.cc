@@ -627,6 +627,67 @@ int prod_env_mat_a_pbc(T* em, T* em_deriv, T* rij, int* nlist, const T* coord,
   return 0;
 }
 
+// ------------------------------------------------- forward_lower path --
+// Neighbour-list formatting of the PyTorch forward_lower path for a
+// compressed se_e2_a (need_sorted_nlist_for_lower: extra_nlist_sort):
+// deepmd/pt/model/model/make_model.py:541-598 (_format_nlist) then
+// deepmd/pt/utils/nlist.py:304-337 (nlist_distinguish_types).  Per local atom
+// i (the first nloc extended atoms): every listed j >= 0 at distance
+// rr = |x_i - x_j| (formed in T, as torch.linalg.norm), sorted ascending
+// (ties by list position); rr > rcut dropped; the nearest nnei kept; then,
+// in that order, the first sel[t] of type t fill section t.
+template <typename T>
+void format_nlist_pt(int* out, const T* ext, const int* etype, const int* nl_in, int nloc,
+                     int nnei_in, T rcut, const int* sec, int ntypes) {
+  const int nnei = sec[ntypes];
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int i = 0; i < nloc; ++i) {
+    std::vector<std::pair<T, int>> c;
+    for (int p = 0; p < nnei_in; ++p) {
+      const int j = nl_in[(size_t)i * nnei_in + p];
+      if (j < 0) continue;
+      T d0 = ext[i * 3] - ext[j * 3], d1 = ext[i * 3 + 1] - ext[j * 3 + 1],
+        d2 = ext[i * 3 + 2] - ext[j * 3 + 2];
+      T rr = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+      if (!(rr > rcut)) c.push_back({rr, p});
+    }
+    std::sort(c.begin(), c.end());
+    if ((int)c.size() > nnei) c.resize(nnei);
+    int* o = out + (size_t)i * nnei;
+    std::fill(o, o + nnei, -1);
+    std::vector<int> fill(ntypes, 0);
+    for (const auto& e : c) {
+      const int j = nl_in[(size_t)i * nnei_in + e.second];
+      const int t = etype[j];
+      if (t < 0 || t >= ntypes) continue;
+      if (fill[t] < sec[t + 1] - sec[t]) o[sec[t] + fill[t]++] = j;
+    }
+  }
+}
+
+// env rows for an already formatted list (env_mat_a_cpu rows as above,
+// prod_env_mat.cc:84-100 normalisation by the centre atom's type)
+template <typename T>
+void env_mat_a_nlist(T* em, T* em_deriv, T* rij, const T* ext, const int* etype,
+                     const int* fmt, const T* avg, const T* std_, int nloc, float rcut,
+                     float rcut_smth, const int* sec, int ntypes) {
+  const int nnei = sec[ntypes];
+  const int nem = nnei * 4;
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int ii = 0; ii < nloc; ++ii) {
+    std::vector<T> e(nem), d(nem * 3), r(nnei * 3);
+    env_mat_a_row(e.data(), d.data(), r.data(), ext, ii, fmt + (size_t)ii * nnei, sec, ntypes,
+                  rcut_smth, rcut);
+    const int t = etype[ii];
+    for (int jj = 0; jj < nem; ++jj)
+      em[(size_t)ii * nem + jj] =
+          t >= 0 ? (e[jj] - avg[t * nem + jj]) / std_[t * nem + jj] : T(0);
+    for (int jj = 0; jj < nem * 3; ++jj)
+      em_deriv[(size_t)ii * nem * 3 + jj] = t >= 0 ? d[jj] / std_[t * nem + jj / 3] : T(0);
+    for (int jj = 0; jj < nnei * 3; ++jj) rij[(size_t)ii * nnei * 3 + jj] = r[jj];
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- C entry --
@@ -680,6 +741,20 @@ int prod_env_mat_a_pbc(T* em, T* em_deriv, T* rij, int* nlist, const T* coord,
                               std_, nloc, rcut, rcut_smth, sec, ntypes,        \
                               map_to_local, nall_out, ext_coord, ext_type,     \
                               ext_map, ext_cap);                               \
+  }                                                                            \
+  OR_EXPORT void or_format_nlist_pt_##SFX(int* out, const T* ext,              \
+                                          const int* etype, const int* nl_in,  \
+                                          int nloc, int nnei_in, double rcut,  \
+                                          const int* sec, int ntypes) {        \
+    format_nlist_pt(out, ext, etype, nl_in, nloc, nnei_in, (T)rcut, sec,       \
+                    ntypes);                                                   \
+  }                                                                            \
+  OR_EXPORT void or_env_mat_a_nlist_##SFX(                                     \
+      T* em, T* em_deriv, T* rij, const T* ext, const int* etype,              \
+      const int* fmt, const T* avg, const T* std_, int nloc, float rcut,       \
+      float rcut_smth, const int* sec, int ntypes) {                           \
+    env_mat_a_nlist(em, em_deriv, rij, ext, etype, fmt, avg, std_, nloc, rcut, \
+                    rcut_smth, sec, ntypes);                                   \
   }                                                                            \
   OR_EXPORT void or_tabulate_fusion_se_a_##SFX(                                \
       T* out, const T* table, const T* info, const T* em_x, const T* em,       \

@@ -142,6 +142,41 @@ def prod_env_mat_a_ext(ext_coord, ext_type, nloc, avg, std, rcut, rcut_smth, sel
     return em, emd, rij, nl
 
 
+def format_nlist_pt(ext_coord, ext_type, nlist_in, nloc, rcut, sel):
+    """The forward_lower neighbour formatting of the PyTorch model
+    (make_model.py:541-598 with extra_nlist_sort, nlist.py:304-337) on one
+    frame: ext_coord [nall, 3], ext_type [nall], nlist_in [nloc, nnei_in]
+    (extended indices, -1 padding).  Returns [nloc, sum(sel)] int32."""
+    c = _c(ext_coord).reshape(-1)
+    dt = c.dtype
+    t = _c(ext_type, np.int32)
+    nl = _c(nlist_in, np.int32).reshape(nloc, -1)
+    sec = _sec(sel)
+    out = np.zeros((nloc, int(sec[-1])), np.int32)
+    _fn("oracle", "format_nlist_pt_" + _sfx(dt))(
+        _ptr(out), _ptr(c), _ptr(t), _ptr(nl), _I(nloc), _I(nl.shape[1]),
+        ctypes.c_double(rcut), _ptr(sec), _I(len(sel)))
+    return out
+
+
+def env_mat_a_nlist(ext_coord, ext_type, fmt, nloc, avg, std, rcut, rcut_smth, sel):
+    """env_mat_a_cpu rows for a formatted list (prod_env_mat.cc:84-100
+    normalisation): returns flat (em, em_deriv, rij)."""
+    c = _c(ext_coord).reshape(-1)
+    dt = c.dtype
+    t = _c(ext_type, np.int32)
+    f = _c(fmt, np.int32).reshape(-1)
+    sec = _sec(sel)
+    nnei = int(sec[-1])
+    em = np.zeros(nloc * nnei * 4, dt)
+    emd = np.zeros(nloc * nnei * 12, dt)
+    rij = np.zeros(nloc * nnei * 3, dt)
+    _fn("oracle", "env_mat_a_nlist_" + _sfx(dt))(
+        _ptr(em), _ptr(emd), _ptr(rij), _ptr(c), _ptr(t), _ptr(f), _ptr(_c(avg, dt)),
+        _ptr(_c(std, dt)), _I(nloc), _F(rcut), _F(rcut_smth), _ptr(sec), _I(len(sel)))
+    return em, emd, rij
+
+
 def prod_env_mat_a_pbc(coord, atype, box, avg, std, rcut, rcut_smth, sel,
                        map_to_local=True, kind="oracle", return_ext=False):
     """The TF ProdEnvMatA op in its internal-PBC (mesh of 6) mode for ONE

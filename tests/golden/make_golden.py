@@ -10,6 +10,13 @@ Two sources, both read only here (the fixtures travel; the reference does not):
 2. ``ref_water.npz``: outputs of the reference's own CPU library
    (``oracle/_ref/libref_cpu.so``, compiled from the reference sources by
    ``oracle/Makefile``) on seeded synthetic water frames.
+3. ``pt_format_nlist.npz``: the reference's own PyTorch neighbour-list
+   formatting for ``forward_lower`` (``_format_nlist`` of
+   ``deepmd/pt/model/model/make_model.py`` with the forced sort a compressed
+   se_e2_a asks for, then ``nlist_distinguish_types`` of
+   ``deepmd/pt/utils/nlist.py``), executed from its source on a seeded water
+   frame whose candidate list is every extended atom within rcut + 2 A in a
+   shuffled order, as an MD engine hands it over.
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -138,6 +145,68 @@ def reference_water_fixture(path_out: str) -> None:
     np.savez_compressed(path_out, **data)
 
 
+def _reference_functions(names: dict) -> dict:
+    """Compile the named functions from the reference sources (file -> names)
+    into one namespace with torch: the reference's own code, run here."""
+    import torch
+
+    ns = {"torch": torch}
+    for rel, fn_names in names.items():
+        tree = ast.parse(open(os.path.join(REF, rel)).read())
+        for node in ast.walk(tree):
+            if isinstance(node, ast.FunctionDef) and node.name in fn_names:
+                node.decorator_list = []
+                mod = ast.Module(body=[node], type_ignores=[])
+                exec(compile(mod, rel, "exec"), ns)
+    return ns
+
+
+def reference_format_nlist_fixture(path_out: str) -> None:
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # noqa: E402
+
+    ns = _reference_functions({
+        "deepmd/pt/model/model/make_model.py": {"_format_nlist"},
+        "deepmd/pt/utils/nlist.py": {"nlist_distinguish_types"},
+    })
+    spec = importlib.util.spec_from_file_location(
+        "water", os.path.join(ROOT, "dpmd-public_gb300", "water.py"))
+    W = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(W)
+    sel, rcut, skin = [46, 92], 6.0, 2.0
+    c, t, b = W.water_frame(4, 12.42, 21)
+    nloc = len(t)
+    ext, etype, emap = O.copy_coord(c, t, b, rcut + skin)
+    ext = ext.reshape(-1, 3)
+    rng = np.random.default_rng(5438)
+    cand = []
+    for i in range(nloc):
+        d = np.linalg.norm(ext - ext[i], axis=1)
+        js = np.nonzero((d <= rcut + skin) & (np.arange(len(ext)) != i))[0]
+        cand.append(rng.permutation(js))
+    nnei_in = max(len(x) for x in cand) + 3
+    nl_in = -np.ones((nloc, nnei_in), np.int64)
+    for i, js in enumerate(cand):
+        nl_in[i, : len(js)] = js
+    data = {"ext_coord": ext, "ext_type": etype.astype(np.int32), "nlist_in": nl_in.astype(np.int32),
+            "mapping": emap.astype(np.int32), "coord": c, "atype": t, "box": b,
+            "nloc": nloc, "sel": np.array(sel), "rcut": rcut}
+
+    class _Desc:
+        def get_rcut(self):
+            return rcut
+
+    for dt, sfx in ((torch.float64, "f64"), (torch.float32, "f32")):
+        ec = torch.tensor(ext[None], dtype=dt)
+        nl = ns["_format_nlist"](_Desc(), ec, torch.tensor(nl_in[None]), sum(sel),
+                                 extra_nlist_sort=True)
+        nl = ns["nlist_distinguish_types"](nl, torch.tensor(etype[None], dtype=torch.int64), sel)
+        data[f"{sfx}_nlist"] = nl[0].numpy().astype(np.int32)
+    np.savez_compressed(path_out, **data)
+
+
 def main() -> None:
     lib = {}
     for f in LIB_TESTS:
@@ -149,6 +218,7 @@ def main() -> None:
     with open(os.path.join(HERE, "pt_tabulate.json"), "w") as fh:
         json.dump(pt, fh, separators=(",", ":"))
     reference_water_fixture(os.path.join(HERE, "ref_water.npz"))
+    reference_format_nlist_fixture(os.path.join(HERE, "pt_format_nlist.npz"))
     print("fixtures:", sorted(os.listdir(HERE)))
 
 

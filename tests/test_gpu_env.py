@@ -167,3 +167,85 @@ def test_sel_overflow_keeps_nearest(gb, oracle):
     plan, r = _run(gb, [c], [t], [b], avg, std, torch.float64, sel=sel)
     em, emd, rij, nl = oracle.prod_env_mat_a_pbc(c, t, b, avg, std, 6.0, 0.5, sel)
     np.testing.assert_array_equal(r.nlist.cpu().numpy().reshape(-1), nl)
+
+
+# ------------------------------------------------- forward_lower (external nlist) --
+def _golden_pt_nlist():
+    import os
+
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "pt_format_nlist.npz"))
+
+
+@pytest.mark.parametrize("sfx,dtype", [("f64", torch.float64), ("f32", torch.float32)])
+def test_external_nlist_vs_reference_pt_formatting(gb, oracle, sfx, dtype):
+    """prod_env_mat_a_nlist on an unsorted rcut + skin candidate list: the
+    formatted list equals the reference's own PyTorch formatting (golden
+    fixture) bit for bit; env values match the oracle's env rows for that
+    list within 1e-12 (fp64) / 5e-6 (fp32, derivative rows 2e-5)."""
+    g = _golden_pt_nlist()
+    nloc = int(g["nloc"])
+    sel = [int(s) for s in g["sel"]]
+    rcut = float(g["rcut"])
+    npd = np.float64 if dtype == torch.float64 else np.float32
+    avg, std = _stats(npd, seed=3, sel=sel)
+    ext = g["ext_coord"].astype(npd)
+    em, emd, rij, nl = torch.ops.deepmd.prod_env_mat_a_nlist(
+        torch.tensor(ext[None], device=DEV), torch.tensor(g["ext_type"][None], device=DEV),
+        torch.tensor(g["nlist_in"][None], device=DEV), torch.tensor(avg, device=DEV),
+        torch.tensor(std, device=DEV), rcut, 0.5, sel)
+    nl = nl.cpu().numpy().reshape(nloc, -1)
+    np.testing.assert_array_equal(nl, g[f"{sfx}_nlist"])
+    e_o, d_o, r_o = oracle.env_mat_a_nlist(ext, g["ext_type"], nl, nloc, avg, std, rcut, 0.5, sel)
+    tol, dtol = (1e-12, 1e-12) if dtype == torch.float64 else (5e-6, 2e-5)
+    np.testing.assert_allclose(em.cpu().numpy().reshape(-1), e_o, rtol=tol, atol=tol)
+    np.testing.assert_allclose(emd.cpu().numpy().reshape(-1), d_o, rtol=dtol, atol=dtol)
+    np.testing.assert_allclose(rij.cpu().numpy().reshape(-1), r_o, rtol=tol, atol=tol)
+
+
+def test_external_nlist_multi_frame_vs_oracle(gb, oracle):
+    """Two frames with differently shuffled lists, -1 padding interleaved
+    and a list shorter than sum(sel) for some atoms; per frame the oracle's
+    restatement of the forward_lower formatting gives the same list."""
+    g = _golden_pt_nlist()
+    nloc = int(g["nloc"])
+    sel = [int(s) for s in g["sel"]]
+    ext = g["ext_coord"]
+    rng = np.random.default_rng(77)
+    lists = []
+    for f in range(2):
+        nl = g["nlist_in"].copy()
+        for i in range(nloc):
+            row = nl[i]
+            if f == 1 and i % 5 == 0:
+                row[rng.random(row.size) < 0.5] = -1  # thin the list out
+            nl[i] = row[rng.permutation(row.size)]
+        lists.append(nl)
+    nl_in = np.stack(lists)
+    exts = np.stack([ext, ext + 0.0])
+    types = np.stack([g["ext_type"]] * 2)
+    avg, std = _stats(np.float64, seed=4, sel=sel)
+    _, _, _, nl = torch.ops.deepmd.prod_env_mat_a_nlist(
+        torch.tensor(exts, device=DEV), torch.tensor(types, device=DEV),
+        torch.tensor(nl_in, device=DEV), torch.tensor(avg, device=DEV),
+        torch.tensor(std, device=DEV), float(g["rcut"]), 0.5, sel)
+    nl = nl.cpu().numpy().reshape(2, nloc, -1)
+    for f in range(2):
+        exp = oracle.format_nlist_pt(exts[f], types[f], nl_in[f], nloc, float(g["rcut"]), sel)
+        np.testing.assert_array_equal(nl[f], exp)
+
+
+def test_external_nlist_bad_index_is_reported(gb):
+    """A listed index >= nall is skipped by the kernel and reported through
+    the status word (an error on the host), never dereferenced."""
+    g = _golden_pt_nlist()
+    nloc = int(g["nloc"])
+    sel = [int(s) for s in g["sel"]]
+    nl_in = g["nlist_in"].copy()
+    nl_in[3, 0] = len(g["ext_type"]) + 5
+    avg, std = _stats(np.float64, seed=5, sel=sel)
+    with pytest.raises(Exception, match="status"):
+        torch.ops.deepmd.prod_env_mat_a_nlist(
+            torch.tensor(g["ext_coord"][None], device=DEV),
+            torch.tensor(g["ext_type"][None], device=DEV), torch.tensor(nl_in[None], device=DEV),
+            torch.tensor(avg, device=DEV), torch.tensor(std, device=DEV), float(g["rcut"]), 0.5,
+            sel)

@@ -135,3 +135,17 @@ def test_env_mat_vs_reference_run(oracle, golden_water, tag, sfx, dtype):
     np.testing.assert_array_equal(em[: keep * 4], g[f"{tag}_{sfx}_em"])
     np.testing.assert_array_equal(emd[: keep * 12], g[f"{tag}_{sfx}_em_deriv"])
     np.testing.assert_array_equal(rij[: keep * 3], g[f"{tag}_{sfx}_rij"])
+
+
+@pytest.mark.parametrize("sfx,dt", [("f64", np.float64), ("f32", np.float32)])
+def test_oracle_format_nlist_pt_matches_reference(oracle, sfx, dt):
+    """The forward_lower neighbour formatting restated in the oracle equals the
+    reference's own PyTorch functions (_format_nlist with the forced sort,
+    nlist_distinguish_types) run on an unsorted rcut + skin candidate list."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "pt_format_nlist.npz"))
+    nloc = int(g["nloc"])
+    out = oracle.format_nlist_pt(g["ext_coord"].astype(dt), g["ext_type"], g["nlist_in"], nloc,
+                                 float(g["rcut"]), list(g["sel"]))
+    np.testing.assert_array_equal(out, g[f"{sfx}_nlist"])

@@ -10,7 +10,13 @@ Two sources, both read only here (the fixtures travel; the reference does not):
 2. ``ref_water.npz``: outputs of the reference's own CPU library
    (``oracle/_ref/libref_cpu.so``, compiled from the reference sources by
    ``oracle/Makefile``) on seeded synthetic water frames.
-3. ``pt_format_nlist.npz``: the reference's own PyTorch neighbour-list
+3. ``ref_deeppot_sea.npz``: the reference's se_e2_a test model
+   (``source/tests/infer/deeppot_sea.yaml``: descriptor statistics,
+   embedding and fitting weights) and the energies, forces and virials its
+   own inference test expects (``source/tests/infer/deeppot-testcase.yaml``),
+   read with the package's YAML reader (``dpmd-public_gb300/serial.py``;
+   PyYAML is not installed here) and stored in its flat format.
+4. ``pt_format_nlist.npz``: the reference's own PyTorch neighbour-list
    formatting for ``forward_lower`` (``_format_nlist`` of
    ``deepmd/pt/model/model/make_model.py`` with the forced sort a compressed
    se_e2_a asks for, then ``nlist_distinguish_types`` of
@@ -145,6 +151,28 @@ def reference_water_fixture(path_out: str) -> None:
     np.savez_compressed(path_out, **data)
 
 
+def reference_model_fixture(path_out: str) -> None:
+    sys.path.insert(0, ROOT)
+    from __graft_entry__ import load_package  # noqa: E402
+
+    load_package()
+    import dpmd_public_gb300.serial as S  # noqa: E402
+
+    with open(os.path.join(REF, "source/tests/infer/deeppot_sea.yaml")) as fh:
+        cfg, params, davg, dstd, type_map = S.se_a_from_dict(S.parse_block_yaml(fh.read()))
+    data = S.flatten(cfg, params, davg, dstd, type_map)
+    case = open(os.path.join(REF, "source/tests/infer/deeppot-testcase.yaml")).read()
+    blocks = re.split(r"\n\s*- coord:", case.split("results:", 1)[1])[1:]
+    for n, blk in enumerate(blocks):
+        blk = "coord:" + blk
+        for key in ("coord", "atype", "box", "atomic_energy", "force", "atomic_virial"):
+            mm = re.search(rf"\b{key}:\s*(null|\[[^\]]*\])", blk, re.S)
+            if mm and mm.group(1) != "null":
+                data[f"case{n}_{key}"] = np.array([float(x) for x in _NUM.findall(mm.group(1))])
+    data["ncases"] = len(blocks)
+    np.savez_compressed(path_out, **data)
+
+
 def _reference_functions(names: dict) -> dict:
     """Compile the named functions from the reference sources (file -> names)
     into one namespace with torch: the reference's own code, run here."""
@@ -219,6 +247,7 @@ def main() -> None:
         json.dump(pt, fh, separators=(",", ":"))
     reference_water_fixture(os.path.join(HERE, "ref_water.npz"))
     reference_format_nlist_fixture(os.path.join(HERE, "pt_format_nlist.npz"))
+    reference_model_fixture(os.path.join(HERE, "ref_deeppot_sea.npz"))
     print("fixtures:", sorted(os.listdir(HERE)))
 
 

@@ -159,3 +159,40 @@ def test_forward_lower_matches_fused(mods, built, dtype):
     assert abs(float(El) - float(Ef[0])) / nloc <= et
     assert float((Fl - Ff).abs().max()) <= ft
     assert float((Vl - Vf[0]).abs().max()) <= vt
+
+
+@pytest.mark.parametrize("dtype,compressed,tol", [(torch.float64, False, (1e-10, 1e-10, 1e-10)),
+                                                   (torch.float32, False, (1e-5, 2e-5, 2e-5)),
+                                                   (torch.float64, True, (1e-10, 1e-10, 1e-10)),
+                                                   (torch.float32, True, (1e-5, 2e-5, 2e-5))])
+def test_reference_model_testcase(mods, dtype, compressed, tol):
+    """The reference's se_e2_a test model (deeppot_sea.yaml) through the
+    operator form on the GPU reproduces its own inference test values
+    (deeppot-testcase.yaml).  Stated tolerances (per-atom energy, force,
+    virial): FP64 1e-10, plain and compressed (tables at the reference's
+    default 0.01 / 0.1 strides: the FP64 CPU composite of the compressed model
+    is within 1e-14 of these values); FP32 1e-5 / 2e-5 / 2e-5 (atomic
+    energies near -93 and -186 eV carry FP32 rounding of ~1e-5)."""
+    import importlib
+    import os
+
+    se_a, mdl, water = mods
+    S = importlib.import_module("dpmd_public_gb300.serial")
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_deeppot_sea.npz"))
+    cfg, params, davg, dstd, _ = S.unflatten(dict(g))
+    tables = infos = None
+    if compressed:
+        tables, infos = mdl.build_tables(params, davg, dstd, 0.9, cfg)
+    m = se_a.SeAModel(cfg, params, davg, dstd, DEV, dtype, tables, infos)
+    et, ft, vt = tol
+    for n in range(int(g["ncases"])):
+        c = g[f"case{n}_coord"].reshape(-1, 3)
+        t = g[f"case{n}_atype"].astype(np.int32)
+        b = g[f"case{n}_box"] if f"case{n}_box" in g.files else np.diag([100.0] * 3).reshape(-1)
+        bt = m.batch([t], np.asarray(b).reshape(1, 9))
+        E, F, V = m.step_ops(bt, torch.tensor(c, dtype=dtype, device=DEV), compressed=compressed)
+        ae = g[f"case{n}_atomic_energy"]
+        assert abs(float(E[0]) - ae.sum()) / len(t) <= et, (n, float(E[0]), ae.sum())
+        assert np.abs(F.cpu().numpy() - g[f"case{n}_force"].reshape(-1, 3)).max() <= ft
+        v_ref = g[f"case{n}_atomic_virial"].reshape(-1, 9).sum(0)
+        assert np.abs(V[0].cpu().numpy() - v_ref).max() <= vt

@@ -149,3 +149,38 @@ def test_oracle_format_nlist_pt_matches_reference(oracle, sfx, dt):
     out = oracle.format_nlist_pt(g["ext_coord"].astype(dt), g["ext_type"], g["nlist_in"], nloc,
                                  float(g["rcut"]), list(g["sel"]))
     np.testing.assert_array_equal(out, g[f"{sfx}_nlist"])
+
+
+def _ref_model_cases():
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_deeppot_sea.npz"))
+    cases = []
+    for n in range(int(g["ncases"])):
+        c = g[f"case{n}_coord"].reshape(-1, 3)
+        t = g[f"case{n}_atype"].astype(np.int32)
+        # the non-periodic case: a box far wider than rcut has no image in range
+        b = g[f"case{n}_box"] if f"case{n}_box" in g.files else np.diag([100.0] * 3).reshape(-1)
+        cases.append((c, t, b, g[f"case{n}_atomic_energy"], g[f"case{n}_force"].reshape(-1, 3),
+                      g[f"case{n}_atomic_virial"].reshape(-1, 9).sum(0)))
+    return g, cases
+
+
+def test_composite_reproduces_reference_model_testcase(gb, oracle):
+    """The FP64 CPU composite with the reference's se_e2_a test model
+    (deeppot_sea.yaml, loaded through the package's serialized-model reader)
+    gives the atomic energies, forces and virial its own inference test
+    expects (deeppot-testcase.yaml: periodic, non-periodic and elongated-box
+    cases) to 1e-12."""
+    import composite
+    import importlib
+
+    S = importlib.import_module("dpmd_public_gb300.serial")
+    g, cases = _ref_model_cases()
+    cfg, params, davg, dstd, tm = S.unflatten(dict(g))
+    assert tm == ["O", "H"]
+    for c, t, b, ae_ref, f_ref, v_ref in cases:
+        E, F, V, ae = composite.energy_force_virial(cfg, params, davg, dstd, c, t, b)
+        np.testing.assert_allclose(ae, ae_ref, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(F, f_ref, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(V.reshape(-1), v_ref, rtol=0, atol=1e-12)

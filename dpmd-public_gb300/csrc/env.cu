@@ -565,14 +565,31 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   for (int s = lane; s < nnei; s += 32) row[s] = -1;
   __syncwarp();
   // ---- rank inside each type: position = number of same-type candidates
-  //      with a smaller (r^2, index) key
-  for (int cidx = lane; cidx < ncand; cidx += 32) {
-    const uint64_t k = keys[cidx];
-    const int t = ctype[cidx];
-    int rank = 0;
-    for (int d = 0; d < ncand; ++d) rank += (ctype[d] == t) & (keys[d] < k);
-    const int sel_t = si.sec[t + 1] - si.sec[t];
-    if (rank < sel_t) row[si.sec[t] + rank] = (int)(uint32_t)(k & 0xffffffffu);
+  //      with a smaller (r^2, index) key.  Each lane holds up to four of its
+  //      candidates in registers and every key is read once per warp (a
+  //      broadcast), instead of once per candidate.
+  for (int base = 0; base < ncand; base += 128) {
+    uint64_t mk[4];
+    int mt[4], rank[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int c = base + e * 32 + lane;
+      mk[e] = c < ncand ? keys[c] : ~0ull;
+      mt[e] = c < ncand ? (int)ctype[c] : -1;
+      rank[e] = 0;
+    }
+    for (int d = 0; d < ncand; ++d) {
+      const uint64_t kd = keys[d];
+      const int td = ctype[d];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) rank[e] += (td == mt[e]) & (kd < mk[e]);
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int t = mt[e];
+      if (t >= 0 && rank[e] < si.sec[t + 1] - si.sec[t])
+        row[si.sec[t] + rank[e]] = (int)(uint32_t)(mk[e] & 0xffffffffu);
+    }
   }
   __syncwarp();
 

@@ -230,6 +230,15 @@ __device__ __forceinline__ void col_ld16(const float* p, float* v) {
   }
 }
 
+// programmatic dependent launch: wait for the grid this one depends on (all
+// its writes visible); let the dependent grid be scheduled
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ------------------------------------------------------------- kernel --
 template <class C>
 __global__ void __launch_bounds__(128, 1)
@@ -276,18 +285,31 @@ __global__ void __launch_bounds__(128, 1)
 
   int issued = 0;
   if (warp == 0 && lane == 0) {
-    // ---- TMA producer
+    // ---- TMA producer.  The weights (B) do not depend on the previous
+    //      layer: the first stages' B tiles are requested before waiting for
+    //      that layer (programmatic dependent launch), the A tiles after.
+    const int pre = nkb < TSTAGES ? nkb : TSTAGES;
+    for (int kb = 0; kb < pre; ++kb) {
+      unsigned char* st = smem + kb * STAGE;
+      mbar_expect_tx(&full[kb], STAGE);
+      tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[kb]);
+      tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[kb]);
+    }
+    issued = pre;
+    griddep_wait();
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % TSTAGES;
       const unsigned ph = (kb / TSTAGES) & 1u;
-      if (kb >= TSTAGES && !mbar_wait_bounded(&empty[s], ph ^ 1u, ep.status)) break;
       unsigned char* st = smem + s * STAGE;
-      mbar_expect_tx(&full[s], STAGE);
+      if (kb >= TSTAGES) {
+        if (!mbar_wait_bounded(&empty[s], ph ^ 1u, ep.status)) break;
+        mbar_expect_tx(&full[s], STAGE);
+        tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[s]);
+        tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[s]);
+      }
       tma_2d(st, &maps.a_hi, kb * TBK, row0, &full[s]);
       tma_2d(st + A_TILE, &maps.a_lo, kb * TBK, row0, &full[s]);
-      tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[s]);
-      tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[s]);
-      issued = kb + 1;
+      issued = kb + 1 > issued ? kb + 1 : issued;
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer: D(f32) += A(tf32, K-major) B(tf32, K-major), M 128, N 80
@@ -322,6 +344,10 @@ __global__ void __launch_bounds__(128, 1)
   // lanes poll on their own: agree on the outcome before any warp-wide op
   const bool got = __all_sync(kFull, mbar_wait_bounded(tfull, 0, ep.status));
   tc_fence_after();
+  // the next layer may start filling SMs as this grid's CTAs leave; this
+  // thread's own reads of the previous layer's outputs come after its wait
+  griddep_launch_dependents();
+  griddep_wait();
   float esum = 0.f;
   if (got) {
     static_assert(4 * EPI_WARP_BYTES <= TSTAGES * STAGE, "epilogue staging exceeds the stage buffers");
@@ -668,12 +694,27 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     if (sp.kind == EPI_B3)
       for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
     if (sp.kind == EPI_F3) ep.epart = ws.epart;
-    if (sp.cfg == LONGK)
-      k_fit_tc<CfgLongK><<<dim3(sp.N / CfgLongK::TBN, (unsigned)(rows / TBM)), 128,
-                           CfgLongK::SMEM, st>>>(maps, ep, sp.K);
-    else
-      k_fit_tc<CfgShortK><<<dim3(sp.N / CfgShortK::TBN, (unsigned)(rows / TBM)), 128,
-                            CfgShortK::SMEM, st>>>(maps, ep, sp.K);
+    // launched with programmatic stream serialization: each layer's CTAs
+    // start (barriers, TMEM, weight tiles) while the previous layer drains
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    lc.blockDim = dim3(128);
+    lc.stream = st;
+    cudaError_t le;
+    if (sp.cfg == LONGK) {
+      lc.gridDim = dim3(sp.N / CfgLongK::TBN, (unsigned)(rows / TBM));
+      lc.dynamicSmemBytes = CfgLongK::SMEM;
+      le = cudaLaunchKernelEx(&lc, k_fit_tc<CfgLongK>, maps, ep, sp.K);
+    } else {
+      lc.gridDim = dim3(sp.N / CfgShortK::TBN, (unsigned)(rows / TBM));
+      lc.dynamicSmemBytes = CfgShortK::SMEM;
+      le = cudaLaunchKernelEx(&lc, k_fit_tc<CfgShortK>, maps, ep, sp.K);
+    }
+    if (le != cudaSuccess) return cuda_status(le, "fit_tc gemm launch");
     GBDP_CHECK_LAUNCH("fit_tc gemm");
   }
   TcRows rw{};

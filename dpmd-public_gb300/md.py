@@ -59,9 +59,12 @@ class NVE:
         return E, F, V
 
     def capture(self):
+        # snapshot first: the side stream only waits for work enqueued
+        # before wait_stream, so a clone issued after it could read x / v
+        # after the warm-up steps on s have already moved them
+        x0, v0 = self.x.clone(), self.v.clone()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
-        x0, v0 = self.x.clone(), self.v.clone()
         with torch.cuda.stream(s):
             for _ in range(2):
                 self._step()

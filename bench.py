@@ -301,7 +301,7 @@ def main():
     launches = graph_kernels(graph)
     if hasattr(graph, "instantiate"):
         graph.instantiate()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    flush = L2Flush(dev)
 
     def barrier():
         if ws > 1:
@@ -318,7 +318,7 @@ def main():
         barrier()
         wall0 = time.perf_counter()
         for k in range(args.steps):
-            flush.zero_()  # L2 flush between timed steps (256 MB write), outside the events
+            flush()  # L2 flush between timed steps, outside the events
             starts[k].record()
             graph.replay()
             ends[k].record()
@@ -346,7 +346,7 @@ def main():
         graph.replay()
     barrier()
     for k in range(args.steps):
-        flush.zero_()
+        flush()
         e_st[k].record()
         coord.copy_(h_coord, non_blocking=True)
         graph.replay()
@@ -375,6 +375,8 @@ def main():
         roof_parts[k] = {x: rp[x] for x in ("kernel", "bound", "achieved", "unit", "frac",
                                             "ms_per_launch", "launches", "traffic") if x in rp}
 
+    opk = op_kernel_times(model, batch, coord, flush, peaks, reps=max(3, min(args.steps, 10)))
+
     # ---- plain (uncompressed) drop-in, eager, same frame
     mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
                        torch.float32)
@@ -394,7 +396,7 @@ def main():
            "data": "synthetic (seeded water generator, random-init weights)",
            "config": {"workload": WORKLOAD, "atoms": nat, "form": "fused compressed, CUDA graph",
                       "fitting_gemm": args.fit_mode,
-                      "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
+                      "l2": L2Flush.DESC, "parallelism": f"replicas x{ws}",
                       "wall_s": wall},
            "e2e": e2e,
            "gpu_launches": None if launches is None else launches["ours"] * args.steps,
@@ -402,7 +404,8 @@ def main():
            "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                      "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
-           "roofline": roof, "roofline_parts": roof_parts, "clocks": clk.summary()}
+           "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
+           "clocks": clk.summary()}
     if rank == 0:
         import oracle as O
         import composite
@@ -629,6 +632,28 @@ def graph_kernels(graph):
     return {"ours": ours, "other": other, "ours_by_kernel": names}
 
 
+class L2Flush:
+    """Empties L2 between timed launches: a 256 MB write (larger than the
+    129 MB L2), then a 256 MB read, so that the lines left in L2 are clean
+    and the timed kernel does not pay for writing the flush back."""
+
+    DESC = "flushed between timed steps (256 MB write, then 256 MB read)"
+
+    def __init__(self, dev):
+        import torch
+
+        n = 256 * 1024 * 1024 // 4
+        self.w = torch.empty(n, dtype=torch.float32, device=dev)
+        self.r = torch.zeros(n, dtype=torch.float32, device=dev)
+        self.o = torch.zeros((), dtype=torch.float32, device=dev)
+
+    def __call__(self):
+        import torch
+
+        self.w.zero_()
+        torch.sum(self.r, dim=0, out=self.o)
+
+
 def kernel_times(model, batch, coord, flush, reps: int = 5):
     """Average device time of each part of the fused step (CUDA events on
     the launching stream, L2 flushed before each part)."""
@@ -679,7 +704,7 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
     for name, fn in parts.items():
         ts = []
         for _ in range(reps):
-            flush.zero_()
+            flush()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record()
             fn()
@@ -687,6 +712,103 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
             torch.cuda.synchronize()
             ts.append(s.elapsed_time(e))
         res[name] = {"ms": statistics.median(ts)}
+    return res
+
+
+def op_kernel_times(model, batch, coord, flush, peaks, reps: int = 5):
+    """The operator-contract kernels (the reference's op sequence on the
+    GPU) on the same frame, one at a time: device time per call (CUDA
+    events, L2 flushed before each call), algorithmic HBM bytes per call
+    (each op's inputs read once and outputs written once) and the fraction
+    of the measured HBM bandwidth.  The env matrix and force / virial
+    scatters are HBM-bound; the tabulation calls are bound by table rows
+    through L2, so their HBM fraction is listed for reference only."""
+    import torch
+
+    ops = sys.modules["dpmd_public_gb300.ops"]
+    cfg = model.cfg
+    b = batch
+    n, nn, M = b.nloc, cfg.nnei, cfg.neuron[-1]
+    dev = coord.device
+    dt = model.dtype
+    f = 4
+    env = ops.EnvMatResult()
+    env.em = torch.empty((n, nn, 4), dtype=dt, device=dev)
+    env.em_deriv = torch.empty((n, nn, 4, 3), dtype=dt, device=dev)
+    env.rij = torch.empty((n, nn, 3), dtype=dt, device=dev)
+    env.nlist = torch.empty((n, nn), dtype=torch.int32, device=dev)
+    env.nlist_ext = None
+    env.ext_coord = torch.empty((b.plan.ext_total, 3), dtype=dt, device=dev)
+    env.ext_type = torch.empty((b.plan.ext_total,), dtype=torch.int32, device=dev)
+    env.ext_map = torch.empty((b.plan.ext_total,), dtype=torch.int32, device=dev)
+    env.ext_nall = torch.empty((b.nframes,), dtype=torch.int32, device=dev)
+
+    def env_op():
+        ops.env_mat_packed(b.plan, coord, b.atype, model.davg, model.dstd, cfg.rcut_smth,
+                           list(cfg.sel), check_status=False, out=env)
+
+    env_op()
+    torch.cuda.synchronize()
+    nall = int(env.ext_nall[0])
+    gen = torch.Generator(device=dev).manual_seed(3)
+    net = torch.randn((1, n * nn * 4), generator=gen, device=dev, dtype=dt)
+    natoms = torch.tensor([n, nall, 0, 0], dtype=torch.int32)
+    ed, rij, nl = env.em_deriv.reshape(1, -1), env.rij.reshape(1, -1), env.nlist.reshape(1, -1)
+    # one tabulation call per neighbour-type section over all atoms (table of
+    # the O-centred net), inputs made contiguous beforehand
+    sec = cfg.sec
+    tab = []
+    for tj in range(cfg.ntypes):
+        k = tj if cfg.type_one_side else tj * cfg.ntypes
+        rr = env.em[:, sec[tj]:sec[tj + 1], :].contiguous()
+        tab.append((model.tables[k], model.table_info_t[k], rr[:, :, :1].reshape(-1, 1).contiguous(),
+                    rr, torch.randn((n, 4, M), generator=gen, device=dev, dtype=dt)))
+    parts = {
+        # coord + type in, ghosts (~nall - nloc) written; em, em_deriv, rij, nlist out
+        "prod_env_mat_a": (env_op, n * (16 + nn * (16 + 48 + 12 + 4)) + (nall - n) * 20),
+        "prod_force_se_a": (lambda: ops.prod_force_se_a_impl(net, ed, nl, natoms, nn, 0),
+                            n * nn * (16 + 48 + 4) + nall * 12),
+        "prod_force_se_a_det": (lambda: ops.prod_force_se_a_impl(net, ed, nl, natoms, nn, 0, True),
+                                n * nn * (16 + 48 + 4) + nall * 12),
+        "prod_virial_se_a": (lambda: ops.prod_virial_se_a_impl(net, ed, rij, nl, natoms, nn, 0),
+                             n * nn * (16 + 48 + 12 + 4) + nall * 36 + 36),
+        "tabulate_fusion_se_a": (lambda: [ops.tabulate_forward(t_, i_, x_, e_, M)
+                                          for t_, i_, x_, e_, _ in tab],
+                                 sum(x_.numel() * f * 5 + n * 4 * M * f for _, _, x_, _, _ in tab)),
+        "tabulate_fusion_se_a_grad": (lambda: [ops.tabulate_grad(t_, i_, x_, e_, d_)
+                                               for t_, i_, x_, e_, d_ in tab],
+                                      sum(x_.numel() * f * 10 + n * 4 * M * f
+                                          for _, _, x_, _, _ in tab)),
+    }
+    res = {}
+    for name, (fn, nbytes) in parts.items():
+        # each op captured in its own graph, so that host work between its
+        # launches (argument checks, output allocation) is not timed
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            fn()
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn()
+        g.replay()
+        ts = []
+        for _ in range(reps):
+            flush()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            g.replay()
+            e.record()
+            torch.cuda.synchronize()
+            ts.append(s.elapsed_time(e))
+        del g
+        ms = statistics.median(ts)
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        res[name] = {"ms": ms, "alg_bytes": nbytes, "achieved_gbs": gbs,
+                     "frac_hbm": gbs / peaks["hbm_gbs"],
+                     "bound": "L2 table rows" if name.startswith("tab") else "hbm"}
     return res
 
 

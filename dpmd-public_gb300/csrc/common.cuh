@@ -44,6 +44,34 @@ __device__ __forceinline__ T warp_sum(T v) {
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
+// ------------------------------------------------------ vector reductions --
+// red.global.add over 2 or 4 consecutive floats (sm_90 and later) where the
+// address is 8- / 16-byte aligned; scalar atomics for the rest and for double
+__device__ __forceinline__ void red2(float* p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+__device__ __forceinline__ void red4(float* p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+
+// p[0..2] += v[0..2]
+__device__ __forceinline__ void scatter3(double* p, const double* v) {
+  atomicAdd(p, v[0]);
+  atomicAdd(p + 1, v[1]);
+  atomicAdd(p + 2, v[2]);
+}
+__device__ __forceinline__ void scatter3(float* p, const float* v) {
+  if ((reinterpret_cast<uintptr_t>(p) & 7) == 0) {
+    red2(p, v[0], v[1]);
+    atomicAdd(p + 2, v[2]);
+  } else {
+    atomicAdd(p, v[0]);
+    red2(p + 1, v[1], v[2]);
+  }
+}
+
 // Device-side error word: kernels record the first problem they hit and
 // return; the host reads the word after the stream is synchronised.
 __device__ __forceinline__ void raise_status(int* status, int code) {

@@ -455,8 +455,7 @@ __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
   return max_sz(slots_bytes<T>(nnei), (size_t)2 * mp * sizeof(V4<T>));
 }
 
-constexpr int kLanesPerNbr = 16;  // phase 1: lanes per neighbour
-
+// Phase 1 runs 16 lanes per neighbour.
 // NK = ceil(M / 16): outputs per lane in phase 1; NQ = ceil(M / 32); U:
 // neighbours in flight per 16-lane group (measured on the 12,288-atom water
 // step: U = 1 at 7 CTAs per SM is faster than U = 2 at 6).
@@ -716,10 +715,7 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
         v3[d] = acc;
       }
       const int jl = ext_map[eoff + je];
-      T* fj = force + (size_t)(aoff + jl) * 3;
-      atomicAdd(fj + 0, v3[0]);
-      atomicAdd(fj + 1, v3[1]);
-      atomicAdd(fj + 2, v3[2]);
+      scatter3(force + (size_t)(aoff + jl) * 3, v3);
       ci[0] += v3[0];
       ci[1] += v3[1];
       ci[2] += v3[2];
@@ -733,10 +729,8 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
   ci[1] = warp_sum(ci[1]);
   ci[2] = warp_sum(ci[2]);
   if (lane == 0) {
-    T* fi = force + (size_t)i * 3;
-    atomicAdd(fi + 0, -ci[0]);
-    atomicAdd(fi + 1, -ci[1]);
-    atomicAdd(fi + 2, -ci[2]);
+    const T m[3] = {-ci[0], -ci[1], -ci[2]};
+    scatter3(force + (size_t)i * 3, m);
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) {

@@ -15,6 +15,8 @@
 //                 atom_virial_j is a gather in that fixed order, so the result
 //                 is bitwise reproducible run to run.
 // Frame virials are reduced in double in a fixed tree.
+#include <climits>
+
 #include "common.cuh"
 
 namespace gbdp {
@@ -58,67 +60,161 @@ __device__ __forceinline__ void pair_force(const T* __restrict__ g, const T* __r
   v[2] = gg[0] * d[2] + gg[1] * d[5] + gg[2] * d[8] + gg[3] * d[11];
 }
 
+// p[0..8] += t[0..8]
+__device__ __forceinline__ void scatter9(double* p, const double* t) {
+#pragma unroll
+  for (int q = 0; q < 9; ++q) atomicAdd(p + q, t[q]);
+}
+__device__ __forceinline__ void scatter9(float* p, const float* t) {
+  // p is 4-byte aligned; split the row at its 8- and 16-byte boundaries
+  switch ((reinterpret_cast<uintptr_t>(p) >> 2) & 3) {
+    case 0:
+      red4(p, t[0], t[1], t[2], t[3]);
+      red4(p + 4, t[4], t[5], t[6], t[7]);
+      atomicAdd(p + 8, t[8]);
+      break;
+    case 1:
+      atomicAdd(p, t[0]);
+      red2(p + 1, t[1], t[2]);
+      red4(p + 3, t[3], t[4], t[5], t[6]);
+      red2(p + 7, t[7], t[8]);
+      break;
+    case 2:
+      red2(p, t[0], t[1]);
+      red4(p + 2, t[2], t[3], t[4], t[5]);
+      red2(p + 6, t[6], t[7]);
+      atomicAdd(p + 8, t[8]);
+      break;
+    default:
+      atomicAdd(p, t[0]);
+      red4(p + 1, t[1], t[2], t[3], t[4]);
+      red4(p + 5, t[5], t[6], t[7], t[8]);
+      break;
+  }
+}
+
 // ---------------------------------------------------------- atomic mode --
+// One warp per centre row (kScatterWarps rows per CTA), lanes over slots, U slots per
+// lane per pass with every load of the pass issued before the first use.
+// F_j and atom_virial_j by (vector) reductions, F_i by one warp reduction;
+// the frame virial as per-warp partials in T, summed in double per CTA and
+// added to the frame's double accumulator.
 template <typename T>
-__global__ void k_force_atomic(T* __restrict__ force, T* __restrict__ atom_virial,
-                               double* __restrict__ vir_acc, const T* __restrict__ net,
-                               const T* __restrict__ dR, const T* __restrict__ rij,
-                               const int* __restrict__ nlist, int nloc, int nall, int nnei,
-                               int nframes) {
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // frame * nloc + i
-  const int lane = threadIdx.x & 31;
-  if (row >= nframes * nloc) return;
-  const int f = row / nloc, i = row - f * nloc;
-  const T* g = net + (size_t)row * nnei * 4;
-  const T* d = dR + (size_t)row * nnei * 12;
-  T ci[3] = {T(0), T(0), T(0)};
-  double vs[9];
+struct ScatterU {
+  static constexpr int U = 5;  // 160 slots per pass covers nnei = 138
+};
+template <>
+struct ScatterU<double> {
+  static constexpr int U = 2;
+};
+
+constexpr int kScatterWarps = 4;  // 140 registers a thread: 3 CTAs per SM
+
+template <typename T, int U>
+__global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
+    T* __restrict__ force, T* __restrict__ atom_virial, double* __restrict__ vir_acc,
+    const T* __restrict__ net, const T* __restrict__ dR, const T* __restrict__ rij,
+    const int* __restrict__ nlist, int nloc, int nall, int nnei, int nframes) {
+  __shared__ double s_vir[kScatterWarps][9];
+  __shared__ int s_frame[kScatterWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long row = (long)blockIdx.x * kScatterWarps + warp;  // frame * nloc + i
+  const bool want_v = atom_virial != nullptr;
+  T vs[9];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) vs[q] = 0.;
-  for (int s = lane; s < nnei; s += 32) {
-    T v[3];
-    pair_force(g, d, s, v);
-    ci[0] += v[0];
-    ci[1] += v[1];
-    ci[2] += v[2];
-    const int j = nlist[(size_t)row * nnei + s];
-    if (j < 0 || j >= nall) continue;
-    if (force) {
-      T* fj = force + ((size_t)f * nall + j) * 3;
-      atomicAdd(fj + 0, v[0]);
-      atomicAdd(fj + 1, v[1]);
-      atomicAdd(fj + 2, v[2]);
-    }
-    if (atom_virial) {
-      const T* r = rij + ((size_t)row * nnei + s) * 3;
-      const T r0 = r[0], r1 = r[1], r2 = r[2];
-      T* av = atom_virial + ((size_t)f * nall + j) * 9;
+  for (int q = 0; q < 9; ++q) vs[q] = T(0);
+  int f = -1;
+  if (row < (long)nframes * nloc) {
+    f = (int)(row / nloc);
+    const int i = (int)(row - (long)f * nloc);
+    const T* g = net + (size_t)row * nnei * 4;
+    const T* d = dR + (size_t)row * nnei * 12;
+    const int* nl = nlist + (size_t)row * nnei;
+    const T* rr = want_v ? rij + (size_t)row * nnei * 3 : nullptr;
+    T ci[3] = {T(0), T(0), T(0)};
+    for (int base = 0; base < nnei; base += 32 * U) {
+      T gg[U][4], dd[U][12], r3[U][3];
+      int jj[U];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const T t0 = v[a] * r0, t1 = v[a] * r1, t2 = v[a] * r2;
-        atomicAdd(av + a * 3 + 0, t0);
-        atomicAdd(av + a * 3 + 1, t1);
-        atomicAdd(av + a * 3 + 2, t2);
-        vs[a * 3 + 0] += (double)t0;
-        vs[a * 3 + 1] += (double)t1;
-        vs[a * 3 + 2] += (double)t2;
+      for (int u = 0; u < U; ++u) {
+        const int s = base + lane + 32 * u;
+        jj[u] = -1;
+        if (s < nnei) {
+          V4<T>::load4(g + 4 * s, gg[u]);
+          V4<T>::load4(d + 12 * s, dd[u]);
+          V4<T>::load4(d + 12 * s + 4, dd[u] + 4);
+          V4<T>::load4(d + 12 * s + 8, dd[u] + 8);
+          jj[u] = __ldg(nl + s);
+          if (want_v) {
+            r3[u][0] = __ldg(rr + 3 * s);
+            r3[u][1] = __ldg(rr + 3 * s + 1);
+            r3[u][2] = __ldg(rr + 3 * s + 2);
+          }
+        } else {
+#pragma unroll
+          for (int w = 0; w < 4; ++w) gg[u][w] = T(0);
+#pragma unroll
+          for (int w = 0; w < 12; ++w) dd[u][w] = T(0);
+        }
+        if (!want_v || s >= nnei) r3[u][0] = r3[u][1] = r3[u][2] = T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        T v[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          v[a] = gg[u][0] * dd[u][a] + gg[u][1] * dd[u][3 + a] + gg[u][2] * dd[u][6 + a] +
+                 gg[u][3] * dd[u][9 + a];
+        ci[0] += v[0];
+        ci[1] += v[1];
+        ci[2] += v[2];
+        const int j = jj[u];
+        if (j < 0 || j >= nall) continue;
+        if (force) scatter3(force + ((size_t)f * nall + j) * 3, v);
+        if (want_v) {
+          T t[9];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) t[a * 3 + b] = v[a] * r3[u][b];
+          scatter9(atom_virial + ((size_t)f * nall + j) * 9, t);
+#pragma unroll
+          for (int q = 0; q < 9; ++q) vs[q] += t[q];
+        }
       }
     }
+    ci[0] = warp_sum(ci[0]);
+    ci[1] = warp_sum(ci[1]);
+    ci[2] = warp_sum(ci[2]);
+    if (lane == 0 && force) {
+      const T m[3] = {-ci[0], -ci[1], -ci[2]};
+      scatter3(force + ((size_t)f * nall + i) * 3, m);
+    }
   }
-  ci[0] = warp_sum(ci[0]);
-  ci[1] = warp_sum(ci[1]);
-  ci[2] = warp_sum(ci[2]);
-  if (lane == 0 && force) {
-    T* fi = force + ((size_t)f * nall + i) * 3;
-    atomicAdd(fi + 0, -ci[0]);
-    atomicAdd(fi + 1, -ci[1]);
-    atomicAdd(fi + 2, -ci[2]);
-  }
-  if (atom_virial) {
+  if (want_v && vir_acc) {  // uniform over the CTA
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      double t = warp_sum(vs[q]);
-      if (lane == 0) atomicAdd(vir_acc + f * 9 + q, t);
+    for (int q = 0; q < 9; ++q) vs[q] = warp_sum(vs[q]);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) s_vir[warp][q] = (double)vs[q];
+      s_frame[warp] = f;
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+      // rows of a CTA are consecutive: runs of equal frames, idle warps last
+      const int q = threadIdx.x;
+      double acc = 0.;
+      int cur = -1;
+      for (int w = 0; w < kScatterWarps; ++w) {
+        const int fw = s_frame[w];
+        if (fw != cur) {
+          if (cur >= 0) atomicAdd(vir_acc + cur * 9 + q, acc);
+          cur = fw;
+          acc = 0.;
+        }
+        acc += s_vir[w][q];
+      }
+      if (cur >= 0) atomicAdd(vir_acc + cur * 9 + q, acc);
     }
   }
 }
@@ -204,14 +300,40 @@ __global__ void k_rev_fill(const int* __restrict__ nlist, int nloc, int nall, in
   pairs[start[fj] + pos] = (int)(t - (size_t)f * nloc * nnei);  // i * nnei + s
 }
 
-// sort every row of the reverse list ascending (rows are short)
-__global__ void k_rev_sort(const int* __restrict__ pairs_in, int* __restrict__ pairs_out,
-                           const int* __restrict__ start, const int* __restrict__ cnt,
-                           int nrows) {
+// Sort every row of the reverse list ascending, one warp per row.  Entries
+// of a row are distinct (i * nnei + s, one per centre), so each entry's rank
+// is the count of smaller ones: up to 128 entries are held in registers and
+// broadcast by shuffles; longer rows rank through memory.
+__global__ void __launch_bounds__(256) k_rev_sort(const int* __restrict__ pairs_in,
+                                                  int* __restrict__ pairs_out,
+                                                  const int* __restrict__ start,
+                                                  const int* __restrict__ cnt, int nrows) {
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (r >= nrows) return;
+  if (r >= nrows) return;  // uniform over the warp
   const int s = start[r], n = cnt[r];
+  if (n <= 128) {
+    int v[4], rank[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int a = lane + 32 * k;
+      v[k] = a < n ? pairs_in[s + a] : INT_MAX;
+      rank[k] = 0;
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      if (32 * k2 >= n) break;  // uniform
+      for (int l = 0; l < 32; ++l) {
+        const int b = __shfl_sync(kFull, v[k2], l);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rank[k] += b < v[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (lane + 32 * k < n) pairs_out[s + rank[k]] = v[k];
+    return;
+  }
   for (int a = lane; a < n; a += 32) {
     const int v = pairs_in[s + a];
     int rank = 0;
@@ -220,22 +342,27 @@ __global__ void k_rev_sort(const int* __restrict__ pairs_in, int* __restrict__ p
   }
 }
 
+// Deterministic gather, one warp per extended atom j of a frame: lanes take
+// the reverse-list entries (ascending (i, s)) in a fixed interleave, local
+// atoms also subtract their own centre sum over their slots, and a fixed
+// butterfly reduces the lanes, so the result is the same bits every run.
 template <typename T>
-__global__ void k_force_gather(T* __restrict__ force, T* __restrict__ atom_virial,
-                               const T* __restrict__ net, const T* __restrict__ dR,
-                               const T* __restrict__ rij, const int* __restrict__ start,
-                               const int* __restrict__ cnt, const int* __restrict__ pairs,
-                               int nloc, int nall, int nnei, int nframes) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;  // frame * nall + j
-  if (r >= nframes * nall) return;
-  const int f = r / nall, j = r - f * nall;
+__global__ void __launch_bounds__(256) k_scatter_gather(
+    T* __restrict__ force, T* __restrict__ atom_virial, const T* __restrict__ net,
+    const T* __restrict__ dR, const T* __restrict__ rij, const int* __restrict__ start,
+    const int* __restrict__ cnt, const int* __restrict__ pairs, int nloc, int nall, int nnei,
+    int nframes) {
+  const long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // frame * nall + j
+  const int lane = threadIdx.x & 31;
+  if (r >= (long)nframes * nall) return;  // uniform over the warp
+  const int f = (int)(r / nall), j = (int)(r - (long)f * nall);
   const int s0 = start[r], n = cnt[r];
+  const size_t fbase = (size_t)f * nloc;
   T F[3] = {T(0), T(0), T(0)};
   T V[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) V[q] = T(0);
-  const size_t fbase = (size_t)f * nloc;
-  for (int k = 0; k < n; ++k) {
+  for (int k = lane; k < n; k += 32) {
     const int p = pairs[s0 + k];
     const int i = p / nnei, s = p - i * nnei;
     const size_t row = fbase + i;
@@ -246,48 +373,64 @@ __global__ void k_force_gather(T* __restrict__ force, T* __restrict__ atom_viria
     F[2] += v[2];
     if (atom_virial) {
       const T* rr = rij + (row * nnei + s) * 3;
+      const T r0 = rr[0], r1 = rr[1], r2 = rr[2];
 #pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) V[a * 3 + b] += v[a] * rr[b];
+      for (int a = 0; a < 3; ++a) {
+        V[a * 3 + 0] += v[a] * r0;
+        V[a * 3 + 1] += v[a] * r1;
+        V[a * 3 + 2] += v[a] * r2;
+      }
     }
-  }
-  if (j < nloc) {
-    const size_t row = fbase + j;
-    T c[3] = {T(0), T(0), T(0)};
-    for (int s = 0; s < nnei; ++s) {
-      T v[3];
-      pair_force(net + row * nnei * 4, dR + row * nnei * 12, s, v);
-      c[0] += v[0];
-      c[1] += v[1];
-      c[2] += v[2];
-    }
-    F[0] -= c[0];
-    F[1] -= c[1];
-    F[2] -= c[2];
   }
   if (force) {
-    force[(size_t)r * 3 + 0] = F[0];
-    force[(size_t)r * 3 + 1] = F[1];
-    force[(size_t)r * 3 + 2] = F[2];
+    if (j < nloc) {
+      const size_t row = fbase + j;
+      for (int s = lane; s < nnei; s += 32) {
+        T v[3];
+        pair_force(net + row * nnei * 4, dR + row * nnei * 12, s, v);
+        F[0] -= v[0];
+        F[1] -= v[1];
+        F[2] -= v[2];
+      }
+    }
+    F[0] = warp_sum(F[0]);
+    F[1] = warp_sum(F[1]);
+    F[2] = warp_sum(F[2]);
+    if (lane == 0) {
+      force[(size_t)r * 3 + 0] = F[0];
+      force[(size_t)r * 3 + 1] = F[1];
+      force[(size_t)r * 3 + 2] = F[2];
+    }
   }
-  if (atom_virial)
+  if (atom_virial) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) atom_virial[(size_t)r * 9 + q] = V[q];
+    for (int q = 0; q < 9; ++q) V[q] = warp_sum(V[q]);
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) atom_virial[(size_t)r * 9 + q] = V[q];
+  }
 }
 
-// frame virial = sum_j atom_virial_j, double, fixed tree (one CTA per frame)
+// Frame virial = sum_j atom_virial_j in double, fixed order: each CTA sums
+// kVirChunk atoms of one frame (thread-strided, then a shared-memory tree)
+// into a partial; k_vir_final adds a frame's partials in chunk order.
+constexpr int kVirChunk = 2048;
+
 template <typename T>
-__global__ void k_vir_reduce(T* __restrict__ virial, const T* __restrict__ atom_virial,
-                             int nall) {
+__global__ void __launch_bounds__(256) k_vir_partial(double* __restrict__ part,
+                                                     const T* __restrict__ atom_virial,
+                                                     int nall) {
   __shared__ double sh[9][256];
-  const int f = blockIdx.x;
+  const int f = blockIdx.y, c = blockIdx.x;
+  const int j0 = c * kVirChunk, j1 = min(nall, j0 + kVirChunk);
   double acc[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = 0.;
-  for (int j = threadIdx.x; j < nall; j += blockDim.x)
+  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const T* av = atom_virial + ((size_t)f * nall + j) * 9;
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] += (double)atom_virial[((size_t)f * nall + j) * 9 + q];
+    for (int q = 0; q < 9; ++q) acc[q] += (double)av[q];
+  }
 #pragma unroll
   for (int q = 0; q < 9; ++q) sh[q][threadIdx.x] = acc[q];
   __syncthreads();
@@ -297,7 +440,17 @@ __global__ void k_vir_reduce(T* __restrict__ virial, const T* __restrict__ atom_
       for (int q = 0; q < 9; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x < 9) virial[f * 9 + threadIdx.x] = (T)sh[threadIdx.x][0];
+  if (threadIdx.x < 9) part[((size_t)f * gridDim.x + c) * 9 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+template <typename T>
+__global__ void k_vir_final(T* __restrict__ virial, const double* __restrict__ part,
+                            int nchunk) {
+  const int f = blockIdx.x, q = threadIdx.x;
+  if (q >= 9) return;
+  double s = 0.;
+  for (int c = 0; c < nchunk; ++c) s += part[((size_t)f * nchunk + c) * 9 + q];
+  virial[f * 9 + q] = (T)s;
 }
 
 // ------------------------------------------------------- backward kernels --
@@ -358,6 +511,7 @@ size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct ProdWs {
   double* vir_acc;
+  double* vir_part;  // deterministic frame-virial partials [nframes, nchunk, 9]
   int* cnt;
   int* start;
   int* cursor;
@@ -378,6 +532,8 @@ ProdWs carve_prod(void* base, int nframes, int nloc, int nall, int nnei, int det
   };
   w.vir_acc = reinterpret_cast<double*>(take(sizeof(double) * 9 * (size_t)nframes));
   if (det) {
+    const size_t nchunk = (size_t)(nall + kVirChunk - 1) / kVirChunk;
+    w.vir_part = reinterpret_cast<double*>(take(sizeof(double) * 9 * (size_t)nframes * nchunk));
     const size_t nrows = (size_t)nframes * nall;
     const size_t npair = (size_t)nframes * nloc * nnei;
     w.cnt = reinterpret_cast<int*>(take(sizeof(int) * nrows));
@@ -405,10 +561,37 @@ int build_reverse(const ProdWs& w, const int* nlist, int nloc, int nall, int nne
   k_scan_sums<<<1, 1024, 0, st>>>(w.bsum, nb);
   k_scan_add<<<nb, 1024, 0, st>>>(w.start, w.bsum, nrows);
   k_rev_fill<<<gp, tb, 0, st>>>(nlist, nloc, nall, nnei, nframes, w.start, w.cursor, w.pairs_a);
-  k_rev_sort<<<(nrows * 32 + tb - 1) / tb, tb, 0, st>>>(w.pairs_a, w.pairs_b, w.start, w.cnt,
-                                                        nrows);
+  k_rev_sort<<<(unsigned)(((size_t)nrows * 32 + tb - 1) / tb), tb, 0, st>>>(
+      w.pairs_a, w.pairs_b, w.start, w.cnt, nrows);
   GBDP_CHECK_LAUNCH("reverse neighbour list");
   return GBDP_OK;
+}
+
+template <typename T>
+void launch_atomic(T* force, T* atom_virial, double* vir_acc, const T* net, const T* dR,
+                   const T* rij, const int* nlist, int nloc, int nall, int nnei, int nframes,
+                   cudaStream_t st) {
+  const size_t rows = (size_t)nframes * nloc;
+  k_scatter_atomic<T, ScatterU<T>::U>
+      <<<(unsigned)((rows + kScatterWarps - 1) / kScatterWarps), kScatterWarps * 32, 0, st>>>(
+      force, atom_virial, vir_acc, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+}
+
+template <typename T>
+void launch_gather(T* force, T* atom_virial, const T* net, const T* dR, const T* rij,
+                   const ProdWs& w, int nloc, int nall, int nnei, int nframes, cudaStream_t st) {
+  const size_t rows = (size_t)nframes * nall;
+  k_scatter_gather<T><<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(
+      force, atom_virial, net, dR, rij, w.start, w.cnt, w.pairs_b, nloc, nall, nnei, nframes);
+}
+
+template <typename T>
+void launch_vir_reduce(T* virial, const T* atom_virial, const ProdWs& w, int nall, int nframes,
+                       cudaStream_t st) {
+  const int nchunk = (nall + kVirChunk - 1) / kVirChunk;
+  if (nchunk == 0) return;  // no atoms: the virial stays at its zero fill
+  k_vir_partial<T><<<dim3(nchunk, nframes), 256, 0, st>>>(w.vir_part, atom_virial, nall);
+  k_vir_final<T><<<nframes, 32, 0, st>>>(virial, w.vir_part, nchunk);
 }
 
 template <typename T>
@@ -432,21 +615,16 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
                "prod_force/virial: null input pointer");
   GBDP_REQUIRE(((uintptr_t)net & 15) == 0 && ((uintptr_t)dR & 15) == 0,
                "prod_force/virial: net_deriv and env_deriv must be 16-byte aligned");
-  const int tb = 256;
   if (!det) {
     cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
-    const long warps = (long)nframes * nloc;
-    k_force_atomic<T><<<(unsigned)((warps * 32 + tb - 1) / tb), tb, 0, st>>>(
-        force, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+    launch_atomic<T>(force, atom_virial, virial ? w.vir_acc : nullptr, net, dR, rij, nlist, nloc,
+                     nall, nnei, nframes, st);
     if (virial) k_vir_finish<T><<<1, 256, 0, st>>>(virial, w.vir_acc, 9 * nframes);
   } else {
     int rc = build_reverse(w, nlist, nloc, nall, nnei, nframes, st);
     if (rc) return rc;
-    const int nrows = nframes * nall;
-    k_force_gather<T><<<(nrows + tb - 1) / tb, tb, 0, st>>>(force, atom_virial, net, dR, rij,
-                                                           w.start, w.cnt, w.pairs_b, nloc,
-                                                           nall, nnei, nframes);
-    if (virial) k_vir_reduce<T><<<nframes, 256, 0, st>>>(virial, atom_virial, nall);
+    launch_gather<T>(force, atom_virial, net, dR, rij, w, nloc, nall, nnei, nframes, st);
+    if (virial) launch_vir_reduce<T>(virial, atom_virial, w, nall, nframes, st);
   }
   GBDP_CHECK_LAUNCH("prod_force/virial");
   return GBDP_OK;
@@ -482,21 +660,18 @@ int prod_virial_impl(T* virial, T* atom_virial, const T* net, const T* dR, const
     return GBDP_OK;
   }
   GBDP_REQUIRE(net && dR && rij && nlist, "prod_virial_a: null input pointer");
-  const int tb = 256;
+  GBDP_REQUIRE(((uintptr_t)net & 15) == 0 && ((uintptr_t)dR & 15) == 0,
+               "prod_virial_a: net_deriv and env_deriv must be 16-byte aligned");
   if (!det) {
     cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
-    const long warps = (long)nframes * nloc;
-    k_force_atomic<T><<<(unsigned)((warps * 32 + tb - 1) / tb), tb, 0, st>>>(
-        nullptr, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+    launch_atomic<T>(nullptr, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
+                     nframes, st);
     k_vir_finish<T><<<1, 256, 0, st>>>(virial, w.vir_acc, 9 * nframes);
   } else {
     int rc = build_reverse(w, nlist, nloc, nall, nnei, nframes, st);
     if (rc) return rc;
-    const int nrows = nframes * nall;
-    k_force_gather<T><<<(nrows + tb - 1) / tb, tb, 0, st>>>(nullptr, atom_virial, net, dR, rij,
-                                                           w.start, w.cnt, w.pairs_b, nloc,
-                                                           nall, nnei, nframes);
-    k_vir_reduce<T><<<nframes, 256, 0, st>>>(virial, atom_virial, nall);
+    launch_gather<T>(nullptr, atom_virial, net, dR, rij, w, nloc, nall, nnei, nframes, st);
+    launch_vir_reduce<T>(virial, atom_virial, w, nall, nframes, st);
   }
   GBDP_CHECK_LAUNCH("prod_virial_a");
   return GBDP_OK;

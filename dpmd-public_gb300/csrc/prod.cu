@@ -15,6 +15,7 @@
 //                 atom_virial_j is a gather in that fixed order, so the result
 //                 is bitwise reproducible run to run.
 // Frame virials are reduced in double in a fixed tree.
+#include <algorithm>
 #include <climits>
 
 #include "common.cuh"
@@ -94,128 +95,167 @@ __device__ __forceinline__ void scatter9(float* p, const float* t) {
 }
 
 // ---------------------------------------------------------- atomic mode --
-// One warp per centre row (kScatterWarps rows per CTA), lanes over slots, U slots per
-// lane per pass with every load of the pass issued before the first use.
-// F_j and atom_virial_j by (vector) reductions, F_i by one warp reduction;
-// the frame virial as per-warp partials in T, summed in double per CTA and
-// added to the frame's double accumulator.
+// Persistent warps, each over a contiguous range of centre rows; a row is
+// taken in chunks of 32 * U slots (one slot per lane and u).  The loads of
+// the next chunk (net 16 B, env deriv 48 B, neighbour index, r_ij for the
+// virial) are issued before the current chunk's scatter, so every warp keeps
+// a chunk in flight while its reductions drain.  F_j and atom_virial_j by
+// (vector) reductions, F_i by one warp reduction per row; the frame virial
+// as per-lane partials in T over at most 8 rows, folded into a double on
+// lane 0 and added to the frame's accumulator when the frame changes.
+template <typename T, int U, bool WV>
+struct ScatterChunk {
+  T g[U][4], d[U][12], r[U][3];
+  int j[U];
+};
+
+template <typename T, int U, bool WV>
+__device__ __forceinline__ void scatter_load(ScatterChunk<T, U, WV>& c, const T* __restrict__ net,
+                                             const T* __restrict__ dR, const T* __restrict__ rij,
+                                             const int* __restrict__ nlist, long row, int base,
+                                             int nnei, int lane) {
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int s = base + lane + 32 * u;
+    c.j[u] = -1;
+    if (s < nnei) {
+      const size_t rs = (size_t)row * nnei + s;
+      V4<T>::load4(net + rs * 4, c.g[u]);
+      V4<T>::load4(dR + rs * 12, c.d[u]);
+      V4<T>::load4(dR + rs * 12 + 4, c.d[u] + 4);
+      V4<T>::load4(dR + rs * 12 + 8, c.d[u] + 8);
+      c.j[u] = __ldg(nlist + rs);
+      if (WV) {
+        c.r[u][0] = __ldg(rij + rs * 3);
+        c.r[u][1] = __ldg(rij + rs * 3 + 1);
+        c.r[u][2] = __ldg(rij + rs * 3 + 2);
+      }
+    } else {
+#pragma unroll
+      for (int w = 0; w < 4; ++w) c.g[u][w] = T(0);
+#pragma unroll
+      for (int w = 0; w < 12; ++w) c.d[u][w] = T(0);
+#pragma unroll
+      for (int w = 0; w < 3; ++w) c.r[u][w] = T(0);
+    }
+  }
+}
+
 template <typename T>
 struct ScatterU {
-  static constexpr int U = 5;  // 160 slots per pass covers nnei = 138
+  static constexpr int U = 2;  // two 64-slot chunks in registers per lane
 };
 template <>
 struct ScatterU<double> {
-  static constexpr int U = 2;
+  static constexpr int U = 1;
 };
 
-constexpr int kScatterWarps = 4;  // 140 registers a thread: 3 CTAs per SM
+constexpr int kScatterWarps = 4;
 
-template <typename T, int U>
+template <typename T, int U, bool WV>
 __global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
     T* __restrict__ force, T* __restrict__ atom_virial, double* __restrict__ vir_acc,
     const T* __restrict__ net, const T* __restrict__ dR, const T* __restrict__ rij,
     const int* __restrict__ nlist, int nloc, int nall, int nnei, int nframes) {
-  __shared__ double s_vir[kScatterWarps][9];
-  __shared__ int s_frame[kScatterWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long row = (long)blockIdx.x * kScatterWarps + warp;  // frame * nloc + i
-  const bool want_v = atom_virial != nullptr;
+  __shared__ double s_vd[kScatterWarps][9];  // lane 0's double virial sums
+  const int lane = threadIdx.x & 31;
+  const long nw = (long)gridDim.x * kScatterWarps;
+  const long gw = (long)blockIdx.x * kScatterWarps + (threadIdx.x >> 5);
+  double* vd = s_vd[threadIdx.x >> 5];
+  const long rows = (long)nframes * nloc;
+  const long per = (rows + nw - 1) / nw;
+  const long r0 = gw * per, r1 = min(rows, r0 + per);
+  if (r0 >= r1) return;  // uniform over the warp; no CTA-wide barrier below
+  const int nch = (nnei + 32 * U - 1) / (32 * U);
   T vs[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) vs[q] = T(0);
-  int f = -1;
-  if (row < (long)nframes * nloc) {
-    f = (int)(row / nloc);
-    const int i = (int)(row - (long)f * nloc);
-    const T* g = net + (size_t)row * nnei * 4;
-    const T* d = dR + (size_t)row * nnei * 12;
-    const int* nl = nlist + (size_t)row * nnei;
-    const T* rr = want_v ? rij + (size_t)row * nnei * 3 : nullptr;
-    T ci[3] = {T(0), T(0), T(0)};
-    for (int base = 0; base < nnei; base += 32 * U) {
-      T gg[U][4], dd[U][12], r3[U][3];
-      int jj[U];
+  if (lane == 0)
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int s = base + lane + 32 * u;
-        jj[u] = -1;
-        if (s < nnei) {
-          V4<T>::load4(g + 4 * s, gg[u]);
-          V4<T>::load4(d + 12 * s, dd[u]);
-          V4<T>::load4(d + 12 * s + 4, dd[u] + 4);
-          V4<T>::load4(d + 12 * s + 8, dd[u] + 8);
-          jj[u] = __ldg(nl + s);
-          if (want_v) {
-            r3[u][0] = __ldg(rr + 3 * s);
-            r3[u][1] = __ldg(rr + 3 * s + 1);
-            r3[u][2] = __ldg(rr + 3 * s + 2);
-          }
-        } else {
+    for (int q = 0; q < 9; ++q) vd[q] = 0.;
+  int vf = (int)(r0 / nloc);  // frame of the virial partials
+  int nfold = 0;              // rows in vs since the last fold
+  auto fold = [&]() {
 #pragma unroll
-          for (int w = 0; w < 4; ++w) gg[u][w] = T(0);
+    for (int q = 0; q < 9; ++q) {
+      const T t = warp_sum(vs[q]);
+      vs[q] = T(0);
+      if (lane == 0) vd[q] += (double)t;
+    }
+    nfold = 0;
+  };
+  auto flush = [&]() {
+    if (lane == 0)
 #pragma unroll
-          for (int w = 0; w < 12; ++w) dd[u][w] = T(0);
-        }
-        if (!want_v || s >= nnei) r3[u][0] = r3[u][1] = r3[u][2] = T(0);
+      for (int q = 0; q < 9; ++q) {
+        atomicAdd(vir_acc + (size_t)vf * 9 + q, vd[q]);
+        vd[q] = 0.;
       }
+  };
+  T ci[3] = {T(0), T(0), T(0)};
+  ScatterChunk<T, U, WV> cur, nxt;
+  long row = r0;
+  int ch = 0;
+  scatter_load<T, U, WV>(cur, net, dR, rij, nlist, row, 0, nnei, lane);
+  while (row < r1) {
+    long nrow = row;
+    int nc = ch + 1;
+    if (nc == nch) {
+      nc = 0;
+      ++nrow;
+    }
+    if (nrow < r1) scatter_load<T, U, WV>(nxt, net, dR, rij, nlist, nrow, nc * 32 * U, nnei, lane);
+    const int f = (int)(row / nloc);
+    if (WV && f != vf) {  // uniform: close the previous frame's partials
+      fold();
+      flush();
+      vf = f;
+    }
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        T v[3];
+    for (int u = 0; u < U; ++u) {
+      T v[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        v[a] = cur.g[u][0] * cur.d[u][a] + cur.g[u][1] * cur.d[u][3 + a] +
+               cur.g[u][2] * cur.d[u][6 + a] + cur.g[u][3] * cur.d[u][9 + a];
+      ci[0] += v[0];
+      ci[1] += v[1];
+      ci[2] += v[2];
+      const int j = cur.j[u];
+      if (j < 0 || j >= nall) continue;
+      if (force) scatter3(force + ((size_t)f * nall + j) * 3, v);
+      if (WV) {
+        T t[9];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
-          v[a] = gg[u][0] * dd[u][a] + gg[u][1] * dd[u][3 + a] + gg[u][2] * dd[u][6 + a] +
-                 gg[u][3] * dd[u][9 + a];
-        ci[0] += v[0];
-        ci[1] += v[1];
-        ci[2] += v[2];
-        const int j = jj[u];
-        if (j < 0 || j >= nall) continue;
-        if (force) scatter3(force + ((size_t)f * nall + j) * 3, v);
-        if (want_v) {
-          T t[9];
 #pragma unroll
-          for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) t[a * 3 + b] = v[a] * cur.r[u][b];
+        scatter9(atom_virial + ((size_t)f * nall + j) * 9, t);
 #pragma unroll
-            for (int b = 0; b < 3; ++b) t[a * 3 + b] = v[a] * r3[u][b];
-          scatter9(atom_virial + ((size_t)f * nall + j) * 9, t);
-#pragma unroll
-          for (int q = 0; q < 9; ++q) vs[q] += t[q];
-        }
+        for (int q = 0; q < 9; ++q) vs[q] += t[q];
       }
     }
-    ci[0] = warp_sum(ci[0]);
-    ci[1] = warp_sum(ci[1]);
-    ci[2] = warp_sum(ci[2]);
-    if (lane == 0 && force) {
-      const T m[3] = {-ci[0], -ci[1], -ci[2]};
-      scatter3(force + ((size_t)f * nall + i) * 3, m);
+    if (ch == nch - 1) {  // row done: F_i -= sum over its slots
+      if (force) {
+        ci[0] = warp_sum(ci[0]);
+        ci[1] = warp_sum(ci[1]);
+        ci[2] = warp_sum(ci[2]);
+        if (lane == 0) {
+          const int i = (int)(row - (long)f * nloc);
+          const T m[3] = {-ci[0], -ci[1], -ci[2]};
+          scatter3(force + ((size_t)f * nall + i) * 3, m);
+        }
+      }
+      ci[0] = ci[1] = ci[2] = T(0);
+      if (WV && ++nfold == 8) fold();
     }
+    cur = nxt;
+    row = nrow;
+    ch = nc;
   }
-  if (want_v && vir_acc) {  // uniform over the CTA
-#pragma unroll
-    for (int q = 0; q < 9; ++q) vs[q] = warp_sum(vs[q]);
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < 9; ++q) s_vir[warp][q] = (double)vs[q];
-      s_frame[warp] = f;
-    }
-    __syncthreads();
-    if (threadIdx.x < 9) {
-      // rows of a CTA are consecutive: runs of equal frames, idle warps last
-      const int q = threadIdx.x;
-      double acc = 0.;
-      int cur = -1;
-      for (int w = 0; w < kScatterWarps; ++w) {
-        const int fw = s_frame[w];
-        if (fw != cur) {
-          if (cur >= 0) atomicAdd(vir_acc + cur * 9 + q, acc);
-          cur = fw;
-          acc = 0.;
-        }
-        acc += s_vir[w][q];
-      }
-      if (cur >= 0) atomicAdd(vir_acc + cur * 9 + q, acc);
-    }
+  if (WV) {
+    fold();
+    flush();
   }
 }
 
@@ -567,14 +607,38 @@ int build_reverse(const ProdWs& w, const int* nlist, int nloc, int nall, int nne
   return GBDP_OK;
 }
 
+// persistent grid: as many CTAs as fit on the device at once (occupancy
+// queried once per kernel), never more than there are warps' worth of rows
+template <typename T, bool WV>
+int scatter_cap() {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_atomic<T, ScatterU<T>::U, WV>,
+                                                kScatterWarps * 32, 0);
+  return std::max(1, sms * std::max(1, per_sm));
+}
+
+template <typename T, bool WV>
+unsigned scatter_grid(size_t rows) {
+  static const int cap = scatter_cap<T, WV>();  // initialised once, thread-safe
+  const size_t need = (rows + kScatterWarps - 1) / kScatterWarps;
+  return (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)cap, need));
+}
+
 template <typename T>
 void launch_atomic(T* force, T* atom_virial, double* vir_acc, const T* net, const T* dR,
                    const T* rij, const int* nlist, int nloc, int nall, int nnei, int nframes,
                    cudaStream_t st) {
   const size_t rows = (size_t)nframes * nloc;
-  k_scatter_atomic<T, ScatterU<T>::U>
-      <<<(unsigned)((rows + kScatterWarps - 1) / kScatterWarps), kScatterWarps * 32, 0, st>>>(
-      force, atom_virial, vir_acc, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+  if (atom_virial)
+    k_scatter_atomic<T, ScatterU<T>::U, true><<<scatter_grid<T, true>(rows), kScatterWarps * 32,
+                                                0, st>>>(force, atom_virial, vir_acc, net, dR,
+                                                         rij, nlist, nloc, nall, nnei, nframes);
+  else
+    k_scatter_atomic<T, ScatterU<T>::U, false><<<scatter_grid<T, false>(rows),
+                                                 kScatterWarps * 32, 0, st>>>(
+        force, nullptr, nullptr, net, dR, rij, nlist, nloc, nall, nnei, nframes);
 }
 
 template <typename T>
@@ -617,8 +681,8 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
                "prod_force/virial: net_deriv and env_deriv must be 16-byte aligned");
   if (!det) {
     cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
-    launch_atomic<T>(force, atom_virial, virial ? w.vir_acc : nullptr, net, dR, rij, nlist, nloc,
-                     nall, nnei, nframes, st);
+    launch_atomic<T>(force, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
+                     nframes, st);
     if (virial) k_vir_finish<T><<<1, 256, 0, st>>>(virial, w.vir_acc, 9 * nframes);
   } else {
     int rc = build_reverse(w, nlist, nloc, nall, nnei, nframes, st);

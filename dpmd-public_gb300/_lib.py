@@ -82,6 +82,9 @@ _SIGS = {
     "gbdp_fitting_tc_workspace_bytes": (_Z, [_I]),
     "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
     "gbdp_fitting_tc_status": (_I, [_P, _I, _P]),
+    "gbdp_embed_tc_net_bytes": (_Z, []),
+    "gbdp_embed_fwd_tc_bf16": (_I, [_P] * 7 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
+    "gbdp_embed_bwd_tc_bf16": (_I, [_P] * 8 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
 }
 
 

@@ -13,6 +13,10 @@
                  (the sequence of deepmd/tf/descriptor/se_a.py:652-765).
 * ``plain``      the uncompressed model: as ``ops`` but the embedding nets
                  run as matmuls (deepmd/pt/model/descriptor/se_a.py:823-845).
+* ``plain-tc``   the uncompressed model with the embedding nets fused with
+                 G^T R on the tensor cores (BF16 MMAs, FP32 accumulation;
+                 libgbdp), forward and backward, then the force / virial
+                 operators.
 
 Energies and virials are reduced per frame in float64.
 """
@@ -37,6 +41,76 @@ def _ptr(t):
 
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ----------------------------------------------- tensor-core embedding --
+# Per-net parameter block of the BF16 embedding kernels (csrc/embed_tc.cu):
+# weight images in the shared-memory layout the MMAs read, then FP32 params.
+EMB_TC_WIDTHS = ((25, 50, 100), (3, 6, 12))
+_NET_B2, _NET_B3, _NET_PAR, _NET_B3T, _NET_B2T, _NET_BYTES = 0, 8192, 24576, 26624, 43008, 51200
+
+
+def _bf16_bits(a: np.ndarray) -> np.ndarray:
+    """FP32 -> BF16 bit patterns, rounded to nearest even."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def _sw128_image(m: np.ndarray, nrows: int) -> bytes:
+    """m [n, k] as the BF16 K-major operand image with nrows rows (zero
+    padded) and K in chunks of 64: chunk c holds rows of 128 bytes, and the
+    16-byte piece p of row n is stored at piece p ^ (n & 7)."""
+    n, k = m.shape
+    nch = (k + 63) // 64
+    pad = np.zeros((nrows, nch * 64), np.float32)
+    pad[:n, :k] = m
+    bits = _bf16_bits(pad).reshape(nrows, nch, 8, 8).transpose(1, 0, 2, 3)
+    out = np.empty_like(bits)
+    rows = np.arange(nrows)
+    for piece in range(8):
+        out[:, rows, piece ^ (rows & 7), :] = bits[:, :, piece, :]
+    return out.tobytes()
+
+
+def embed_tc_images(emb) -> np.ndarray:
+    """[nnets, 51200] uint8: per embedding net W2^T, W3^T (forward), w1, b1,
+    b2, b3 (FP32), W3, W2 (backward)."""
+    out = np.zeros((len(emb), _NET_BYTES), np.uint8)
+    for k, layers in enumerate(emb):
+        (w1, b1), (w2, b2), (w3, b3) = [(np.asarray(l["w"], np.float32),
+                                         np.asarray(l["b"], np.float32)) for l in layers]
+        blk = out[k]
+
+        def put(off, data):
+            blk[off:off + len(data)] = np.frombuffer(data, np.uint8)
+
+        put(_NET_B2, _sw128_image(w2.T, 64))
+        put(_NET_B3, _sw128_image(w3.T, 128))
+        par = np.zeros(320, np.float32)
+        par[:w1.shape[1]] = w1[0]
+        par[64:64 + len(b1)] = b1
+        par[128:128 + len(b2)] = b2
+        par[192:192 + len(b3)] = b3
+        put(_NET_PAR, par.tobytes())
+        put(_NET_B3T, _sw128_image(w3, 64))
+        put(_NET_B2T, _sw128_image(w2, 64))
+    return out
+
+
+def _emb_tc_ok(cfg, emb) -> bool:
+    """The tensor-core kernels serve 1 -> N1 -> N2 -> N3 nets of the built
+    widths whose skips follow the widths (none, then identity or [x, x])."""
+    if tuple(cfg.neuron) not in EMB_TC_WIDTHS:
+        return False
+    for net in emb:
+        if len(net) != 3 or net[0]["skip"] != "none":
+            return False
+        for l in net[1:]:
+            n_in, n_out = np.asarray(l["w"]).shape
+            want = "same" if n_in == n_out else ("double" if n_out == 2 * n_in else "none")
+            if l["skip"] != want:
+                return False
+    return True
 
 
 class SeAModel:
@@ -125,6 +199,10 @@ class SeAModel:
                 ip = (_P * nh)(*[(0 if idt is None else idt.data_ptr()) for _, _, idt, _ in hidden])
                 wout = wf[:, 0].contiguous()
                 self._fit_c.append((nh, widths, wp, bp, ip, wout, float(bf[0])))
+        # BF16 tensor-core embedding for the uncompressed form (FP32 models)
+        self._emb_tc = None
+        if dtype == torch.float32 and _emb_tc_ok(cfg, params["emb"]):
+            self._emb_tc = torch.from_numpy(embed_tc_images(params["emb"])).to(self.device)
         self._sfx = L.sfx(dtype)
         self._lib = L.load()
 
@@ -277,6 +355,66 @@ class SeAModel:
                 ctypes.c_size_t(ws.numel()), _stream()), "fitting_fwd_bwd")
             if float(self.params_bias[t]) != 0.0:
                 b.ae[s0:s0 + nt].add_(self.params_bias[t])
+
+    def embed_tc_forward(self, b: "Batch", em: torch.Tensor):
+        """X [nloc, 4, M] and D (rows of b) of the uncompressed descriptor
+        from the env matrix, embedding on the tensor cores (BF16)."""
+        if self._emb_tc is None:
+            raise RuntimeError("the tensor-core embedding serves FP32 models with embedding "
+                               f"widths {EMB_TC_WIDTHS}")
+        cfg = self.cfg
+        n1, n2, n3 = cfg.neuron
+        sel = (ctypes.c_int * cfg.ntypes)(*[int(x) for x in cfg.sel])
+        L.check(self._lib.gbdp_embed_fwd_tc_bf16(
+            _ptr(b.X), _ptr(b.D), _ptr(getattr(b, "D_lo", None)), _ptr(b.drow), _ptr(em),
+            _ptr(b.atype), _ptr(b.units), b.nunits, _ptr(self._emb_tc), cfg.ntypes, sel,
+            int(cfg.type_one_side), b.nloc, cfg.nnei, n1, n2, n3, cfg.axis_neuron,
+            _ptr(b.emb_status), _stream()), "embed_fwd_tc")
+
+    def embed_tc_backward(self, b: "Batch", em: torch.Tensor) -> torch.Tensor:
+        """dE/d(env matrix) [nloc, nnei, 4] from b.dD (the fitting's dE/dD)."""
+        cfg = self.cfg
+        n1, n2, n3 = cfg.neuron
+        sel = (ctypes.c_int * cfg.ntypes)(*[int(x) for x in cfg.sel])
+        L.check(self._lib.gbdp_embed_bwd_tc_bf16(
+            _ptr(b.net_deriv), _ptr(b.dx_work), _ptr(b.dD), _ptr(b.X), _ptr(b.drow), _ptr(em),
+            _ptr(b.atype), _ptr(b.units), b.nunits, _ptr(self._emb_tc), cfg.ntypes, sel,
+            int(cfg.type_one_side), b.nloc, cfg.nnei, n1, n2, n3, cfg.axis_neuron,
+            _ptr(b.emb_status), _stream()), "embed_bwd_tc")
+        return b.net_deriv
+
+    def step_plain_tc(self, b: "Batch", coord: torch.Tensor):
+        """The uncompressed model on the GPU with the embedding nets on the
+        tensor cores: env matrix (with derivatives) -> fused embedding +
+        G^T R + D (BF16 MMAs) -> fitting -> fused embedding backward ->
+        prod_force_se_a / prod_virial_se_a per frame.  E [nframes] f64,
+        F [nloc_total, 3], virial [nframes, 9] f64."""
+        cfg = self.cfg
+        nnei = cfg.nnei
+        b.ensure_plain_tc(self)
+        env = env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth,
+                             list(cfg.sel), check_status=False, out=b.env_full)
+        self.embed_tc_forward(b, env.em)
+        if self._tc_nets is not None:
+            self.fitting_tc(b)
+        else:
+            self.fitting_rows(b)
+        net = self.embed_tc_backward(b, env.em)
+        forces, virs = [], []
+        for f in range(b.nframes):
+            a0, nl = int(b.plan.atom_off[f]), int(b.plan.nloc[f])
+            natoms = torch.tensor([nl, nl] + [0] * cfg.ntypes, dtype=torch.int32)
+            nd = net[a0:a0 + nl].reshape(1, -1)
+            ed = env.em_deriv[a0:a0 + nl].reshape(1, -1)
+            nlst = env.nlist[a0:a0 + nl].reshape(1, -1)
+            forces.append(prod_force_se_a_impl(nd, ed, nlst, natoms, nnei, 0).reshape(nl, 3))
+            v, _ = prod_virial_se_a_impl(nd, ed, env.rij[a0:a0 + nl].reshape(1, -1), nlst, natoms,
+                                         nnei, 0)
+            virs.append(v.reshape(9))
+        L.check(getattr(self._lib, f"gbdp_frame_energy_{self._sfx}")(
+            _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes,
+            _stream()), "frame_energy")
+        return b.energy, torch.cat(forces), torch.stack(virs).to(torch.float64)
 
     # --------------------------------------------- operator-contract forms --
     def _descriptor_from_em(self, em: torch.Tensor, atype: torch.Tensor, compressed: bool):
@@ -537,6 +675,38 @@ class Batch:
         self.force = torch.empty((n, 3), dtype=dt, device=dev)
         self.vir = torch.empty((self.nframes, 9), dtype=torch.float64, device=dev)
         self.energy = torch.empty((self.nframes,), dtype=torch.float64, device=dev)
+
+    def ensure_plain_tc(self, model: SeAModel):
+        """Buffers of the tensor-core plain form (allocated once): atom pairs
+        of one centre type, the full env matrix with derivatives, dE/d(env)
+        and the embedding kernels' scratch and status."""
+        if hasattr(self, "units"):
+            return
+        cfg = model.cfg
+        dev = self.atype.device
+        flat = self.atype.cpu().numpy()
+        pairs = []
+        for t in range(cfg.ntypes):
+            idx = np.nonzero(flat == t)[0]
+            for k in range(0, len(idx), 2):
+                pairs.append((idx[k], idx[k + 1] if k + 1 < len(idx) else -1))
+        self.nunits = len(pairs)
+        self.units = torch.tensor(np.asarray(pairs, np.int32).reshape(-1, 2), device=dev)
+        n, nnei, dt = self.nloc, cfg.nnei, model.dtype
+        e = EnvMatResult()
+        e.em = torch.empty((n, nnei, 4), dtype=dt, device=dev)
+        e.em_deriv = torch.empty((n, nnei, 4, 3), dtype=dt, device=dev)
+        e.rij = torch.empty((n, nnei, 3), dtype=dt, device=dev)
+        e.nlist = torch.empty((n, nnei), dtype=torch.int32, device=dev)
+        e.nlist_ext = None
+        e.ext_coord = torch.empty((self.plan.ext_total, 3), dtype=dt, device=dev)
+        e.ext_type = torch.empty((self.plan.ext_total,), dtype=torch.int32, device=dev)
+        e.ext_map = torch.empty((self.plan.ext_total,), dtype=torch.int32, device=dev)
+        e.ext_nall = torch.empty((self.nframes,), dtype=torch.int32, device=dev)
+        self.env_full = e
+        self.net_deriv = torch.empty((n, nnei, 4), dtype=dt, device=dev)
+        self.dx_work = torch.empty((n, 4, cfg.neuron[-1]), dtype=dt, device=dev)
+        self.emb_status = torch.zeros(1, dtype=torch.int32, device=dev)
 
     def fit_ws(self, t: int, model: SeAModel):
         """Workspace of the native fitting call for type t (allocated once)."""

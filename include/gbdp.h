@@ -431,6 +431,40 @@ GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, cons
  * run on this workspace (GBDP_OK or GBDP_STATUS_TIMEOUT). */
 GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream);
 
+/* ---- uncompressed embedding net on the tensor cores (BF16) ----------------
+ * Replaces the plain-form embedding of DescrptBlockSeA.forward
+ * (deepmd/pt/model/descriptor/se_a.py:750-866; EmbeddingNet / MLPLayer,
+ * deepmd/pt/model/network/mlp.py:188-219) together with its G^T R
+ * contraction and D = X^T X[:, :axis]: layers 2 and 3 as BF16 tcgen05 MMAs
+ * with FP32 accumulation, everything else in FP32.  Built for embedding
+ * widths 25-50-100 and 3-6-12 (tanh, identity / [x, x] skips).
+ *
+ * nets: one block of gbdp_embed_tc_net_bytes() per net (net index tj when
+ * type_one_side, else tj * ntypes + ti), 16-byte aligned, holding the bf16
+ * weight images and FP32 parameters in the layout the kernels stage (built
+ * once per model on the host).  units: [nunits, 2] pairs of atoms of one
+ * centre type (second entry -1 when absent), covering every local atom once.
+ * sel: host array of ntypes.  status: device int, GBDP_STATUS_TIMEOUT if a
+ * tensor-core wait gave up.
+ *
+ * forward:  X [nloc, 4, n3] (sums / nnei), D [rows, n3 * axis] at row drow[i]
+ *           (drow null: row i), D_lo optional TF32 remainder of D.
+ * backward: from dE/dD (same rows), the gradient wrt the env matrix
+ *           net_deriv [nloc, nnei, 4] (every slot written); dx_work is
+ *           caller scratch of nloc * 4 * n3 floats. */
+GBDP_API size_t gbdp_embed_tc_net_bytes(void);
+GBDP_API int gbdp_embed_fwd_tc_bf16(float* X, float* D, float* D_lo, const int* drow,
+                                    const float* em, const int* atype, const int* units,
+                                    int nunits, const void* nets, int ntypes, const int* sel,
+                                    int type_one_side, int nloc, int nnei, int n1, int n2, int n3,
+                                    int axis, int* status, gbdp_stream stream);
+GBDP_API int gbdp_embed_bwd_tc_bf16(float* net_deriv, float* dx_work, const float* dD,
+                                    const float* X, const int* drow, const float* em,
+                                    const int* atype, const int* units, int nunits,
+                                    const void* nets, int ntypes, const int* sel,
+                                    int type_one_side, int nloc, int nnei, int n1, int n2, int n3,
+                                    int axis, int* status, gbdp_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -227,8 +227,9 @@ def main():
     ap.add_argument("--md-out-scale", type=float, default=0.01,
                     help="md786k: scale of the random fitting output layer (physical force range)")
     ap.add_argument("--profile", action="store_true",
-                    help="profiling run: set up, then 2 fused steps and 1 operator-form step "
-                         "between cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+                    help="profiling run: set up, then 2 fused steps, 1 operator-form step and "
+                         "1 plain tensor-core step between cudaProfilerStart/Stop (for ncu "
+                         "--profile-from-start off)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.fit_mode is None:
@@ -274,11 +275,16 @@ def main():
         for _ in range(3):
             model.step_fused(batch, coord)
         model.step_ops(batch, coord, compressed=True)
+        mpt = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(),
+                            dev, torch.float32, fit_mode=args.fit_mode)
+        bpt = mpt.batch([t], b[None])
+        mpt.step_plain_tc(bpt, coord)
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
         for _ in range(2):
             model.step_fused(batch, coord)
         model.step_ops(batch, coord, compressed=True)
+        mpt.step_plain_tc(bpt, coord)
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
         print(json.dumps({"profile": "ok", "status": batch.status()}))
@@ -390,6 +396,8 @@ def main():
     torch.cuda.synchronize()
     plain_ms = (time.perf_counter() - p0) / n_plain * 1e3
 
+    plain_tc = plain_tc_times(se_a, cfg, m64, args.fit_mode, t, b, coord, flush, ws)
+
     out = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -403,6 +411,7 @@ def main():
            "graph_kernels_per_step": launches,
            "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                      "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
+           "plain_tc": plain_tc,
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
            "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
            "clocks": clk.summary()}
@@ -420,6 +429,8 @@ def main():
             "energy_per_atom_eV": abs(float(E_g[0]) - E64) / nat,
             "virial_max_abs_eV": float(np.abs(V_g[0].cpu().numpy() - V64).max()),
             "plain_force_max_abs_eV_per_A": float(np.abs(Fp.detach().cpu().numpy() - F64).max()),
+            "plain_tc_force_max_abs_eV_per_A_vs_plain_fp64": plain_tc.pop("_force_err_fn")(
+                composite, np_model, c, t, b),
             "reference": "FP64 CPU composite (oracle) of the compressed model"}
         if not args.no_cpu:
             out["cpu_baseline"] = {k: v for k, v in cpu_baseline((c, t, b), np_model, steps=2).items()
@@ -713,6 +724,68 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
             ts.append(s.elapsed_time(e))
         res[name] = {"ms": statistics.median(ts)}
     return res
+
+
+def plain_tc_times(se_a, cfg, m64, fit_mode, t, b, coord, flush, ws, reps: int = 10):
+    """The uncompressed model with the embedding nets on the tensor cores
+    (BF16 MMAs, FP32 accumulation): the whole step captured in a CUDA graph
+    and timed with CUDA events (L2 flushed between steps), plus the two
+    embedding kernels alone."""
+    import torch
+
+    m = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(),
+                      coord.device, torch.float32, fit_mode=fit_mode)
+    bt = m.batch([t], b[None])
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            m.step_plain_tc(bt, coord)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        E, F, V = m.step_plain_tc(bt, coord)
+    g.replay()
+    torch.cuda.synchronize()
+    if int(bt.emb_status.item()) != 0:
+        raise RuntimeError("tensor-core embedding reported a device status")
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            flush()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            fn()
+            s1.record()
+            torch.cuda.synchronize()
+            ts.append(s0.elapsed_time(s1))
+        return statistics.median(ts)
+
+    step_ms = timed(g.replay)
+    em = bt.env_full.em
+    fwd_ms = timed(lambda: m.embed_tc_forward(bt, em))
+    bwd_ms = timed(lambda: m.embed_tc_backward(bt, em))
+    nat = len(t)
+    F_dev = F
+
+    def force_err(composite, np_model, c, t_, b_):
+        E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t_, b_, None, None)
+        return float(np.abs(F_dev.cpu().numpy().astype(np.float64) - F64).max())
+
+    # MMA work per neighbour row (algorithmic widths): forward 1x25x50 + 50x100;
+    # backward recomputes the forward and adds the two transposed products
+    n1, n2, n3 = cfg.neuron
+    rows = nat * cfg.nnei
+    f_fwd = 2 * (n1 * n2 + n2 * n3) * rows
+    return {"value": ws * nat / (step_ms * 1e-3), "ms_per_step": step_ms,
+            "form": "uncompressed, embedding + G^T R on tcgen05 BF16 (FP32 accumulation), "
+                    f"fitting {fit_mode}, force/virial operators; CUDA graph",
+            "embed_fwd_ms": fwd_ms, "embed_bwd_ms": bwd_ms,
+            "embed_mma_tflops": {"fwd": f_fwd / (fwd_ms * 1e-3) / 1e12,
+                                 "bwd": 2 * f_fwd / (bwd_ms * 1e-3) / 1e12},
+            "_force_err_fn": force_err}
 
 
 def op_kernel_times(model, batch, coord, flush, peaks, reps: int = 5):

@@ -15,7 +15,8 @@
 //
 // Work unit: two atoms of one centre type.  For each neighbour type the two
 // atoms' section rows are concatenated and cut into 128-row tiles; a tile's
-// rows are one thread's each (thread r of a warpgroup <-> TMEM lane r).
+// rows are one thread's each (thread r <-> TMEM lane r); one warpgroup per
+// CTA, two CTAs per SM.
 //   layer 1 (SIMT)  -> A (bf16, 128 x 64, SW128 K-major, shared)
 //   MMA  D2 = A W2   (N 64, TMEM columns 0-63)
 //   epilogue 2       -> A (bf16), the layer-2 output in FP32 registers
@@ -46,8 +47,11 @@ constexpr int kNetFwdBytes = kNetPar + 320 * 4;  // what the forward stages
 constexpr int kParW1 = 0, kParB1 = 64, kParB2 = 128, kParB3 = 192;
 
 constexpr int kRows = 128;
-constexpr int kGStride = 129;  // FP32 G rows in shared memory (odd: no bank conflicts)
-constexpr int kSlot = 26624;   // one staged net (1024-aligned)
+// FP32 rows of G / dG in shared memory: an odd stride, so that a warp's
+// 32 rows writing one column hit 32 banks
+template <int N3>
+__host__ __device__ constexpr int gstride() { return N3 % 2 ? N3 : N3 + 1; }
+constexpr int kSlot = 26624;   // one staged net, forward part (1024-aligned)
 constexpr int kMaxTypes = 8;
 
 struct EmbArgs {
@@ -123,6 +127,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// the same load without the wait: several may be in flight before one
+// tcgen05.wait::ld (tmem_wait) makes all their registers valid
+__device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&h);
@@ -172,33 +191,40 @@ struct Skip {
 template <int N2, int N3, int G0>
 __device__ __forceinline__ void epi3(uint32_t trow, const float* par, const float* h2, bool live,
                                      float* grow) {
+  constexpr int NC = N3 > G0 * 64 ? ((N3 - G0 * 64 + 15) / 16 < 4 ? (N3 - G0 * 64 + 15) / 16 : 4)
+                                  : 0;  // 16-column chunks of this half
+  if constexpr (NC > 0) {
+  uint32_t v[4][16];
 #pragma unroll
-  for (int c16 = 0; c16 < 4; ++c16) {
+  for (int c16 = 0; c16 < NC; ++c16) tmem_ld16_nw(trow + 128 + G0 * 64 + c16 * 16, v[c16]);
+  tmem_wait();
+#pragma unroll
+  for (int c16 = 0; c16 < NC; ++c16) {
     const int m0 = G0 * 64 + c16 * 16;
-    if (m0 >= N3) break;
-    float v[16];
-    tmem_ld16(trow + 128 + m0, v);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       const int m = m0 + k;
       if (m < N3) {
         float gv = 0.f;
-        if (live) gv = tanh_fast(v[k] + par[kParB3 + m]) + Skip<N2, N3>::at(h2, m);
+        if (live)
+          gv = tanh_fast(__uint_as_float(v[c16][k]) + par[kParB3 + m]) + Skip<N2, N3>::at(h2, m);
         grow[m] = gv;
       }
     }
+  }
   }
 }
 
 // ---------------------------------------------------------------- kernel --
 template <int N1, int N2, int N3>
-__global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbArgs p) {
+__global__ void __launch_bounds__(128, 2) k_emb_fwd(const __grid_constant__ EmbArgs p) {
   static_assert(N1 <= 32 && N2 <= 64 && N3 <= 128 && N3 >= 1, "embedding widths");
+  constexpr int kGStride = gstride<N3>();
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* slots = sm;                  // 2 staged nets
-  unsigned char* atile = sm + 2 * kSlot;      // A operand, 16 KiB
+  unsigned char* slot = sm;                   // the staged net (one at a time)
+  unsigned char* atile = sm + kSlot;          // A operand, 16 KiB
   float* gsm = reinterpret_cast<float*>(atile + 16384);   // [128][kGStride]
   float* rsm = gsm + kRows * kGStride;                    // [128][4]
   float* xacc = rsm + kRows * 4;                          // [2][4][128]
@@ -206,14 +232,13 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   int* cached = reinterpret_cast<int*>(tslot + 1);        // net index held by each slot
 
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, g = warp >> 2;  // TMEM lane quarter, column half
-  const int r = q * 32 + lane;             // this thread's tile row
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int r = tid;                       // this thread's tile row = TMEM lane
 
   if (tid == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
-    cached[0] = cached[1] = -1;
+    cached[0] = -1;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
@@ -221,12 +246,12 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  for (int k = tid; k < 2 * 4 * 128; k += 256) xacc[k] = 0.f;
+  for (int k = tid; k < 2 * 4 * 128; k += 128) xacc[k] = 0.f;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
   unsigned phase = 0;
   bool alive = true;
 
@@ -242,16 +267,14 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
       const int sel = p.sec[tj + 1] - p.sec[tj];
       if (sel == 0) continue;
       const int net = p.type_one_side ? tj : tj * p.ntypes + ti;
-      const int s = tj & 1;
-      unsigned char* slot = slots + s * kSlot;
-      if (cached[s] != net) {  // uniform: stage this net's weights and params
+      if (cached[0] != net) {  // uniform: stage this net's weights and params
         __syncthreads();
         const uint4* src = reinterpret_cast<const uint4*>(p.nets + (size_t)net * kNetBytes);
         uint4* dst = reinterpret_cast<uint4*>(slot);
-        for (int k = tid; k < kNetFwdBytes / 16; k += 256) dst[k] = __ldg(src + k);
+        for (int k = tid; k < kNetFwdBytes / 16; k += 128) dst[k] = __ldg(src + k);
         fence_proxy_async_smem();
         __syncthreads();
-        if (tid == 0) cached[s] = net;
+        if (tid == 0) cached[0] = net;
         __syncthreads();
       }
       const float* par = reinterpret_cast<const float*>(slot + kNetPar);
@@ -269,16 +292,14 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
           const int slot_j = p.sec[tj] + gi - a * sel;
           e = __ldg(reinterpret_cast<const float4*>(p.em + ((size_t)atom * p.nnei + slot_j) * 4));
         }
-        if (g == 0) reinterpret_cast<float4*>(rsm)[r] = e;
+        reinterpret_cast<float4*>(rsm)[r] = e;
         // ---- layer 1 (FP32): h1 = tanh(s w1 + b1), all N1 columns per thread
         float h1[N1];
 #pragma unroll
         for (int j = 0; j < N1; ++j) h1[j] = tanh_fast(fmaf(e.x, par[kParW1 + j], par[kParB1 + j]));
         // A = h1 (bf16), this warpgroup's four 16-byte pieces of the row
-        if (g == 0)
-          st_half<N1, 0>(atile, r, h1);
-        else
-          st_half<N1, 1>(atile, r, h1);
+        st_half<N1, 0>(atile, r, h1);
+        st_half<N1, 1>(atile, r, h1);
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -296,22 +317,26 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
         tc_fence_after();
         // ---- epilogue 2: h2 = tanh(D2 + b2) + skip(h1), all N2 columns
         float h2[N2];
+        {
+          constexpr int NC = (N2 + 15) / 16;
+          uint32_t v[NC][16];
 #pragma unroll
-        for (int c16 = 0; c16 < (N2 + 15) / 16; ++c16) {
-          float v[16];
-          tmem_ld16(trow + c16 * 16, v);
+          for (int c16 = 0; c16 < NC; ++c16) tmem_ld16_nw(trow + c16 * 16, v[c16]);
+          tmem_wait();
 #pragma unroll
-          for (int k = 0; k < 16; ++k) {
-            const int j = c16 * 16 + k;
-            if (j < N2) h2[j] = tanh_fast(v[k] + par[kParB2 + j]) + Skip<N1, N2>::at(h1, j);
-          }
+          for (int c16 = 0; c16 < NC; ++c16)
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              const int j = c16 * 16 + k;
+              if (j < N2)
+                h2[j] = tanh_fast(__uint_as_float(v[c16][k]) + par[kParB2 + j]) +
+                        Skip<N1, N2>::at(h1, j);
+            }
         }
         tc_fence_before();
         __syncthreads();  // every lane has read D2 and MMA 2 is done with A
-        if (g == 0)
-          st_half<N2, 0>(atile, r, h2);
-        else
-          st_half<N2, 1>(atile, r, h2);
+        st_half<N2, 0>(atile, r, h2);
+        st_half<N2, 1>(atile, r, h2);
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
@@ -327,18 +352,17 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
         if (!alive) break;
         tc_fence_after();
         // ---- epilogue 3: G = tanh(D3 + b3) + skip(h2), this half's columns
-        if (g == 0)
-          epi3<N2, N3, 0>(trow, par, h2, live, gsm + r * kGStride);
-        else
-          epi3<N2, N3, 1>(trow, par, h2, live, gsm + r * kGStride);
+        epi3<N2, N3, 0>(trow, par, h2, live, gsm + r * kGStride);
+        epi3<N2, N3, 1>(trow, par, h2, live, gsm + r * kGStride);
         tc_fence_before();
         __syncthreads();
-        // ---- G^T R: thread (atom half, column m) over the tile rows of its atom
-        {
-          const int ah = tid >> 7, m = tid & 127;
-          if (ah < na && m < N3) {
+        // ---- G^T R: thread m, for each atom over that atom's tile rows
+        for (int ah = 0; ah < na; ++ah) {
+          const int m = tid;
+          if (m < N3) {
             const int lo = max(0, ah * sel - t0), hi = min(nrow, (ah + 1) * sel - t0);
             float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
             for (int rr = lo; rr < hi; ++rr) {
               const float4 R = reinterpret_cast<const float4*>(rsm)[rr];
               const float gv = gsm[rr * kGStride + m];
@@ -356,9 +380,9 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
     }
     if (!alive) break;
     // ---- X and D of the unit's atoms
-    {
-      const int ah = tid >> 7, m = tid & 127;
-      if (ah < na && m < N3) {
+    for (int ah = 0; ah < na; ++ah) {
+      const int m = tid;
+      if (m < N3) {
         const int atom = ah ? at1 : at0;
         float xm[4];
 #pragma unroll
@@ -384,7 +408,7 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
       }
     }
     __syncthreads();
-    for (int k = tid; k < 2 * 4 * 128; k += 256) xacc[k] = 0.f;
+    for (int k = tid; k < 2 * 4 * 128; k += 128) xacc[k] = 0.f;
     __syncthreads();
   }
   tc_fence_before();
@@ -397,34 +421,40 @@ __global__ void __launch_bounds__(256, 1) k_emb_fwd(const __grid_constant__ EmbA
 // dX (gradient wrt the un-normalised sums X * nnei) of every atom from dE/dD:
 // D[m][a] = sum_c X[c][m] X[c][a] (a < A), so
 //   dX[c][m] = sum_a dD[m][a] X[c][a] + [m < A] sum_m' dD[m'][m] X[c][m'].
-// One CTA per atom, one thread per column m.
+// One CTA per atom: threads over m for the first term, threads over (c, a)
+// for the second (4 A sums of N3 terms), combined through shared memory.
 __global__ void k_emb_dx(float* __restrict__ dxs, const float* __restrict__ dD,
                          const float* __restrict__ X, const int* __restrict__ drow, int N3, int A,
                          float inv_nnei) {
   extern __shared__ float sh[];
-  float* xs = sh;            // [4][N3]
-  float* dds = sh + 4 * N3;  // [N3][A]
+  float* xs = sh;                // [4][N3]
+  float* dds = sh + 4 * N3;      // [N3][A]
+  float* t2 = dds + N3 * A;      // [4][A] second term
   const int atom = blockIdx.x;
   const size_t row = drow ? (size_t)drow[atom] : (size_t)atom;
   for (int k = threadIdx.x; k < 4 * N3; k += blockDim.x) xs[k] = X[(size_t)atom * 4 * N3 + k];
   for (int k = threadIdx.x; k < N3 * A; k += blockDim.x) dds[k] = dD[row * N3 * A + k];
   __syncthreads();
-  const int m = threadIdx.x;
-  if (m >= N3) return;
-  float o[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int a = 0; a < A; ++a) {
-    const float w = dds[m * A + a];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) o[c] = fmaf(w, xs[c * N3 + a], o[c]);
+  for (int k = threadIdx.x; k < 4 * A; k += blockDim.x) {
+    const int c = k / A, a = k - c * A;
+    float o = 0.f;
+    for (int m2 = 0; m2 < N3; ++m2) o = fmaf(dds[m2 * A + a], xs[c * N3 + m2], o);
+    t2[k] = o;
   }
-  if (m < A)
-    for (int m2 = 0; m2 < N3; ++m2) {
-      const float w = dds[m2 * A + m];
+  __syncthreads();
+  for (int m = threadIdx.x; m < N3; m += blockDim.x) {
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < A; ++a) {
+      const float w = dds[m * A + a];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) o[c] = fmaf(w, xs[c * N3 + m2], o[c]);
+      for (int c = 0; c < 4; ++c) o[c] = fmaf(w, xs[c * N3 + a], o[c]);
     }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) dxs[((size_t)atom * 4 + c) * N3 + m] = o[c] * inv_nnei;
+    for (int c = 0; c < 4; ++c) {
+      if (m < A) o[c] += t2[c * A + m];
+      dxs[((size_t)atom * 4 + c) * N3 + m] = o[c] * inv_nnei;
+    }
+  }
 }
 
 struct EmbBwdArgs {
@@ -441,15 +471,15 @@ struct EmbBwdArgs {
 
 constexpr int kBwdSlot = kNetBytes;  // the whole net block (forward and transposed images)
 
-// Backward epilogue 3 for one warpgroup's half of the columns: G (recomputed)
-// and the incoming dG = R . dX give dR (partial over this half), the skip
-// gradient dG -> shared (gsm row) and dZ3 = dG (1 - t3^2) -> the K = 128
-// A operand (bf16, chunk G0).
+// Backward epilogue 3 over one half of the D3 columns (G0 compile-time, so
+// that every register array is indexed statically): G (recomputed) and the
+// incoming dG = R . dX give dR, the skip gradient of dG into sk (the layer
+// 2 -> 3 skip: identity or [x, x]) and dZ3 = dG (1 - t3^2) -> the K = 128 A
+// operand (bf16, chunk G0).
 template <int N1, int N2, int N3, int G0>
 __device__ __forceinline__ void bepi3(uint32_t trow, const float* par, const float* t2,
-                                      const float* h1, bool live,
-                                      float4 R, const float* dx, float* grow, unsigned char* atile,
-                                      int r, float* dr) {
+                                      const float* h1, bool live, float4 R, const float* dx,
+                                      float* sk, unsigned char* atile, int r, float* dr) {
   unsigned char* chunk = atile + G0 * 16384;
 #pragma unroll
   for (int c16 = 0; c16 < 4; ++c16) {
@@ -478,10 +508,9 @@ __device__ __forceinline__ void bepi3(uint32_t trow, const float* par, const flo
           dr[1] = fmaf(gv, d1, dr[1]);
           dr[2] = fmaf(gv, d2, dr[2]);
           dr[3] = fmaf(gv, d3, dr[3]);
-          grow[m] = dg;
+          if (Skip<N2, N3>::kind == 1) sk[m] += dg;
+          if (Skip<N2, N3>::kind == 2) sk[m < N2 ? m : m - N2] += dg;
           z = dg * (1.f - t3 * t3);
-        } else if (m < N3) {
-          grow[m] = 0.f;
         }
         dz[k] = z;
       }
@@ -492,22 +521,19 @@ __device__ __forceinline__ void bepi3(uint32_t trow, const float* par, const flo
 }
 
 template <int N1, int N2, int N3>
-__global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbBwdArgs p) {
+__global__ void __launch_bounds__(128, 2) k_emb_bwd(const __grid_constant__ EmbBwdArgs p) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* slot = sm;                      // one staged net (all images)
   unsigned char* atile = sm + kBwdSlot;          // A operand, 2 chunks of 16 KiB
-  float* gsm = reinterpret_cast<float*>(atile + 32768);  // [128][kGStride] dG
-  float* rsm = gsm + kRows * kGStride;                   // [2][128][4] dR halves
-  float* dxsm = rsm + 2 * kRows * 4;                     // [2 atoms][4][128]
+  float* dxsm = reinterpret_cast<float*>(atile + 32768);  // [2 atoms][4][128]
   uint64_t* bar = reinterpret_cast<uint64_t*>(dxsm + 2 * 4 * 128);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   int* cached = reinterpret_cast<int*>(tslot + 1);
 
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, g = warp >> 2;
-  const int r = q * 32 + lane;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int r = tid;  // this thread's tile row = TMEM lane
 
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -524,7 +550,7 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
   unsigned phase = 0;
   bool alive = true;
 
@@ -544,12 +570,12 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
       if (cached[0] != net) {
         const uint4* src = reinterpret_cast<const uint4*>(p.nets + (size_t)net * kNetBytes);
         uint4* dst = reinterpret_cast<uint4*>(slot);
-        for (int k = tid; k < kNetBytes / 16; k += 256) dst[k] = __ldg(src + k);
+        for (int k = tid; k < kNetBytes / 16; k += 128) dst[k] = __ldg(src + k);
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) cached[0] = net;
       }
-      for (int k = tid; k < 2 * 4 * 128; k += 256) {
+      for (int k = tid; k < 2 * 4 * 128; k += 128) {
         const int ah = k >> 9, c = (k >> 7) & 3, m = k & 127;
         float v = 0.f;
         if (ah < na && m < N3) v = p.dxs[((size_t)(ah ? at1 : at0) * 4 + c) * N3 + m];
@@ -574,10 +600,8 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
         float h1[N1];
 #pragma unroll
         for (int j = 0; j < N1; ++j) h1[j] = tanh_fast(fmaf(e.x, par[kParW1 + j], par[kParB1 + j]));
-        if (g == 0)
-          st_half<N1, 0>(atile, r, h1);
-        else
-          st_half<N1, 1>(atile, r, h1);
+        st_half<N1, 0>(atile, r, h1);
+        st_half<N1, 1>(atile, r, h1);
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -610,10 +634,8 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
           float h2[N2];
 #pragma unroll
           for (int j = 0; j < N2; ++j) h2[j] = t2[j] + Skip<N1, N2>::at(h1, j);
-          if (g == 0)
-            st_half<N2, 0>(atile, r, h2);
-          else
-            st_half<N2, 1>(atile, r, h2);
+          st_half<N2, 0>(atile, r, h2);
+          st_half<N2, 1>(atile, r, h2);
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -629,14 +651,14 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
         phase ^= 1u;
         if (!alive) break;
         tc_fence_after();
-        // ---- backward epilogue 3: dG, dR (this half), dZ3 -> A (K = 128)
+        // ---- backward epilogue 3: dG, dR, the skip gradient, dZ3 -> A (K = 128)
         float dr[4] = {0.f, 0.f, 0.f, 0.f};
+        float sk[N2];
+#pragma unroll
+        for (int j = 0; j < N2; ++j) sk[j] = 0.f;
         const float* dx = dxsm + a * 512;
-        if (g == 0)
-          bepi3<N1, N2, N3, 0>(trow, par, t2, h1, live, e, dx, gsm + r * kGStride, atile, r, dr);
-        else
-          bepi3<N1, N2, N3, 1>(trow, par, t2, h1, live, e, dx, gsm + r * kGStride, atile, r, dr);
-        reinterpret_cast<float4*>(rsm)[g * kRows + r] = make_float4(dr[0], dr[1], dr[2], dr[3]);
+        bepi3<N1, N2, N3, 0>(trow, par, t2, h1, live, e, dx, sk, atile, r, dr);
+        bepi3<N1, N2, N3, 1>(trow, par, t2, h1, live, e, dx, sk, atile, r, dr);
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -657,7 +679,6 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
         // ---- epilogue 4: dH2 = dZ3 W3 + skip(dG), dZ2 = dH2 (1 - t2^2)
         float sb1[N1];  // t2 becomes dZ2 in place
         {
-          const float* gr = gsm + r * kGStride;
           float dh2[N2];
 #pragma unroll
           for (int c16 = 0; c16 < (N2 + 15) / 16; ++c16) {
@@ -667,10 +688,7 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
             for (int k = 0; k < 16; ++k) {
               const int j = c16 * 16 + k;
               if (j < N2) {
-                float sk = 0.f;
-                if (Skip<N2, N3>::kind == 1) sk = gr[j];
-                if (Skip<N2, N3>::kind == 2) sk = gr[j] + gr[j + N2];
-                dh2[j] = v[k] + sk;
+                dh2[j] = v[k] + sk[j];
                 t2[j] = dh2[j] * (1.f - t2[j] * t2[j]);
               }
             }
@@ -685,10 +703,8 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
         }
         tc_fence_before();
         __syncthreads();  // MMA 4 done with A; every lane has read D4
-        if (g == 0)
-          st_half<N2, 0>(atile, r, t2);
-        else
-          st_half<N2, 1>(atile, r, t2);
+        st_half<N2, 0>(atile, r, t2);
+        st_half<N2, 1>(atile, r, t2);
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {  // dH1 (partial) = dZ2 W2
@@ -718,14 +734,11 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
             }
           }
         }
+        if (live)
+          *reinterpret_cast<float4*>(p.net + ((size_t)atom * p.nnei + slot_j) * 4) =
+              make_float4(ds + dr[0], dr[1], dr[2], dr[3]);
         tc_fence_before();
-        __syncthreads();  // dR halves are in shared memory
-        if (g == 0 && live) {
-          const float4 d0 = reinterpret_cast<const float4*>(rsm)[r];
-          const float4 d1 = reinterpret_cast<const float4*>(rsm)[kRows + r];
-          const float4 o = make_float4(ds + d0.x + d1.x, d0.y + d1.y, d0.z + d1.z, d0.w + d1.w);
-          *reinterpret_cast<float4*>(p.net + ((size_t)atom * p.nnei + slot_j) * 4) = o;
-        }
+        __syncthreads();  // every lane has read D5 before the next tile
       }
     }
   }
@@ -735,38 +748,64 @@ __global__ void __launch_bounds__(256, 1) k_emb_bwd(const __grid_constant__ EmbB
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
 }
 
-constexpr size_t kBwdSmem = 1024 + kBwdSlot + 32768 + (size_t)kRows * kGStride * 4 +
-                            2 * kRows * 4 * 4 + 2 * 4 * 128 * 4 + 64;
+// about 88 KiB: two CTAs per SM (2 x 256 TMEM columns)
+template <int N3>
+constexpr size_t bwd_smem() {
+  return 1024 + kBwdSlot + 32768 + 2 * 4 * 128 * 4 + 64;
+}
 
 template <int N1, int N2, int N3>
 int emb_bwd_launch(const EmbBwdArgs& a, cudaStream_t st) {
   auto kern = k_emb_bwd<N1, N2, N3>;
-  static const cudaError_t attr =
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+  constexpr size_t smem = bwd_smem<N3>();
+  static const cudaError_t attr = [&] {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    return e;
+  }();
   if (attr != cudaSuccess) return cuda_status(attr, "embed_bwd_tc attribute");
+  // two CTAs per SM: registers by __launch_bounds__(128, 2), shared memory
+  // below half an SM's
+  static_assert(2 * (smem + 1024) <= 228 * 1024, "two CTAs per SM");
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = std::max(1, std::min(sms, a.nunits));
-  kern<<<grid, 256, kBwdSmem, st>>>(a);
+  const int grid = std::max(1, std::min(2 * sms, a.nunits));
+  kern<<<grid, 128, smem, st>>>(a);
   GBDP_CHECK_LAUNCH("embed_bwd_tc");
   return GBDP_OK;
 }
 
-constexpr size_t kFwdSmem =
-    1024 + 2 * kSlot + 16384 + (size_t)kRows * kGStride * 4 + kRows * 4 * 4 + 2 * 4 * 128 * 4 + 64;
+// about 100 KiB for N3 = 100: two CTAs per SM (2 x 256 TMEM columns)
+template <int N3>
+constexpr size_t fwd_smem() {
+  return 1024 + kSlot + 16384 + (size_t)kRows * gstride<N3>() * 4 + kRows * 4 * 4 +
+         2 * 4 * 128 * 4 + 64;
+}
 
 template <int N1, int N2, int N3>
 int emb_fwd_launch(const EmbArgs& a, cudaStream_t st) {
   auto kern = k_emb_fwd<N1, N2, N3>;
-  static const cudaError_t attr =
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+  constexpr size_t smem = fwd_smem<N3>();
+  // the largest shared-memory carveout, so that two CTAs fit an SM
+  static const cudaError_t attr = [&] {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    return e;
+  }();
   if (attr != cudaSuccess) return cuda_status(attr, "embed_fwd_tc attribute");
+  // two CTAs per SM: registers by __launch_bounds__(128, 2), shared memory
+  // below half an SM's
+  static_assert(2 * (smem + 1024) <= 228 * 1024, "two CTAs per SM");
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = std::max(1, std::min(sms, a.nunits));
-  kern<<<grid, 256, kFwdSmem, st>>>(a);
+  const int grid = std::max(1, std::min(2 * sms, a.nunits));
+  kern<<<grid, 128, smem, st>>>(a);
   GBDP_CHECK_LAUNCH("embed_fwd_tc");
   return GBDP_OK;
 }
@@ -863,7 +902,7 @@ extern "C" int gbdp_embed_bwd_tc_bf16(float* net_deriv, float* dx_work, const fl
     set_error("embed_bwd_tc: embedding widths %d-%d-%d not built (25-50-100, 3-6-12)", n1, n2, n3);
     return GBDP_ERR_INVALID;
   }
-  const size_t shm = sizeof(float) * (size_t)(4 * n3 + n3 * axis);
+  const size_t shm = sizeof(float) * (size_t)(4 * n3 + n3 * axis + 4 * axis);
   GBDP_REQUIRE(shm <= 48 * 1024, "embed_bwd_tc: N3 * axis too large");
   k_emb_dx<<<nloc, 128, shm, st>>>(dx_work, dD, X, drow, n3, axis, 1.f / (float)nnei);
   GBDP_CHECK_LAUNCH("embed_dx");

@@ -220,7 +220,8 @@ def main():
                          "one GPU), torch GEMMs (fp32, split tf32x3, bf16) or the native call with a "
                          "cuBLAS compute type (native-*; native-bf16x9 is the default when "
                          "WORLD_SIZE > 1)")
-    ap.add_argument("--workload", default="water12k", choices=["water12k", "ragged512", "md786k"],
+    ap.add_argument("--workload", default="water12k",
+                    choices=["water12k", "ragged512", "md786k", "train8x192"],
                     help="water12k: the headline config; ragged512: 512 ragged frames, batched "
                          "fused graph vs the plain per-frame loop; md786k: 786,432-atom NVE MD")
     ap.add_argument("--md-steps", type=int, default=1000)
@@ -242,6 +243,8 @@ def main():
         return ragged_workload(args)
     if args.workload == "md786k":
         return md_workload(args)
+    if args.workload == "train8x192":
+        return train_workload(args)
 
     import torch
 
@@ -460,6 +463,72 @@ def _setup_models(dev, fit_mode):
         m64.tables_np if compressed else None, m64.infos_np if compressed else None,
         fit_mode=fit_mode)
     return se_a, cfg, m64, mk(True), mk(False)
+
+
+def train_workload(args):
+    """Training step: 8 seeded 192-atom water frames in one packed batch of
+    the compressed FP32 model, EnergyStdLoss (pref_e 0.02, pref_f 1000,
+    pref_v 0.02) through the force and virial (double backward: tabulate
+    grad-grad, prod_force_grad, prod_virial_grad) and its gradient wrt every
+    fitting parameter; the fitting GEMMs in FP32 and in BF16 (FP32
+    accumulation), the loss and gradients compared."""
+    import importlib
+
+    import torch
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dev = torch.device("cuda", 0)
+    se_a, cfg, m64, model, plain = _setup_models(dev, "fp32")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    frames = [water.water_frame(4, 12.42, SEED + k) for k in range(8)]
+    nat = sum(len(f[1]) for f in frames)
+    batch = model.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    coord = torch.tensor(np.concatenate([f[0] for f in frames]), dtype=torch.float32, device=dev)
+    E0, F0, V0 = se_a.Trainable(model).energy_force_virial(batch, coord)
+    gen = torch.Generator(device=dev).manual_seed(1)
+    E_ref = (E0 + 0.1 * torch.randn(E0.shape, generator=gen, device=dev)).detach()
+    F_ref = (F0 + 0.05 * torch.randn(F0.shape, generator=gen, device=dev)).detach()
+    V_ref = (V0 + 0.1 * torch.randn(V0.shape, generator=gen, device=dev)).detach()
+    res = {}
+    for gemm in ("fp32", "bf16"):
+        tr = se_a.Trainable(model, gemm)
+
+        def step():
+            E, F, V = tr.energy_force_virial(batch, coord)
+            L = se_a.energy_std_loss(E, F, V, E_ref, F_ref, V_ref, len(frames[0][1]))
+            return L, torch.autograd.grad(L, tr.params)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.record()
+        for _ in range(args.steps):
+            L, g = step()
+        en.record()
+        torch.cuda.synchronize()
+        res[gemm] = (st.elapsed_time(en) / args.steps, float(L.detach()),
+                     torch.cat([x.reshape(-1) for x in g]))
+    ms32, l32, g32 = res["fp32"]
+    ms16, l16, g16 = res["bf16"]
+    out = {"metric": "training atom-steps/s (force-loss step, double backward)",
+           "value": nat / (ms32 * 1e-3), "unit": "atom-steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded water frames, random-init "
+                                                     "weights, perturbed labels)",
+           "config": {"workload": "8 x 192-atom water frames (12.42 A boxes), compressed se_e2_a FP32, "
+                                  "EnergyStdLoss pref_e 0.02 / pref_f 1000 / pref_v 0.02, gradients wrt "
+                                  "the fitting parameters", "atoms": nat,
+                      "form": "operator form with autograd (eager)"},
+           "bf16_fitting_gemms": {
+               "value": nat / (ms16 * 1e-3), "ms_per_step": ms16,
+               "loss_rel_diff_vs_fp32": abs(l16 - l32) / abs(l32),
+               "grad_rel_l2_diff_vs_fp32": float((g16 - g32).norm() / g32.norm()),
+               "grad_cosine_vs_fp32": float((g16.double() @ g32.double())
+                                            / (g16.double().norm() * g32.double().norm())),
+               "grad_max_abs_diff_vs_fp32": float((g16 - g32).abs().max())}}
+    print(json.dumps(out))
+    return 0
 
 
 def ragged_workload(args):

@@ -428,24 +428,30 @@ __global__ void k_emb_dx(float* __restrict__ dxs, const float* __restrict__ dD,
                          float inv_nnei) {
   extern __shared__ float sh[];
   float* xs = sh;                // [4][N3]
-  float* dds = sh + 4 * N3;      // [N3][A]
-  float* t2 = dds + N3 * A;      // [4][A] second term
+  const int As = A + 1;          // odd row stride: threads over m hit distinct banks
+  float* dds = sh + 4 * N3;      // [N3][As]
+  float* t2 = dds + N3 * As;     // [4][A] second term
   const int atom = blockIdx.x;
   const size_t row = drow ? (size_t)drow[atom] : (size_t)atom;
   for (int k = threadIdx.x; k < 4 * N3; k += blockDim.x) xs[k] = X[(size_t)atom * 4 * N3 + k];
-  for (int k = threadIdx.x; k < N3 * A; k += blockDim.x) dds[k] = dD[row * N3 * A + k];
+  {  // warps over rows m, lanes over columns a: no division by A
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const float* src = dD + row * N3 * A;
+    for (int m = w; m < N3; m += nw)
+      for (int a = lane; a < A; a += 32) dds[m * As + a] = src[m * A + a];
+  }
   __syncthreads();
   for (int k = threadIdx.x; k < 4 * A; k += blockDim.x) {
     const int c = k / A, a = k - c * A;
     float o = 0.f;
-    for (int m2 = 0; m2 < N3; ++m2) o = fmaf(dds[m2 * A + a], xs[c * N3 + m2], o);
+    for (int m2 = 0; m2 < N3; ++m2) o = fmaf(dds[m2 * As + a], xs[c * N3 + m2], o);
     t2[k] = o;
   }
   __syncthreads();
   for (int m = threadIdx.x; m < N3; m += blockDim.x) {
     float o[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = 0; a < A; ++a) {
-      const float w = dds[m * A + a];
+      const float w = dds[m * As + a];
 #pragma unroll
       for (int c = 0; c < 4; ++c) o[c] = fmaf(w, xs[c * N3 + a], o[c]);
     }
@@ -902,7 +908,7 @@ extern "C" int gbdp_embed_bwd_tc_bf16(float* net_deriv, float* dx_work, const fl
     set_error("embed_bwd_tc: embedding widths %d-%d-%d not built (25-50-100, 3-6-12)", n1, n2, n3);
     return GBDP_ERR_INVALID;
   }
-  const size_t shm = sizeof(float) * (size_t)(4 * n3 + n3 * axis + 4 * axis);
+  const size_t shm = sizeof(float) * (size_t)(4 * n3 + n3 * (axis + 1) + 4 * axis);
   GBDP_REQUIRE(shm <= 48 * 1024, "embed_bwd_tc: N3 * axis too large");
   k_emb_dx<<<nloc, 128, shm, st>>>(dx_work, dD, X, drow, n3, axis, 1.f / (float)nnei);
   GBDP_CHECK_LAUNCH("embed_dx");

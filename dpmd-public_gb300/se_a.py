@@ -549,9 +549,20 @@ def energy_std_loss(E, F, V, E_ref, F_ref, V_ref, natoms: int, pref_e=0.02, pref
 class Trainable:
     """Fitting-net parameters of a compressed model as autograd leaves, and
     a training forward that keeps the graph through the force (double
-    backward: tabulate grad-grad, prod_force_grad / prod_virial_grad)."""
+    backward: tabulate grad-grad, prod_force_grad / prod_virial_grad).
 
-    def __init__(self, model: SeAModel):
+    gemm: "fp32" runs the fitting GEMMs in the model's dtype; "bf16" casts
+    both operands of every fitting GEMM to BF16 (cuBLAS tensor-core GEMM,
+    FP32 accumulation, product rounded to BF16, then back to the model's
+    dtype), in the forward and in every backward order; the table path
+    stays in the model's dtype."""
+
+    GEMMS = ("fp32", "bf16")
+
+    def __init__(self, model: SeAModel, gemm: str = "fp32"):
+        if gemm not in self.GEMMS:
+            raise ValueError(f"gemm must be one of {self.GEMMS}")
+        self.gemm = gemm
         self.model = model
         self.params = []
         fit = []
@@ -569,6 +580,11 @@ class Trainable:
             fit.append((h, wf, bf))
         self.fit = fit
 
+    def _mm(self, a: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
+        if self.gemm == "bf16":
+            return torch.matmul(a.to(torch.bfloat16), w.to(torch.bfloat16)).to(a.dtype)
+        return a @ w
+
     def energy_force_virial(self, b: "Batch", coord, compressed: bool = True):
         m = self.model
         cfg = m.cfg
@@ -585,10 +601,10 @@ class Trainable:
             hidden, wf, bf = self.fit[t]
             h = D.index_select(0, idx)
             for w, bb, idt, skip in hidden:
-                tt = torch.tanh(h @ w + bb)
+                tt = torch.tanh(self._mm(h, w) + bb)
                 out = tt * idt if idt is not None else tt
                 h = out + h if skip == "same" else out
-            E_atom = E_atom.index_add(0, idx, (h @ wf + bf)[:, 0] + m.bias_atom_e[t])
+            E_atom = E_atom.index_add(0, idx, (self._mm(h, wf) + bf)[:, 0] + m.bias_atom_e[t])
         net = torch.autograd.grad(E_atom.sum(), em, create_graph=True)[0]
         from .ops import ProdForceFn, ProdVirialFn
 

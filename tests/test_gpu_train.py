@@ -83,3 +83,44 @@ def test_force_loss_gradient_double_backward(setup):
             p[idx] += h
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g) <= 1e-5 * max(1.0, abs(fd)), (pi, idx, fd, g)
+
+
+def test_bf16_fitting_gemms_training_step(gb):
+    """The training step on a batch of 8 seeded 192-atom frames (FP32 model)
+    with the fitting GEMMs in BF16 (FP32 accumulation, products rounded to
+    BF16) against FP32.  Stated BF16 tolerances: loss within 1e-3 relative;
+    the fitting-parameter gradient within 0.2 relative L2 and at cosine
+    similarity >= 0.99 (a force-loss gradient of perturbed labels is a small
+    residual, and every double-backward product is BF16-rounded; measured
+    values printed)."""
+    gb.load_library()
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    cfg = mdl.SeAConfig()
+    stat = [water.water_frame(4, 12.42, 2000 + s) for s in range(4)]
+    m64 = se_a.build_model(cfg, 17, stat, DEV, torch.float64)
+    m = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), DEV,
+                      torch.float32, m64.tables_np, m64.infos_np)
+    frames = [water.water_frame(4, 12.42, 40 + k) for k in range(8)]
+    batch = m.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    x = torch.tensor(np.concatenate([f[0] for f in frames]), dtype=torch.float32, device=DEV)
+    E0, F0, V0 = se_a.Trainable(m).energy_force_virial(batch, x)
+    gen = torch.Generator(device=DEV).manual_seed(3)
+    E_ref = (E0 + 0.1 * torch.randn(E0.shape, generator=gen, device=DEV)).detach()
+    F_ref = (F0 + 0.05 * torch.randn(F0.shape, generator=gen, device=DEV)).detach()
+    V_ref = (V0 + 0.1 * torch.randn(V0.shape, generator=gen, device=DEV)).detach()
+    out = {}
+    for gemm in ("fp32", "bf16"):
+        tr = se_a.Trainable(m, gemm)
+        E, F, V = tr.energy_force_virial(batch, x)
+        L = se_a.energy_std_loss(E, F, V, E_ref, F_ref, V_ref, 192)
+        g = torch.autograd.grad(L, tr.params)
+        out[gemm] = (float(L), torch.cat([t.reshape(-1) for t in g]))
+    dl = abs(out["bf16"][0] - out["fp32"][0]) / abs(out["fp32"][0])
+    g16, g32 = out["bf16"][1].double(), out["fp32"][1].double()
+    dg = float((g16 - g32).norm() / g32.norm())
+    cos = float(g16 @ g32 / (g16.norm() * g32.norm()))
+    print(f"BF16 fitting GEMMs: loss rel diff {dl:.3e}, gradient rel L2 diff {dg:.3e}, "
+          f"cosine {cos:.6f}")
+    assert dl <= 1e-3 and dg <= 0.2 and cos >= 0.99

@@ -265,6 +265,8 @@ def main():
     pkg.load_library()
     se_a = importlib.import_module("dpmd_public_gb300.se_a")
     mdl = importlib.import_module("dpmd_public_gb300.model")
+    L = importlib.import_module("dpmd_public_gb300._lib")
+    L.set_autotune(True)  # launch shapes tuned during the (untimed) warm-up
     cfg = mdl.SeAConfig()
     c, t, b = _frame()
     nat = len(t)
@@ -417,6 +419,7 @@ def main():
            "plain_tc": plain_tc,
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
            "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
+           "autotune": L.autotune_report(),
            "clocks": clk.summary()}
     if rank == 0:
         import oracle as O
@@ -454,6 +457,7 @@ def _setup_models(dev, fit_mode):
 
     pkg = load_package()
     pkg.load_library()
+    importlib.import_module("dpmd_public_gb300._lib").set_autotune(True)
     se_a = importlib.import_module("dpmd_public_gb300.se_a")
     mdl = importlib.import_module("dpmd_public_gb300.model")
     cfg = mdl.SeAConfig()
@@ -586,7 +590,8 @@ def ragged_workload(args):
                            "1.0 g/cm3, compressed FP32, one packed graph-captured step",
                "atoms": nat, "frames": 512, "fitting_gemm": args.fit_mode},
            "plain_per_frame": {"value": nat / (plain_ms * 1e-3), "ms_per_step": plain_ms},
-           "chosen_over_plain": plain_ms / fused_ms}
+           "chosen_over_plain": plain_ms / fused_ms,
+           "autotune": sys.modules["dpmd_public_gb300._lib"].autotune_report()}
     print(json.dumps(out))
     return 0
 
@@ -646,6 +651,7 @@ def md_workload(args):
                "atoms": nat, "fitting_gemm": args.fit_mode,
                "model": f"random weights, fitting output layer x {args.md_out_scale}"},
            "energy_drift_eV_per_atom_per_ps": drift,
+           "autotune": sys.modules["dpmd_public_gb300._lib"].autotune_report(),
            "trace": [{"step": s_, "etot_eV": e_, "T_K": T_, "max_abs_F_eV_per_A": f_}
                      for s_, e_, T_, f_ in trace]}
     print(json.dumps(out))

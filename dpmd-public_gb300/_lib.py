@@ -82,6 +82,8 @@ _SIGS = {
     "gbdp_fitting_tc_workspace_bytes": (_Z, [_I]),
     "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
     "gbdp_fitting_tc_status": (_I, [_P, _I, _P]),
+    "gbdp_set_autotune": (None, [_I]),
+    "gbdp_autotune_report": (_I, [ctypes.c_char_p, _I]),
     "gbdp_embed_tc_net_bytes": (_Z, []),
     "gbdp_embed_fwd_tc_bf16": (_I, [_P] * 7 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
     "gbdp_embed_bwd_tc_bf16": (_I, [_P] * 8 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
@@ -155,3 +157,19 @@ def sfx(dtype) -> str:
     if dtype == torch.float32:
         return "f32"
     raise TypeError(f"unsupported dtype {dtype}; float32 and float64 only")
+
+
+def set_autotune(on: bool) -> None:
+    """Launch-shape autotuning of the fused descriptor kernels (off by
+    default): the first uncaptured call per shape times each choice."""
+    load().gbdp_set_autotune(1 if on else 0)
+
+
+def autotune_report() -> list[str]:
+    """One line per tuned shape key: kernel, dtype, sizes, the chosen warps
+    per CTA and the measured milliseconds of 1, 2 and 4 warps."""
+    lib = load()
+    n = lib.gbdp_autotune_report(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib.gbdp_autotune_report(buf, n + 1)
+    return [l for l in buf.value.decode().splitlines() if l]

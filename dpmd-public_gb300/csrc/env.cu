@@ -493,6 +493,48 @@ __device__ __forceinline__ void env_row_store(const T* xj, T xi, T yi, T zi, int
   }
 }
 
+// Ascending bitonic sort of 128 64-bit keys held by a warp, element
+// e * 32 + lane in v[e]: partners closer than 32 are in other lanes
+// (shuffles), farther ones in the same lane (register swaps).
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t x, int m) {
+  const uint32_t lo = __shfl_xor_sync(kFull, (uint32_t)x, m);
+  const uint32_t hi = __shfl_xor_sync(kFull, (uint32_t)(x >> 32), m);
+  return ((uint64_t)hi << 32) | lo;
+}
+
+__device__ __forceinline__ void warp_bitonic128(uint64_t* v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 128; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int je = j >> 5;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (e & je) continue;
+          const int i = e * 32 + lane;
+          const bool asc = (i & k) == 0;
+          const uint64_t a = v[e], b = v[e ^ je];
+          if ((a > b) == asc) {
+            v[e] = b;
+            v[e ^ je] = a;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = e * 32 + lane;
+          const bool asc = (i & k) == 0;
+          const bool lower = (lane & j) == 0;
+          const uint64_t o = shfl_xor64(v[e], j);
+          const uint64_t mn = o < v[e] ? o : v[e], mx = o < v[e] ? v[e] : o;
+          v[e] = (asc == lower) ? mn : mx;
+        }
+      }
+    }
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kEnvWarps * 32)
     k_nlist_env(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
@@ -564,6 +606,32 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   }
   for (int s = lane; s < nnei; s += 32) row[s] = -1;
   __syncwarp();
+  if (ncand <= 128) {
+    // ---- up to 128 candidates: a bitonic sort of (type, r^2, index) keys
+    //      in registers; a candidate's rank in its type is its sorted
+    //      position minus the number of candidates of lower types.
+    uint64_t v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int c = e * 32 + lane;
+      v[e] = c < ncand ? ((uint64_t)ctype[c] << 56) | ((keys[c] >> 8) & 0x00ffffffff000000ull) |
+                             (keys[c] & 0xffffffull)
+                       : ~0ull;
+    }
+    warp_bitonic128(v, lane);
+    int below = 0;  // candidates of types lower than the current one
+    for (int t = 0; t < si.ntypes; ++t) {
+      int cnt = 0;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const bool is_t = (int)(v[e] >> 56) == t;
+        const int pos = e * 32 + lane - below;
+        if (is_t && pos < si.sec[t + 1] - si.sec[t]) row[si.sec[t] + pos] = (int)(v[e] & 0xffffff);
+        cnt += __popc(__ballot_sync(kFull, is_t));
+      }
+      below += cnt;
+    }
+  } else {
   // ---- rank inside each type: position = number of same-type candidates
   //      with a smaller (r^2, index) key.  Each lane holds up to four of its
   //      candidates in registers and every key is read once per warp (a
@@ -590,6 +658,7 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
       if (t >= 0 && rank[e] < si.sec[t + 1] - si.sec[t])
         row[si.sec[t] + rank[e]] = (int)(uint32_t)(mk[e] & 0xffffffffu);
     }
+  }
   }
   __syncwarp();
 

@@ -39,6 +39,11 @@
 //             the reference's FPTYPE accumulation) and added to the frame's
 //             FP64 accumulator (9 atomics per atom).
 //   Padding slots carry no coordinate dependence and are skipped.
+#include <array>
+#include <atomic>
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 
 namespace gbdp {
@@ -234,8 +239,8 @@ __host__ __device__ constexpr size_t fwd_warp_bytes(int nnei, int mp) {
 // NQF: 32-wide output chunks handled lanes-over-k (the last may be partial);
 // tail_w (runtime, 0..16): outputs after them, handled tw = pow2 >= tail_w
 // lanes per neighbour, 32 / tw neighbours per instruction.
-template <typename T, int NQF>
-__global__ void __launch_bounds__(kFWarps * 32)
+template <typename T, int NQF, int W>
+__global__ void __launch_bounds__(W * 32)
     k_desc_fwd(T* __restrict__ X, T* __restrict__ D, T* __restrict__ D_lo,
                const T* __restrict__ em, const int* __restrict__ atype,
                const int* __restrict__ drow, TabSet<T> ts, int nloc, int nnei, int M, int tail_w,
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(kFWarps * 32)
   extern __shared__ __align__(32) unsigned char smem_raw[];
   constexpr int NA = NQF + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kFWarps + warp;
+  const int i = blockIdx.x * W + warp;
   if (i >= nloc) return;
   const int MP = (NQF + (tail_w > 0 ? 1 : 0)) * 32;
   unsigned char* wbase = smem_raw + (size_t)warp * fwd_warp_bytes<T>(nnei, MP);
@@ -460,8 +465,8 @@ __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
 // neighbours in flight per 16-lane group (measured on the 12,288-atom water
 // step: U = 1 at 7 CTAs per SM is faster than U = 2 at 6).
 constexpr int kBwdU = 1;
-template <typename T, int NQ, int NK, int U>
-__global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6) : 1)
+template <typename T, int NQ, int NK, int U, int W>
+__global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / W : 1)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
                const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
@@ -471,7 +476,7 @@ __global__ void __launch_bounds__(kBWarps * 32, sizeof(T) == 4 ? (U == 1 ? 7 : 6
   extern __shared__ __align__(32) unsigned char smem_raw[];
   constexpr int MP = NQ * 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kBWarps + warp;
+  const int i = blockIdx.x * W + warp;
   if (i >= nloc) return;
   const int ti = atype[i];
   if (ti < 0) return;
@@ -817,6 +822,93 @@ int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntype
   return GBDP_OK;
 }
 
+// ------------------------------------------------------------- autotune --
+// Warps per CTA of the fused descriptor kernels (1, 2 or 4 centre atoms per
+// CTA; per-warp shared memory, so only the launch shape changes): a small
+// batch fills more SMs with smaller CTAs.  With autotuning on
+// (gbdp_set_autotune), the first call for a shape key (kernel, dtype, M,
+// nnei, floor(log2 nloc)) that is not under stream capture times every
+// choice with CUDA events on the caller's stream (three runs each, the
+// minimum) and keeps the fastest; later calls with that key use it.  The
+// cache is the library's only mutable global state and sits behind a mutex.
+// Without a tuned entry the choice is 4 warps.
+enum { kTuneFwd = 0, kTuneBwd = 1 };
+constexpr int kTuneW[3] = {1, 2, 4};
+struct TuneEntry {
+  int w;
+  float ms[3];
+};
+std::mutex g_tune_mu;
+std::map<std::array<int, 5>, TuneEntry> g_tune;
+std::atomic<int> g_autotune{0};
+
+std::array<int, 5> tune_key(int kid, int tsize, int M, int nnei, int nloc) {
+  int lg = 0;
+  while (lg < 30 && (1 << (lg + 1)) <= nloc) ++lg;
+  return {kid, tsize, M, nnei, lg};
+}
+
+int tuned_warps(int kid, int tsize, int M, int nnei, int nloc, int dflt) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const auto it = g_tune.find(tune_key(kid, tsize, M, nnei, nloc));
+  return it == g_tune.end() ? dflt : it->second.w;
+}
+
+// run(w): one whole call with w warps per CTA (0: the tuned or default
+// choice), returning a status.  Tunes first when that is on and possible.
+template <typename F>
+int tune_run(int kid, int tsize, int M, int nnei, int nloc, cudaStream_t st, F&& run) {
+  if (g_autotune.load() && nloc > 0 && nnei > 0) {
+    const auto key = tune_key(kid, tsize, M, nnei, nloc);
+    bool have;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      have = g_tune.count(key) != 0;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (!have && cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusNone) {
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      TuneEntry te{4, {0.f, 0.f, 0.f}};
+      float best = 1e30f;
+      int rc = GBDP_OK;
+      for (int c = 0; c < 3 && rc == GBDP_OK; ++c) {
+        rc = run(kTuneW[c]);  // warm-up
+        float t = 1e30f;
+        for (int rep = 0; rep < 3 && rc == GBDP_OK; ++rep) {
+          cudaEventRecord(e0, st);
+          rc = run(kTuneW[c]);
+          cudaEventRecord(e1, st);
+          if (cudaEventSynchronize(e1) != cudaSuccess) rc = cuda_status(cudaGetLastError(), "autotune");
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          t = std::min(t, ms);
+        }
+        te.ms[c] = t;
+        if (t < best) {
+          best = t;
+          te.w = kTuneW[c];
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (rc != GBDP_OK) return rc;
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = te;
+    }
+  }
+  return run(0);
+}
+
+inline int sum_sel(const int* sel, int ntypes) {
+  int n = 0;
+  if (sel)
+    for (int t = 0; t < ntypes && t < kMaxTab; ++t) n += sel[t] > 0 ? sel[t] : 0;
+  return n;
+}
+
 template <typename T>
 int check_shapes(int M, int A, int nnei) {
   GBDP_REQUIRE(M >= kAxis && M <= 128, "se_a descriptor: neuron[-1] %d not in [%d,128]", M,
@@ -826,26 +918,56 @@ int check_shapes(int M, int A, int nnei) {
   return GBDP_OK;
 }
 
-template <typename T, int NQF>
-void launch_fwd(dim3 grid, size_t smem, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
+template <typename T, int NQF, int W>
+void launch_fwd(size_t warp_bytes, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
                 const int* atype, const int* drow, const TabSet<T>& ts, int nloc, int nnei, int M,
                 int tail_w, int tail_lg) {
-  auto kern = k_desc_fwd<T, NQF>;
+  auto kern = k_desc_fwd<T, NQF, W>;
+  const size_t smem = (size_t)W * warp_bytes;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  // the smallest shared-memory carveout that holds the resident CTAs (9 at
-  // 56 registers in FP32): the rest of the unified L1 caches table rows
-  const int per_sm = 9 * (int)(smem + 1024);
+  // the smallest shared-memory carveout that holds the resident CTAs (36
+  // warps at 56 registers in FP32): the rest of the unified L1 caches table
+  // rows
+  const int per_sm = (36 / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
-  kern<<<grid, kFWarps * 32, smem, st>>>(X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                                         tail_lg);
+  kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(X, D, D_lo, em, atype, drow, ts, nloc,
+                                                             nnei, M, tail_w, tail_lg);
+}
+
+template <typename T, int W>
+void fwd_dispatch(int nqf, size_t warp_bytes, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
+                  const int* atype, const int* drow, const TabSet<T>& ts, int nloc, int nnei,
+                  int M, int tail_w, int tail_lg) {
+  switch (nqf) {
+    case 0:
+      launch_fwd<T, 0, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                          tail_lg);
+      break;
+    case 1:
+      launch_fwd<T, 1, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                          tail_lg);
+      break;
+    case 2:
+      launch_fwd<T, 2, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                          tail_lg);
+      break;
+    case 3:
+      launch_fwd<T, 3, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                          tail_lg);
+      break;
+    default:
+      launch_fwd<T, 4, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                          tail_lg);
+      break;
+  }
 }
 
 template <typename T>
 int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
-             int nloc, int M, int A, cudaStream_t st) {
+             int nloc, int M, int A, cudaStream_t st, int w = 0) {
   TabSet<T> ts;
   int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side, M);
   if (rc) return rc;
@@ -858,58 +980,71 @@ int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow
                    (!D_lo || ((uintptr_t)D_lo & 15) == 0),
                "se_a descriptor fwd: em / D must be 16-byte aligned");
   // outputs past the last full 32-chunk: at most 16 of them run as a tail
-  const int w = M & 31;
-  const int nqf = (w == 0 || w > 16) ? (M + 31) / 32 : M / 32;
-  const int tail_w = (w == 0 || w > 16) ? 0 : w;
+  const int mr = M & 31;
+  const int nqf = (mr == 0 || mr > 16) ? (M + 31) / 32 : M / 32;
+  const int tail_w = (mr == 0 || mr > 16) ? 0 : mr;
   int tail_lg = 0;
   while ((1 << tail_lg) < tail_w) ++tail_lg;
   const int mp = (nqf + (tail_w > 0 ? 1 : 0)) * 32;
-  const size_t smem = (size_t)kFWarps * fwd_warp_bytes<T>(nnei, mp);
-  GBDP_REQUIRE(smem <= 200 * 1024, "se_a descriptor fwd: nnei %d needs %zu bytes of shared memory",
-               nnei, smem);
-  const dim3 grid((nloc + kFWarps - 1) / kFWarps);
-  switch (nqf) {
-    case 0:
-      launch_fwd<T, 0>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                       tail_lg);
-      break;
-    case 1:
-      launch_fwd<T, 1>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                       tail_lg);
-      break;
-    case 2:
-      launch_fwd<T, 2>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                       tail_lg);
-      break;
-    case 3:
-      launch_fwd<T, 3>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                       tail_lg);
-      break;
-    default:
-      launch_fwd<T, 4>(grid, smem, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                       tail_lg);
-      break;
-  }
+  const size_t wb = fwd_warp_bytes<T>(nnei, mp);
+  GBDP_REQUIRE((size_t)kFWarps * wb <= 200 * 1024,
+               "se_a descriptor fwd: nnei %d needs %zu bytes of shared memory", nnei,
+               (size_t)kFWarps * wb);
+  if (w == 0) w = tuned_warps(kTuneFwd, sizeof(T), M, nnei, nloc, kFWarps);
+  if (w == 1)
+    fwd_dispatch<T, 1>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
+  else if (w == 2)
+    fwd_dispatch<T, 2>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
+  else
+    fwd_dispatch<T, 4>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
   GBDP_CHECK_LAUNCH("se_a_descriptor_fwd");
   return GBDP_OK;
 }
 
-template <typename T, int NQ, int NK, int U>
-void launch_bwd(dim3 grid, size_t smem, cudaStream_t st, T* force, double* vir_acc, const T* X,
+template <typename T, int NQ, int NK, int U, int W>
+void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, const T* X,
                 const T* dD, const int* drow, const T* em, const int* nlist_ext,
                 const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
                 BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
-  auto kern = k_desc_bwd<T, NQ, NK, U>;
+  auto kern = k_desc_bwd<T, NQ, NK, U, W>;
+  const size_t smem = (size_t)W * warp_bytes;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  // the smallest shared-memory carveout that holds the resident CTAs: the
-  // rest of the unified L1 caches table rows
-  const int per_sm = 7 * (int)(smem + 1024);
+  // the smallest shared-memory carveout that holds the resident CTAs (28
+  // warps): the rest of the unified L1 caches table rows
+  const int per_sm = (28 / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
-  kern<<<grid, kBWarps * 32, smem, st>>>(force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
-                                         ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei,
-                                         M);
+  kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(
+      force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, inv_std, geo, ts,
+      rmin, rmax, nloc, nnei, M);
+}
+
+template <typename T, int W>
+void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc, const T* X,
+                  const T* dD, const int* drow, const T* em, const int* nlist_ext,
+                  const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
+                  BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
+#define GBDP_BWD_CASE(NKV)                                                                    \
+  case NKV:                                                                                   \
+    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU, W>(wb, st, force, vir_acc, X, dD, drow, em,     \
+                                                nlist_ext, ext_coord, ext_map, atype,       \
+                                                inv_std, geo, ts, rmin, rmax, nloc, nnei, M); \
+    break;
+  switch (nk) {
+    GBDP_BWD_CASE(1)
+    GBDP_BWD_CASE(2)
+    GBDP_BWD_CASE(3)
+    GBDP_BWD_CASE(4)
+    GBDP_BWD_CASE(5)
+    GBDP_BWD_CASE(6)
+    GBDP_BWD_CASE(7)
+    default:
+      launch_bwd<T, 4, 8, kBwdU, W>(wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+                                    ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+      break;
+  }
+#undef GBDP_BWD_CASE
 }
 
 template <typename T>
@@ -917,7 +1052,8 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
              const int* nlist_ext, const T* ext_coord, const int* ext_map, const int* atype,
              const T* inv_std, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
-             float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st) {
+             float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st,
+             int w = 0) {
   TabSet<T> ts;
   int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side, M);
   if (rc) return rc;
@@ -936,33 +1072,22 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
                "se_a descriptor bwd: em / dE_dD / inv_std must be 16-byte aligned");
   BwdGeom geo{atom_frame, frame_aoff, frame_eoff};
   const int nq = (M + 31) / 32;
-  const size_t smem = (size_t)kBWarps * bwd_warp_bytes<T>(nnei, nq * 32);
-  GBDP_REQUIRE(smem <= 200 * 1024, "se_a descriptor bwd: nnei %d needs %zu bytes of shared memory",
-               nnei, smem);
-  const dim3 grid((nloc + kBWarps - 1) / kBWarps);
+  const size_t wb = bwd_warp_bytes<T>(nnei, nq * 32);
+  GBDP_REQUIRE((size_t)kBWarps * wb <= 200 * 1024,
+               "se_a descriptor bwd: nnei %d needs %zu bytes of shared memory", nnei,
+               (size_t)kBWarps * wb);
   const T rmin = (T)rcut_smth, rmax = (T)rcut;
   const int nk = (M + 15) / 16;
-#define GBDP_BWD_CASE(NKV)                                                                       \
-  case NKV:                                                                                      \
-    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU>(grid, smem, st, force, vir_acc, X, dD, drow, em,   \
-                                             nlist_ext, ext_coord, ext_map, atype, inv_std, geo, \
-                                             ts, rmin, rmax, nloc, nnei, M);                     \
-    break;
-  switch (nk) {
-    GBDP_BWD_CASE(1)
-    GBDP_BWD_CASE(2)
-    GBDP_BWD_CASE(3)
-    GBDP_BWD_CASE(4)
-    GBDP_BWD_CASE(5)
-    GBDP_BWD_CASE(6)
-    GBDP_BWD_CASE(7)
-    default:
-      launch_bwd<T, 4, 8, kBwdU>(grid, smem, st, force, vir_acc, X, dD, drow, em, nlist_ext,
-                             ext_coord, ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei,
-                             M);
-      break;
-  }
-#undef GBDP_BWD_CASE
+  if (w == 0) w = tuned_warps(kTuneBwd, sizeof(T), M, nnei, nloc, kBWarps);
+  if (w == 1)
+    bwd_dispatch<T, 1>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+  else if (w == 2)
+    bwd_dispatch<T, 2>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+  else
+    bwd_dispatch<T, 4>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
   GBDP_CHECK_LAUNCH("se_a_descriptor_bwd");
   return GBDP_OK;
 }
@@ -1018,9 +1143,13 @@ extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow
       T* X, T* D, const T* em, const int* atype, const int* d_row, const T* const* tables,      \
       const T* table_infos, int ntypes, const int* sel, int type_one_side, int nloc,           \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
-    return desc_fwd<T>(X, D, nullptr, em, atype, d_row, tables, table_infos, ntypes, sel,       \
-                       type_one_side, nloc, last_layer_size, axis_neuron,                      \
-                       (cudaStream_t)stream);                                                   \
+    const cudaStream_t st = (cudaStream_t)stream;                                               \
+    return tune_run(kTuneFwd, (int)sizeof(T), last_layer_size, sum_sel(sel, ntypes), nloc, st,  \
+                    [&](int w) {                                                                \
+                      return desc_fwd<T>(X, D, nullptr, em, atype, d_row, tables, table_infos,  \
+                                         ntypes, sel, type_one_side, nloc, last_layer_size,     \
+                                         axis_neuron, st, w);                                   \
+                    });                                                                         \
   }                                                                                             \
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
       T* force, double* virial_acc, const T* X, const T* dE_dD, const int* d_row, const T* em, \
@@ -1029,10 +1158,15 @@ extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow
       const int* frame_ext_off, const T* const* tables, const T* table_infos, int ntypes,      \
       const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
       int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
-    return desc_bwd<T>(force, virial_acc, X, dE_dD, d_row, em, nlist_ext, ext_coord, ext_map,  \
-                       atype, inv_std, atom_frame, frame_atom_off, frame_ext_off, tables,      \
-                       table_infos, ntypes, sel, type_one_side, rcut_smth, rcut, nloc,         \
-                       nframes, last_layer_size, axis_neuron, (cudaStream_t)stream);           \
+    const cudaStream_t st = (cudaStream_t)stream;                                               \
+    return tune_run(kTuneBwd, (int)sizeof(T), last_layer_size, sum_sel(sel, ntypes), nloc, st,  \
+                    [&](int w) {                                                                \
+                      return desc_bwd<T>(force, virial_acc, X, dE_dD, d_row, em, nlist_ext,     \
+                                         ext_coord, ext_map, atype, inv_std, atom_frame,       \
+                                         frame_atom_off, frame_ext_off, tables, table_infos,   \
+                                         ntypes, sel, type_one_side, rcut_smth, rcut, nloc,    \
+                                         nframes, last_layer_size, axis_neuron, st, w);        \
+                    });                                                                         \
   }
 
 GBDP_FUSED_ENTRY(float, f32)
@@ -1043,7 +1177,33 @@ extern "C" int gbdp_se_a_descriptor_fwd_split_f32(
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
     int type_one_side, int nloc, int last_layer_size, int axis_neuron, gbdp_stream stream) {
   GBDP_REQUIRE(D_lo != nullptr, "se_a_descriptor_fwd_split: null D_lo");
-  return desc_fwd<float>(X, D_hi, D_lo, em, atype, d_row, tables, table_infos, ntypes, sel,
-                         type_one_side, nloc, last_layer_size, axis_neuron,
-                         (cudaStream_t)stream);
+  const cudaStream_t st = (cudaStream_t)stream;
+  return tune_run(kTuneFwd, 4, last_layer_size, sum_sel(sel, ntypes), nloc, st, [&](int w) {
+    return desc_fwd<float>(X, D_hi, D_lo, em, atype, d_row, tables, table_infos, ntypes, sel,
+                           type_one_side, nloc, last_layer_size, axis_neuron, st, w);
+  });
+}
+
+extern "C" void gbdp_set_autotune(int on) { g_autotune.store(on ? 1 : 0); }
+
+extern "C" int gbdp_autotune_report(char* buf, int len) {
+  std::string out;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto& kv : g_tune) {
+      char line[256];
+      const auto& k = kv.first;
+      const auto& e = kv.second;
+      snprintf(line, sizeof(line), "%s f%d M=%d nnei=%d nloc=2^%d warps=%d ms=%.4f,%.4f,%.4f\n",
+               k[0] == kTuneFwd ? "se_a_descriptor_fwd" : "se_a_descriptor_bwd", 8 * k[1], k[2],
+               k[3], k[4], e.w, e.ms[0], e.ms[1], e.ms[2]);
+      out += line;
+    }
+  }
+  if (buf && len > 0) {
+    const size_t n = std::min((size_t)len - 1, out.size());
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+  }
+  return (int)out.size();
 }

@@ -431,6 +431,20 @@ GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, cons
  * run on this workspace (GBDP_OK or GBDP_STATUS_TIMEOUT). */
 GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream);
 
+/* ---- launch-shape autotuning ----------------------------------------------
+ * The fused descriptor kernels (the gbdp_se_a_descriptor_ fwd and bwd entry
+ * points) run 1, 2 or 4 centre atoms per CTA.  With autotuning on, the first
+ * call for a shape key
+ * (kernel, dtype, last_layer_size, nnei, floor(log2 nloc)) that is not under
+ * stream capture times every choice on the caller's stream (it synchronises
+ * that stream) and keeps the fastest in a mutex-guarded cache; later calls
+ * with that key, captured or not, use it.  Off by default (4 per CTA).
+ * No reference counterpart.  gbdp_autotune_report writes one line per tuned
+ * key into buf (NUL-terminated, at most len bytes) and returns the full
+ * length. */
+GBDP_API void gbdp_set_autotune(int on);
+GBDP_API int gbdp_autotune_report(char* buf, int len);
+
 /* ---- uncompressed embedding net on the tensor cores (BF16) ----------------
  * Replaces the plain-form embedding of DescrptBlockSeA.forward
  * (deepmd/pt/model/descriptor/se_a.py:750-866; EmbeddingNet / MLPLayer,

@@ -196,3 +196,40 @@ def test_reference_model_testcase(mods, dtype, compressed, tol):
         assert np.abs(F.cpu().numpy() - g[f"case{n}_force"].reshape(-1, 3)).max() <= ft
         v_ref = g[f"case{n}_atomic_virial"].reshape(-1, 9).sum(0)
         assert np.abs(V[0].cpu().numpy() - v_ref).max() <= vt
+
+
+def test_autotuned_launch_shape(mods, built):
+    """Launch-shape autotuning of the fused descriptor kernels: the first
+    uncaptured call of a new shape times 1, 2 and 4 centres per CTA and keeps
+    the fastest; the step's results do not depend on the choice, and a CUDA
+    graph captured afterwards uses the tuned shape."""
+    L = __import__("dpmd_public_gb300._lib", fromlist=["x"])
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    frame = water.water_frame(3, 9.315, 21)  # 81 atoms: a shape no other test uses
+    b = m32.batch([frame[1]], frame[2][None])
+    coord = torch.tensor(frame[0], dtype=torch.float32, device=DEV)
+    E0, F0, V0 = (x.clone() for x in m32.step_fused(b, coord))
+    L.set_autotune(True)
+    try:
+        E1, F1, V1 = (x.clone() for x in m32.step_fused(b, coord))
+    finally:
+        L.set_autotune(False)
+    rep = L.autotune_report()
+    mine = [l for l in rep if "nloc=2^6" in l and "f32 M=100 nnei=138" in l]
+    assert {l.split()[0] for l in mine} == {"se_a_descriptor_fwd", "se_a_descriptor_bwd"}, rep
+    for l in mine:
+        assert int(l.split("warps=")[1].split()[0]) in (1, 2, 4)
+    assert torch.allclose(E1, E0, rtol=1e-6, atol=1e-6)
+    assert torch.allclose(F1, F0, rtol=1e-5, atol=1e-6)
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        m32.step_fused(b, coord)
+    torch.cuda.current_stream().wait_stream(s)
+    with torch.cuda.graph(g):
+        out = m32.step_fused(b, coord)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.allclose(out[1], F0, rtol=1e-5, atol=1e-6)

@@ -569,37 +569,65 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   const int c2 = c % g.ncell[2];
   const int n1 = g.ncell[1] + 2 * g.ngcell[1], n2 = g.ncell[2] + 2 * g.ngcell[2];
 
-  // ---- gather candidates from the stencil of extended cells
+  // ---- gather candidates from the stencil of extended cells: one lane per
+  //      stencil cell fetches its (start, count) in a single round trip, a
+  //      warp scan makes the cells one flat candidate range, and every pass
+  //      tests 32 candidates across cell boundaries (the owning cell found by
+  //      a binary search over the scan with shuffles)
   int ncand = 0;
-  for (int d0 = -g.stencil[0]; d0 <= g.stencil[0]; ++d0)
-    for (int d1 = -g.stencil[1]; d1 <= g.stencil[1]; ++d1)
-      for (int d2 = -g.stencil[2]; d2 <= g.stencil[2]; ++d2) {
-        const int e = g.ext_cell_off + ((c0 + g.ngcell[0] + d0) * n1 + (c1 + g.ngcell[1] + d1)) * n2 +
-                      (c2 + g.ngcell[2] + d2);
-        const int st = ext_start[e], cnt = ext_cnt[e];
-        for (int b = 0; b < cnt; b += 32) {
-          bool ok = false;
-          uint64_t key = 0;
-          int t = 0;
-          if (b + lane < cnt) {
-            const auto r = xs[st + b + lane];
-            const int pk = xs_packed(r);
-            const int idx = pk & 0xffffff;
-            t = (int)((unsigned)pk >> 24);
-            float k2;
-            ok = cand_test<T>(r, xi, yi, zi, rc2f, k2) && idx != il && t != 0xff &&
-                 t < si.ntypes;
-            key = ((uint64_t)__float_as_uint(k2) << 32) | (uint32_t)idx;
-          }
-          const unsigned m = __ballot_sync(kFull, ok);
-          const int pos = ncand + __popc(m & ((1u << lane) - 1u));
-          if (ok && pos < max_cand) {
-            keys[pos] = key;
-            ctype[pos] = (unsigned char)t;
-          }
-          ncand += __popc(m);
-        }
+  const int sy = 2 * g.stencil[1] + 1, sz = 2 * g.stencil[2] + 1;
+  const int nst = (2 * g.stencil[0] + 1) * sy * sz;
+  for (int cg = 0; cg < nst; cg += 32) {
+    const int q = cg + lane;
+    int st = 0, cnt = 0;
+    if (q < nst) {
+      const int d0 = q / (sy * sz) - g.stencil[0];
+      const int d1 = (q / sz) % sy - g.stencil[1];
+      const int d2 = q % sz - g.stencil[2];
+      const int e = g.ext_cell_off + ((c0 + g.ngcell[0] + d0) * n1 + (c1 + g.ngcell[1] + d1)) * n2 +
+                    (c2 + g.ngcell[2] + d2);
+      st = ext_start[e];
+      cnt = ext_cnt[e];
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    const int excl = incl - cnt;
+    for (int base = 0; base < total; base += 32) {
+      const int f = base + lane;
+      int L = 0;  // lanes whose cells end at or before f: the owner of f
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int v = __shfl_sync(kFull, incl, L + step - 1);
+        if (v <= f) L += step;
       }
+      L = min(L, 31);
+      const int stL = __shfl_sync(kFull, st, L), exL = __shfl_sync(kFull, excl, L);
+      bool ok = false;
+      uint64_t key = 0;
+      int t = 0;
+      if (f < total) {
+        const auto r = xs[stL + (f - exL)];
+        const int pk = xs_packed(r);
+        const int idx = pk & 0xffffff;
+        t = (int)((unsigned)pk >> 24);
+        float k2;
+        ok = cand_test<T>(r, xi, yi, zi, rc2f, k2) && idx != il && t != 0xff && t < si.ntypes;
+        key = ((uint64_t)__float_as_uint(k2) << 32) | (uint32_t)idx;
+      }
+      const unsigned m = __ballot_sync(kFull, ok);
+      const int pos = ncand + __popc(m & ((1u << lane) - 1u));
+      if (ok && pos < max_cand) {
+        keys[pos] = key;
+        ctype[pos] = (unsigned char)t;
+      }
+      ncand += __popc(m);
+    }
+  }
   if (ncand > max_cand) {
     if (lane == 0) raise_status(status, GBDP_STATUS_CAND_OVERFLOW);
     ncand = max_cand;

@@ -424,64 +424,72 @@ __device__ __forceinline__ void store4<double>(double* p, double a, double b, do
   *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
 }
 
+// a / b: the fast reciprocal-multiply division in FP32 (2 ulp), IEEE in FP64
+__device__ __forceinline__ float div_t(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double div_t(double a, double b) { return a / b; }
+
 // Env row of one slot (env_mat.cc:122-226: s(r) [1/r, x/r^2, y/r^2, z/r^2]
 // and its derivative wrt r_ij), normalised by the centre type's davg/dstd
 // (prod_env_mat.cc:84-100), stored at row o; xj == nullptr: the padding row
-// (0 - avg) / std; centre type < 0: zeros.
+// (0 - avg) / std; centre type < 0: zeros.  1/r and x/r^2 are formed from
+// 1/sqrt(r^2) and the normalisation divides with div_t (within two ulp of
+// the reference's divisions in FP32); the derivative row is formed only when
+// em_deriv is requested.
 template <typename T>
 __device__ __forceinline__ void env_row_store(const T* xj, T xi, T yi, T zi, int ti,
                                               const T* av, const T* sd, int s, T rmin, T rmax,
                                               size_t o, T* em, T* em_deriv, T* rij) {
   T e[4] = {T(0), T(0), T(0), T(0)};
-  T dv[12];
-#pragma unroll
-  for (int q = 0; q < 12; ++q) dv[q] = T(0);
   T rr[3] = {T(0), T(0), T(0)};
+  T inr = T(0), inr2 = T(0), sw = T(0), dsw = T(0);
   if (xj) {
     rr[0] = xj[0] - xi;
     rr[1] = xj[1] - yi;
     rr[2] = xj[2] - zi;
     const T nr2 = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
-    const T inr = T(1) / sqrt(nr2);
+    inr = T(1) / sqrt(nr2);
     const T nr = nr2 * inr;
-    const T inr2 = inr * inr;
-    const T inr4 = inr2 * inr2;
-    const T inr3 = inr4 * nr;
-    T sw, dsw;
+    inr2 = inr * inr;
     spline5<T>(sw, dsw, nr, rmin, rmax);
-    e[0] = T(1) / nr;
-    e[1] = rr[0] / nr2;
-    e[2] = rr[1] / nr2;
-    e[3] = rr[2] / nr2;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) dv[d] = rr[d] * inr3 * sw - e[0] * dsw * rr[d] * inr;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        T t = T(2) * rr[a] * rr[d] * inr4;
-        if (a == d) t -= inr2;
-        dv[3 + a * 3 + d] = t * sw - e[1 + a] * dsw * rr[d] * inr;
-      }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) e[q] *= sw;
+    e[0] = inr;
+    e[1] = rr[0] * inr2;
+    e[2] = rr[1] * inr2;
+    e[3] = rr[2] * inr2;
   }
   T out[4];
   if (ti >= 0) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) out[q] = (e[q] - av[s * 4 + q]) / sd[s * 4 + q];
+    for (int q = 0; q < 4; ++q) out[q] = div_t(e[q] * sw - av[s * 4 + q], sd[s * 4 + q]);
   } else {
 #pragma unroll
     for (int q = 0; q < 4; ++q) out[q] = T(0);
   }
   store4<T>(em + o * 4, out[0], out[1], out[2], out[3]);
   if (em_deriv) {
+    T dv[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) dv[q] = T(0);
+    if (xj) {
+      const T inr4 = inr2 * inr2;
+      const T inr3 = inr2 * inr;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dv[d] = rr[d] * inr3 * sw - e[0] * dsw * rr[d] * inr;
+#pragma unroll
+      for (int a2 = 0; a2 < 3; ++a2)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          T t = T(2) * rr[a2] * rr[d] * inr4;
+          if (a2 == d) t -= inr2;
+          dv[3 + a2 * 3 + d] = t * sw - e[1 + a2] * dsw * rr[d] * inr;
+        }
+    }
     T* dp = em_deriv + o * 12;
 #pragma unroll
     for (int q = 0; q < 12; q += 4) {
       if (ti >= 0)
-        store4<T>(dp + q, dv[q] / sd[s * 4 + q / 3], dv[q + 1] / sd[s * 4 + (q + 1) / 3],
-                  dv[q + 2] / sd[s * 4 + (q + 2) / 3], dv[q + 3] / sd[s * 4 + (q + 3) / 3]);
+        store4<T>(dp + q, div_t(dv[q], sd[s * 4 + q / 3]), div_t(dv[q + 1], sd[s * 4 + (q + 1) / 3]),
+                  div_t(dv[q + 2], sd[s * 4 + (q + 2) / 3]),
+                  div_t(dv[q + 3], sd[s * 4 + (q + 3) / 3]));
       else
         store4<T>(dp + q, T(0), T(0), T(0), T(0));
     }

@@ -688,9 +688,16 @@ class Batch:
             self.D_lo = torch.zeros((nr, M * A), dtype=dt, device=dev)
             tcb = int(model._lib.gbdp_fitting_tc_workspace_bytes(nr))
             self.tc_ws = torch.zeros(tcb, dtype=torch.uint8, device=dev)
-        self.force = torch.empty((n, 3), dtype=dt, device=dev)
-        self.vir = torch.empty((self.nframes, 9), dtype=torch.float64, device=dev)
-        self.energy = torch.empty((self.nframes,), dtype=torch.float64, device=dev)
+        # the step's outputs in one device buffer (energies and virials FP64,
+        # then forces), so that a caller reads them back with a single copy:
+        # `out` is that buffer, energy / vir / force are views into it
+        nf = self.nframes
+        esz = np.dtype(np.float64).itemsize
+        fbytes = n * 3 * torch.tensor([], dtype=dt).element_size()
+        self.out = torch.empty(nf * 10 * esz + fbytes, dtype=torch.uint8, device=dev)
+        self.energy = self.out[:nf * esz].view(torch.float64)
+        self.vir = self.out[nf * esz:nf * 10 * esz].view(torch.float64).view(nf, 9)
+        self.force = self.out[nf * 10 * esz:].view(dt).view(n, 3)
 
     def ensure_plain_tc(self, model: SeAModel):
         """Buffers of the tensor-core plain form (allocated once): atom pairs

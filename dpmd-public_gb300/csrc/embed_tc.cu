@@ -21,7 +21,7 @@
 //   MMA  D2 = A W2   (N 64, TMEM columns 0-63)
 //   epilogue 2       -> A (bf16), the layer-2 output in FP32 registers
 //   MMA  D3 = A W3   (N 128, TMEM columns 128-255)
-//   epilogue 3       -> G (FP32, shared), columns split between warpgroups
+//   epilogue 3       -> G (FP32, shared), every column of the thread's row
 //   G^T R            -> X of the two atoms (FP32, shared)
 #include <cuda_bf16.h>
 
@@ -157,8 +157,8 @@ __device__ __forceinline__ void st_piece(unsigned char* tile, int r, int u, cons
   *reinterpret_cast<uint4*>(tile + r * 128 + ((u ^ (r & 7)) << 4)) = w;
 }
 
-// One warpgroup's half (pieces 4 G0 .. 4 G0 + 3, columns 32 G0 .. 32 G0 + 31)
-// of a tile row from the NV activations h (zero beyond NV); G0 is
+// Half G0 (pieces 4 G0 .. 4 G0 + 3, columns 32 G0 .. 32 G0 + 31) of a tile
+// row from the NV activations h (zero beyond NV); G0 is
 // compile-time so that h is indexed statically.
 template <int NV, int G0>
 __device__ __forceinline__ void st_half(unsigned char* tile, int r, const float* h) {
@@ -186,7 +186,7 @@ struct Skip {
   }
 };
 
-// Epilogue 3 for one warpgroup's half of the D3 columns (compile-time, so
+// Epilogue 3 for one half of the D3 columns (G0 compile-time, so
 // that the skip reads h2 with static register indices): G row -> grow.
 template <int N2, int N3, int G0>
 __device__ __forceinline__ void epi3(uint32_t trow, const float* par, const float* h2, bool live,
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(128, 2) k_emb_fwd(const __grid_constant__ EmbA
         float h1[N1];
 #pragma unroll
         for (int j = 0; j < N1; ++j) h1[j] = tanh_fast(fmaf(e.x, par[kParW1 + j], par[kParB1 + j]));
-        // A = h1 (bf16), this warpgroup's four 16-byte pieces of the row
+        // A = h1 (bf16), the row's eight 16-byte pieces
         st_half<N1, 0>(atile, r, h1);
         st_half<N1, 1>(atile, r, h1);
         fence_proxy_async_smem();
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(128, 2) k_emb_fwd(const __grid_constant__ EmbA
         phase ^= 1u;
         if (!alive) break;
         tc_fence_after();
-        // ---- epilogue 3: G = tanh(D3 + b3) + skip(h2), this half's columns
+        // ---- epilogue 3: G = tanh(D3 + b3) + skip(h2), both column halves
         epi3<N2, N3, 0>(trow, par, h2, live, gsm + r * kGStride);
         epi3<N2, N3, 1>(trow, par, h2, live, gsm + r * kGStride);
         tc_fence_before();

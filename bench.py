@@ -385,6 +385,32 @@ def main():
 
     opk = op_kernel_times(model, batch, coord, flush, peaks, reps=max(3, min(args.steps, 10)))
 
+    # ---- the same step with floating-point atomic sums (the FP32 default is
+    #      the deterministic fixed-point mode), graph-replayed
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            model.step_fused(batch, coord, deterministic=False)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    gdet = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gdet):
+        model.step_fused(batch, coord, deterministic=False)
+    for _ in range(3):
+        gdet.replay()
+    det_ts = []
+    for _ in range(max(3, min(args.steps, 10))):
+        flush()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        gdet.replay()
+        s1.record()
+        torch.cuda.synchronize()
+        det_ts.append(s0.elapsed_time(s1))
+    det_ms = statistics.median(det_ts)
+    del gdet
+
     # ---- plain (uncompressed) drop-in, eager, same frame
     mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
                        torch.float32)
@@ -404,7 +430,8 @@ def main():
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded water generator, random-init weights)",
-           "config": {"workload": WORKLOAD, "atoms": nat, "form": "fused compressed, CUDA graph",
+           "config": {"workload": WORKLOAD, "atoms": nat,
+                      "form": "fused compressed, CUDA graph, deterministic (fixed-point) sums",
                       "fitting_gemm": args.fit_mode,
                       "l2": L2Flush.DESC, "parallelism": f"replicas x{ws}",
                       "wall_s": wall},
@@ -414,6 +441,10 @@ def main():
            "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                      "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
            "plain_tc": plain_tc,
+           "atomic_sums": {"value": ws * nat / (det_ms * 1e-3), "ms_per_step": det_ms,
+                           "form": "the fused step with floating-point atomic force / virial / "
+                                   "energy sums instead of the default fixed-point (bitwise "
+                                   "reproducible) sums, CUDA graph"},
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
            "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
            "autotune": L.autotune_report(),
@@ -780,7 +811,8 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
             P(b.force), P(b.vir), P(b.X), P(b.dD), P(b.drow), P(b.env.em), P(b.env.nlist_ext), P(b.env.ext_coord),
             P(b.env.ext_map), P(b.atype), P(model.dstd_inv), P(b.atom_frame), P(b.frame_aoff), P(b.frame_eoff),
             model._tab_ptrs, model._tab_infos, cfg.ntypes, model._sel_c, int(cfg.type_one_side),
-            ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), b.nloc, b.nframes, M, A, S())
+            ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), b.nloc, b.nframes, M, A,
+            P(b.force_fx()), S())
 
     parts = {"env_nlist": env, "desc_fwd": fwd, "fitting_gemm": fit, "desc_bwd": bwd}
     res = {}

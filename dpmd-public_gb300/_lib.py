@@ -73,8 +73,8 @@ _SIGS = {
                                                         ctypes.c_float, _P, _I, _P]),
     "gbdp_prod_env_mat_a_nlist_f64": (_I, [_P] * 10 + [_I, _I, _I, _I, ctypes.c_float,
                                                         ctypes.c_float, _P, _I, _P]),
-    "gbdp_frame_energy_f32": (_I, [_P, _P, _P, _I, _I, _P]),
-    "gbdp_frame_energy_f64": (_I, [_P, _P, _P, _I, _I, _P]),
+    "gbdp_frame_energy_f32": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "gbdp_frame_energy_f64": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "gbdp_table_planar_row_elems": (ctypes.c_size_t, [_I, _I]),
     "gbdp_table_to_planar_f32": (_I, [_P, _P, _I, _I, _P]),
     "gbdp_table_to_planar_f64": (_I, [_P, _P, _I, _I, _P]),
@@ -112,7 +112,7 @@ for _s in ("f32", "f64"):
         f"gbdp_prod_force_grad_a_{_s}": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
         f"gbdp_prod_virial_grad_a_{_s}": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _P]),
         f"gbdp_se_a_descriptor_fwd_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P]),
-        f"gbdp_se_a_descriptor_bwd_{_s}": (_I, [_P] * 16 + [_I, _P, _I, _F, _F, _I, _I, _I, _I, _P]),
+        f"gbdp_se_a_descriptor_bwd_{_s}": (_I, [_P] * 16 + [_I, _P, _I, _F, _F, _I, _I, _I, _I, _P, _P]),
     })
 
 _lib = None

@@ -72,6 +72,54 @@ __device__ __forceinline__ void scatter3(float* p, const float* v) {
   }
 }
 
+// ------------------------------------------------------ fixed-point sums --
+// Deterministic accumulation: a value v is added as the 64-bit integer
+// round(v * 2^s).  Integer addition is associative, so a total has the
+// same bits whatever order the additions arrive in; it is read back as
+// total * 2^-s.  Scaling by a power of two is exact, so the only rounding is
+// that of each term to the grid 2^-s.
+template <typename T>
+struct FxScale;
+template <>
+struct FxScale<float> {
+  static constexpr int force = 32;  // 2.3e-10 grid, |F| < 2^31
+  static constexpr int virial = 32;
+};
+template <>
+struct FxScale<double> {
+  static constexpr int force = 40;  // 9.1e-13 grid, |F| < 2^23
+  static constexpr int virial = 36;
+};
+constexpr int kFxEnergy = 30;  // 9.3e-10 grid, |E| per frame < 2^33
+
+// 2^s from its bit pattern (|s| well inside the exponent range)
+__host__ __device__ inline float pow2f(int s) {
+  union {
+    unsigned u;
+    float f;
+  } x{(unsigned)(127 + s) << 23};
+  return x.f;
+}
+__host__ __device__ inline double pow2d(int s) {
+  union {
+    unsigned long long u;
+    double d;
+  } x{(unsigned long long)(1023 + s) << 52};
+  return x.d;
+}
+__device__ __forceinline__ long long fx_of(float v, int s) { return __float2ll_rn(v * pow2f(s)); }
+__device__ __forceinline__ long long fx_of(double v, int s) { return __double2ll_rn(v * pow2d(s)); }
+template <typename T>
+__device__ __forceinline__ void fx_add(long long* p, T v, int s) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)fx_of(v, s));
+}
+template <typename T>
+__device__ __forceinline__ void fx_add3(long long* p, const T* v, int s) {
+  fx_add(p, v[0], s);
+  fx_add(p + 1, v[1], s);
+  fx_add(p + 2, v[2], s);
+}
+
 // Device-side error word: kernels record the first problem they hit and
 // return; the host reads the word after the stream is synchronised.
 __device__ __forceinline__ void raise_status(int* status, int code) {

@@ -467,7 +467,8 @@ __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
 constexpr int kBwdU = 1;
 template <typename T, int NQ, int NK, int U, int W>
 __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / W : 1)
-    k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc, const T* __restrict__ X,
+    k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc,
+               long long* __restrict__ force_fx, const T* __restrict__ X,
                const T* __restrict__ dD, const int* __restrict__ drow, const T* __restrict__ em,
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
                const int* __restrict__ ext_map, const int* __restrict__ atype,
@@ -720,7 +721,10 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
         v3[d] = acc;
       }
       const int jl = ext_map[eoff + je];
-      scatter3(force + (size_t)(aoff + jl) * 3, v3);
+      if (force_fx)
+        fx_add3(force_fx + (size_t)(aoff + jl) * 3, v3, FxScale<T>::force);
+      else
+        scatter3(force + (size_t)(aoff + jl) * 3, v3);
       ci[0] += v3[0];
       ci[1] += v3[1];
       ci[2] += v3[2];
@@ -735,12 +739,20 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
   ci[2] = warp_sum(ci[2]);
   if (lane == 0) {
     const T m[3] = {-ci[0], -ci[1], -ci[2]};
-    scatter3(force + (size_t)i * 3, m);
+    if (force_fx)
+      fx_add3(force_fx + (size_t)i * 3, m, FxScale<T>::force);
+    else
+      scatter3(force + (size_t)i * 3, m);
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     const T v = warp_sum(vir[q]);
-    if (lane == 0) atomicAdd(vir_acc + f * 9 + q, (double)v);
+    if (lane == 0) {
+      if (force_fx)  // the accumulator holds fixed-point sums in this mode
+        fx_add(reinterpret_cast<long long*>(vir_acc) + f * 9 + q, v, FxScale<T>::virial);
+      else
+        atomicAdd(vir_acc + f * 9 + q, (double)v);
+    }
   }
 }
 
@@ -749,9 +761,24 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
 // come in runs (rows are grouped by type, frames in order within a type),
 // so each warp adds one partial per run it sees: a handful of atomics per
 // warp instead of one per row.  Rows with frame -1 (padding) are skipped.
+// fixed-point totals -> values (out = acc * 2^-s)
+template <typename T>
+__global__ void k_fx_finish(T* __restrict__ out, const long long* __restrict__ acc, size_t n,
+                            int s) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = (T)((double)acc[k] * pow2d(-s));
+}
+// the same in place: the double buffer held the int64 totals
+__global__ void k_fx_finish_inplace(double* __restrict__ buf, size_t n, int s) {
+  for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+    const long long v = reinterpret_cast<const long long*>(buf)[k];
+    buf[k] = (double)v * pow2d(-s);
+  }
+}
+
 template <typename T>
 __global__ void k_frame_energy(double* __restrict__ E, const T* __restrict__ ae,
-                               const int* __restrict__ frame_of_row, int nrows) {
+                               const int* __restrict__ frame_of_row, int nrows, int det) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const int f = r < nrows ? frame_of_row[r] : -1;
@@ -763,20 +790,27 @@ __global__ void k_frame_energy(double* __restrict__ E, const T* __restrict__ ae,
     const bool mine = f == lf;
     const unsigned mk = __ballot_sync(kFull, mine);
     const double sum = warp_sum(mine ? v : 0.);
-    if (lane == leader) atomicAdd(E + lf, sum);
+    if (lane == leader) {
+      if (det)  // fixed point: the same bits whatever order the warps add in
+        fx_add(reinterpret_cast<long long*>(E) + lf, sum, kFxEnergy);
+      else
+        atomicAdd(E + lf, sum);
+    }
     todo &= ~mk;
   }
 }
 
 template <typename T>
 int frame_energy(double* E, const T* ae, const int* frame_of_row, int nrows, int nframes,
-                 cudaStream_t st) {
+                 int det, cudaStream_t st) {
   GBDP_REQUIRE(nrows >= 0 && nframes >= 1, "frame_energy: nrows %d, nframes %d", nrows, nframes);
   GBDP_REQUIRE(E != nullptr, "frame_energy: null E");
   cudaMemsetAsync(E, 0, sizeof(double) * (size_t)nframes, st);
   if (nrows == 0) return GBDP_OK;
   GBDP_REQUIRE(ae && frame_of_row, "frame_energy: null input");
-  k_frame_energy<T><<<(unsigned)((nrows + 255) / 256), 256, 0, st>>>(E, ae, frame_of_row, nrows);
+  k_frame_energy<T><<<(unsigned)((nrows + 255) / 256), 256, 0, st>>>(E, ae, frame_of_row, nrows,
+                                                                     det);
+  if (det) k_fx_finish_inplace<<<1, 256, 0, st>>>(E, (size_t)nframes, kFxEnergy);
   GBDP_CHECK_LAUNCH("frame_energy");
   return GBDP_OK;
 }
@@ -1002,7 +1036,8 @@ int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow
 }
 
 template <typename T, int NQ, int NK, int U, int W>
-void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, const T* X,
+void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, long long* force_fx,
+                const T* X,
                 const T* dD, const int* drow, const T* em, const int* nlist_ext,
                 const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
                 BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
@@ -1016,18 +1051,20 @@ void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, c
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
   kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(
-      force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, inv_std, geo, ts,
-      rmin, rmax, nloc, nnei, M);
+      force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, inv_std,
+      geo, ts, rmin, rmax, nloc, nnei, M);
 }
 
 template <typename T, int W>
-void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc, const T* X,
+void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc,
+                  long long* force_fx, const T* X,
                   const T* dD, const int* drow, const T* em, const int* nlist_ext,
                   const T* ext_coord, const int* ext_map, const int* atype, const T* inv_std,
                   BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
 #define GBDP_BWD_CASE(NKV)                                                                    \
   case NKV:                                                                                   \
-    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU, W>(wb, st, force, vir_acc, X, dD, drow, em,     \
+    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU, W>(wb, st, force, vir_acc, force_fx, X, dD, drow, \
+                                                em,                                         \
                                                 nlist_ext, ext_coord, ext_map, atype,       \
                                                 inv_std, geo, ts, rmin, rmax, nloc, nnei, M); \
     break;
@@ -1040,7 +1077,8 @@ void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc,
     GBDP_BWD_CASE(6)
     GBDP_BWD_CASE(7)
     default:
-      launch_bwd<T, 4, 8, kBwdU, W>(wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord,
+      launch_bwd<T, 4, 8, kBwdU, W>(wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext,
+                                    ext_coord,
                                     ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
       break;
   }
@@ -1053,7 +1091,7 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
              const T* inv_std, const int* atom_frame, const int* frame_aoff, const int* frame_eoff,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
              float rcut_smth, float rcut, int nloc, int nframes, int M, int A, cudaStream_t st,
-             int w = 0) {
+             long long* force_fx, int w = 0) {
   TabSet<T> ts;
   int rc = make_tabset(ts, tables, infos, ntypes, sel, one_side, M);
   if (rc) return rc;
@@ -1061,9 +1099,16 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
   const int nnei = ts.sec[ntypes];
   rc = check_shapes<T>(M, A, nnei);
   if (rc) return rc;
-  cudaMemsetAsync(force, 0, sizeof(T) * 3 * (size_t)nloc, st);
+  GBDP_REQUIRE(((uintptr_t)force_fx & 7) == 0, "se_a descriptor bwd: force_fx not 8-byte aligned");
+  if (force_fx)
+    cudaMemsetAsync(force_fx, 0, sizeof(long long) * 3 * (size_t)nloc, st);
+  else
+    cudaMemsetAsync(force, 0, sizeof(T) * 3 * (size_t)nloc, st);
   cudaMemsetAsync(vir_acc, 0, sizeof(double) * 9 * (size_t)nframes, st);
-  if (nloc == 0) return GBDP_OK;
+  if (nloc == 0) {
+    if (force_fx) cudaMemsetAsync(force, 0, sizeof(T) * 3 * (size_t)nloc, st);
+    return GBDP_OK;
+  }
   GBDP_REQUIRE(X && dD && em && nlist_ext && ext_coord && ext_map && atype && inv_std &&
                    atom_frame && frame_aoff && frame_eoff,
                "se_a descriptor bwd: null argument");
@@ -1080,14 +1125,20 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
   const int nk = (M + 15) / 16;
   if (w == 0) w = tuned_warps(kTuneBwd, sizeof(T), M, nnei, nloc, kBWarps);
   if (w == 1)
-    bwd_dispatch<T, 1>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+    bwd_dispatch<T, 1>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
                        atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
   else if (w == 2)
-    bwd_dispatch<T, 2>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+    bwd_dispatch<T, 2>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
                        atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
   else
-    bwd_dispatch<T, 4>(nk, wb, st, force, vir_acc, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
+    bwd_dispatch<T, 4>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
                        atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+  if (force_fx) {
+    const size_t nf = 3 * (size_t)nloc;
+    k_fx_finish<T><<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(force, force_fx, nf,
+                                                                 FxScale<T>::force);
+    k_fx_finish_inplace<<<1, 256, 0, st>>>(vir_acc, 9 * (size_t)nframes, FxScale<T>::virial);
+  }
   GBDP_CHECK_LAUNCH("se_a_descriptor_bwd");
   return GBDP_OK;
 }
@@ -1119,13 +1170,17 @@ extern "C" size_t gbdp_table_planar_row_elems(int last_layer_size, int elem_byte
 }
 
 extern "C" int gbdp_frame_energy_f32(double* E, const float* ae, const int* frame_of_row,
-                                     int nrows, int nframes, gbdp_stream stream) {
-  return frame_energy<float>(E, ae, frame_of_row, nrows, nframes, (cudaStream_t)stream);
+                                     int nrows, int nframes, int deterministic,
+                                     gbdp_stream stream) {
+  return frame_energy<float>(E, ae, frame_of_row, nrows, nframes, deterministic,
+                             (cudaStream_t)stream);
 }
 
 extern "C" int gbdp_frame_energy_f64(double* E, const double* ae, const int* frame_of_row,
-                                     int nrows, int nframes, gbdp_stream stream) {
-  return frame_energy<double>(E, ae, frame_of_row, nrows, nframes, (cudaStream_t)stream);
+                                     int nrows, int nframes, int deterministic,
+                                     gbdp_stream stream) {
+  return frame_energy<double>(E, ae, frame_of_row, nrows, nframes, deterministic,
+                              (cudaStream_t)stream);
 }
 
 extern "C" int gbdp_table_to_planar_f32(float* dst, const float* src, int nrow,
@@ -1157,7 +1212,7 @@ extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow
       const T* inv_std, const int* atom_frame, const int* frame_atom_off,                      \
       const int* frame_ext_off, const T* const* tables, const T* table_infos, int ntypes,      \
       const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc, int nframes,   \
-      int last_layer_size, int axis_neuron, gbdp_stream stream) {                               \
+      int last_layer_size, int axis_neuron, long long* force_fx, gbdp_stream stream) {          \
     const cudaStream_t st = (cudaStream_t)stream;                                               \
     return tune_run(kTuneBwd, (int)sizeof(T), last_layer_size, sum_sel(sel, ntypes), nloc, st,  \
                     [&](int w) {                                                                \
@@ -1165,7 +1220,8 @@ extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow
                                          ext_coord, ext_map, atype, inv_std, atom_frame,       \
                                          frame_atom_off, frame_ext_off, tables, table_infos,   \
                                          ntypes, sel, type_one_side, rcut_smth, rcut, nloc,    \
-                                         nframes, last_layer_size, axis_neuron, st, w);        \
+                                         nframes, last_layer_size, axis_neuron, st, force_fx,  \
+                                         w);                                                    \
                     });                                                                         \
   }
 

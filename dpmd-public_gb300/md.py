@@ -37,16 +37,20 @@ class NVE:
     """Graph-captured velocity-Verlet integrator for one packed batch."""
 
     def __init__(self, model, batch, coord: np.ndarray, vel: np.ndarray, atype: np.ndarray,
-                 dt: float = 0.5):
+                 dt: float = 0.5, deterministic: bool | None = None):
+        """deterministic: forces and energies summed in fixed point, so that a
+        trajectory is the same bits on every run (default: the model's
+        default, on for FP32)."""
         dev = model.device
         dt_t = model.dtype
         self.model, self.batch, self.dt = model, batch, dt
+        self.det = deterministic
         self.x = torch.tensor(coord, dtype=dt_t, device=dev)
         self.v = torch.tensor(vel, dtype=dt_t, device=dev)
         m = np.array([MASS[int(t)] for t in atype])
         self.minv = torch.tensor(ACC_UNIT / m, dtype=dt_t, device=dev)[:, None]
         self.mass = torch.tensor(m, dtype=torch.float64, device=dev)
-        E, F, V = model.step_fused(batch, self.x)
+        E, F, V = model.step_fused(batch, self.x, self.det)
         self.E, self.F, self.V = E, F, V
         self.graph = None
 
@@ -54,7 +58,7 @@ class NVE:
         h = 0.5 * self.dt
         self.v.add_(self.F * self.minv, alpha=h)
         self.x.add_(self.v, alpha=self.dt)
-        E, F, V = self.model.step_fused(self.batch, self.x)
+        E, F, V = self.model.step_fused(self.batch, self.x, self.det)
         self.v.add_(F * self.minv, alpha=h)
         return E, F, V
 
@@ -71,14 +75,14 @@ class NVE:
         torch.cuda.current_stream().wait_stream(s)
         self.x.copy_(x0)
         self.v.copy_(v0)
-        self.model.step_fused(self.batch, self.x)
+        self.model.step_fused(self.batch, self.x, self.det)
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.E, self.F, self.V = self._step()
         # capture ran nothing: restore the state before the first real step
         self.x.copy_(x0)
         self.v.copy_(v0)
-        self.model.step_fused(self.batch, self.x)
+        self.model.step_fused(self.batch, self.x, self.det)
 
     def run(self, nsteps: int):
         for _ in range(nsteps):

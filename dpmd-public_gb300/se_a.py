@@ -289,8 +289,16 @@ class SeAModel:
         return torch.addmm(bf, h, wf)[:, 0] + self.bias_atom_e[t]
 
     # ------------------------------------------------------- chosen form --
-    def step_fused(self, b: "Batch", coord: torch.Tensor):
-        """E [nframes] f64, F [nloc_total, 3], virial [nframes, 9] f64."""
+    def step_fused(self, b: "Batch", coord: torch.Tensor, deterministic: bool | None = None):
+        """E [nframes] f64, F [nloc_total, 3], virial [nframes, 9] f64.
+        deterministic: forces, virials and energies summed in 64-bit fixed
+        point, the same bits on every run (floating-point atomics otherwise).
+        Default: on for FP32 models (its 2^-32 eV/A grid is far below FP32
+        rounding, and the integer sums measured faster than the FP64
+        atomics of the frame virial), off for FP64 models (whose rounding is
+        finer than the 2^-40 grid)."""
+        if deterministic is None:
+            deterministic = self.dtype == torch.float32
         cfg = self.cfg
         if self.tables is None:
             raise RuntimeError("the fused form needs the compression tables")
@@ -318,10 +326,10 @@ class SeAModel:
             _ptr(b.atom_frame), _ptr(b.frame_aoff), _ptr(b.frame_eoff), self._tab_ptrs,
             self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side),
             ctypes.c_float(cfg.rcut_smth), ctypes.c_float(cfg.rcut), n, b.nframes, M, A,
-            _stream()), "se_a_descriptor_bwd")
+            _ptr(b.force_fx() if deterministic else None), _stream()), "se_a_descriptor_bwd")
         L.check(getattr(lib, f"gbdp_frame_energy_{self._sfx}")(
             _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes,
-            _stream()), "frame_energy")
+            int(deterministic), _stream()), "frame_energy")
         return b.energy, b.force, b.vir
 
     def fitting_tc(self, b: "Batch"):
@@ -412,7 +420,7 @@ class SeAModel:
                                          nnei, 0)
             virs.append(v.reshape(9))
         L.check(getattr(self._lib, f"gbdp_frame_energy_{self._sfx}")(
-            _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes,
+            _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes, 0,
             _stream()), "frame_energy")
         return b.energy, torch.cat(forces), torch.stack(virs).to(torch.float64)
 
@@ -730,6 +738,13 @@ class Batch:
         self.net_deriv = torch.empty((n, nnei, 4), dtype=dt, device=dev)
         self.dx_work = torch.empty((n, 4, cfg.neuron[-1]), dtype=dt, device=dev)
         self.emb_status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def force_fx(self) -> torch.Tensor:
+        """The fixed-point force accumulator of the deterministic fused step
+        (allocated once)."""
+        if not hasattr(self, "_force_fx"):
+            self._force_fx = torch.empty((self.nloc, 3), dtype=torch.int64, device=self.atype.device)
+        return self._force_fx
 
     def fit_ws(self, t: int, model: SeAModel):
         """Workspace of the native fitting call for type t (allocated once)."""

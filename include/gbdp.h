@@ -315,7 +315,12 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * frames) and virial_acc [nframes, 9] (double, zeroed here) get the
  * contributions of every real neighbour, the env-matrix derivative being
  * recomputed from ext_coord (prod_force.cc:22-72, prod_virial.cc:22-68
- * semantics); inv_std [ntypes, nnei * 4] is 1 / dstd.  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
+ * semantics); inv_std [ntypes, nnei * 4] is 1 / dstd.  force_fx (device,
+ * may be NULL): with it, every force and virial contribution is summed in
+ * 64-bit fixed point (forces on a grid of 2^-32 eV/A in FP32, 2^-40 in FP64;
+ * virials 2^-32 / 2^-36 eV) in force_fx [nloc, 3] and in virial_acc, then
+ * written as values, so that the results are the same bits on every run;
+ * without it the sums are floating-point atomics.  atom_frame [nloc], frame_atom_off / frame_ext_off [nframes]
  * are device arrays describing the packed batch (see gbdp_nbr_frame).
  * ---------------------------------------------------------------------- */
 /* The fused descriptor kernels read the tables of tabulate_fusion_se_a
@@ -349,7 +354,7 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f32(
     const float* inv_std, const int* atom_frame, const int* frame_atom_off, const int* frame_ext_off,
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
     int type_one_side, float rcut_smth, float rcut, int nloc, int nframes, int last_layer_size,
-    int axis_neuron, gbdp_stream stream);
+    int axis_neuron, long long* force_fx, gbdp_stream stream);
 GBDP_API int gbdp_se_a_descriptor_bwd_f64(
     double* force, double* virial_acc, const double* X, const double* dE_dD, const int* d_row,
     const double* em,
@@ -357,17 +362,19 @@ GBDP_API int gbdp_se_a_descriptor_bwd_f64(
     const double* inv_std, const int* atom_frame, const int* frame_atom_off,
     const int* frame_ext_off, const double* const* tables, const double* table_infos,
     int ntypes, const int* sel, int type_one_side, float rcut_smth, float rcut, int nloc,
-    int nframes, int last_layer_size, int axis_neuron, gbdp_stream stream);
+    int nframes, int last_layer_size, int axis_neuron, long long* force_fx, gbdp_stream stream);
 
 /* Frame energies of a packed batch: E [nframes] (FP64, zeroed here) = the
  * sum of the per-row energies ae [nrows] whose frame_of_row [nrows] is the
  * frame (rows with -1 are skipped).  Device pointers.  The energy reduction
  * of the reference's model output (atomic energies summed per frame in the
- * FP64 energy precision, deepmd/pt/model/model/transform_output.py:165,181). */
+ * FP64 energy precision, deepmd/pt/model/model/transform_output.py:165,181).
+ * deterministic != 0: the partial sums are added in 64-bit fixed point
+ * (grid 2^-30 eV), so that E is the same bits on every run. */
 GBDP_API int gbdp_frame_energy_f32(double* E, const float* ae, const int* frame_of_row, int nrows,
-                                   int nframes, gbdp_stream stream);
+                                   int nframes, int deterministic, gbdp_stream stream);
 GBDP_API int gbdp_frame_energy_f64(double* E, const double* ae, const int* frame_of_row,
-                                   int nrows, int nframes, gbdp_stream stream);
+                                   int nrows, int nframes, int deterministic, gbdp_stream stream);
 
 /* ------------------------------------------------------------------------
  * Fitting net of one atom type: per-atom energy e = H_L w_out + b_out and

@@ -233,3 +233,44 @@ def test_autotuned_launch_shape(mods, built):
     g.replay()
     torch.cuda.synchronize()
     assert torch.allclose(out[1], F0, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_fused_deterministic_mode(mods, built, dtype):
+    """step_fused(deterministic=True): forces, virials and energies summed in
+    64-bit fixed point are the same bits on every run (also across a CUDA
+    graph replay), agree with the atomic sums within the FP32 / FP64
+    rounding, and keep the stated tolerances against the FP64 composite."""
+    import composite
+
+    se_a, mdl, water = mods
+    cfg, m64, m32 = built
+    m = m64 if dtype == torch.float64 else m32
+    frame = water.water_frame(4, 12.42, 13)
+    b = m.batch([frame[1]], frame[2][None])
+    coord = torch.tensor(frame[0], dtype=dtype, device=DEV)
+    runs = [tuple(x.clone() for x in m.step_fused(b, coord, deterministic=True)) for _ in range(3)]
+    for r in runs[1:]:
+        for a, c in zip(r, runs[0]):
+            assert torch.equal(a, c)
+    Ea, Fa, Va = (x.clone() for x in m.step_fused(b, coord))
+    E, F, V = runs[0]
+    # fixed-point grid per term: 2^-40 eV/A (FP64), 2^-32 (FP32), ~100 terms per atom
+    ft = 1e-10 if dtype == torch.float64 else 1e-6
+    assert float((F - Fa).abs().max()) <= ft
+    assert float((E - Ea).abs().max()) <= 1e-8
+    assert float((V - Va).abs().max()) <= (1e-9 if dtype == torch.float64 else 1e-4)
+    _check(E[0].item(), F.cpu().numpy().astype(np.float64), V[0].cpu().numpy(),
+           _ref(composite, cfg, m64, frame), len(frame[1]), dtype)
+    # a graph captured in this mode replays the same bits
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        m.step_fused(b, coord, deterministic=True)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = m.step_fused(b, coord, deterministic=True)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out[1], F) and torch.equal(out[0], E) and torch.equal(out[2], V)

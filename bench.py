@@ -215,8 +215,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline")
     ap.add_argument("--fit-mode", default=None,
                     choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
-                             "native-bf16", "tc-tf32x3"],
-                    help="fitting net: tc-tf32x3 (tcgen05 kernel, TF32 hi/lo split; default on "
+                             "native-bf16", "tc-f16x3"],
+                    help="fitting net: tc-f16x3 (tcgen05 kernel, scaled FP16 hi/lo split; default on "
                          "one GPU), torch GEMMs (fp32, split tf32x3, bf16) or the native call with a "
                          "cuBLAS compute type (native-*; native-bf16x9 is the default when "
                          "WORLD_SIZE > 1)")
@@ -236,7 +236,7 @@ def main():
     if args.fit_mode is None:
         # the tensor-core fitting stages operands with TMA, which jobs on two or
         # more GPUs keep out of: replicas there take the cuBLAS BF16x9 fitting
-        args.fit_mode = "tc-tf32x3" if _dist()[0] == 1 else "native-bf16x9"
+        args.fit_mode = "tc-f16x3" if _dist()[0] == 1 else "native-bf16x9"
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "ragged512":
@@ -791,10 +791,10 @@ def kernel_times(model, batch, coord, flush, reps: int = 5):
 
     def fwd():
         if model._tc_nets is not None:
-            lib.gbdp_se_a_descriptor_fwd_split_f32(P(b.X), P(b.D), P(b.D_lo), P(b.env.em), P(b.atype),
-                                                   P(b.drow), model._tab_ptrs, model._tab_infos,
-                                                   cfg.ntypes, model._sel_c, int(cfg.type_one_side),
-                                                   b.nloc, M, A, S())
+            lib.gbdp_se_a_descriptor_fwd_split_f32(P(b.X), P(b.D), P(b.D_lo), P(b.D_rs), P(b.env.em),
+                                                   P(b.atype), P(b.drow), model._tab_ptrs,
+                                                   model._tab_infos, cfg.ntypes, model._sel_c,
+                                                   int(cfg.type_one_side), b.nloc, M, A, S())
         else:
             lib.gbdp_se_a_descriptor_fwd_f32(P(b.X), P(b.D), P(b.env.em), P(b.atype), P(b.drow),
                                              model._tab_ptrs, model._tab_infos, cfg.ntypes,
@@ -999,16 +999,16 @@ def _peaks():
 
 # algorithmic HBM bytes per local atom of each part (FP32, nnei 138, M 100,
 # A 16): inputs read once, outputs written once
-def _alg_bytes(name, cfg, fit_mode="tc-tf32x3"):
+def _alg_bytes(name, cfg, fit_mode="tc-f16x3"):
     nn, M, A = cfg.nnei, cfg.neuron[-1], cfg.axis_neuron
     f = 4
     if name == "env_nlist":
         # coord + type in; em, nlist (local + ext) out; ghosts ~0.9 x nloc x 16 B
         return 12 + 4 + nn * 4 * f + 2 * nn * 4 + 16
     if name == "desc_fwd":
-        # em in; X, D out (D as TF32 hi and lo for the tensor-core fitting)
-        nd = 2 if fit_mode == "tc-tf32x3" else 1
-        return nn * 4 * f + 4 * M * f + nd * M * A * f + 4
+        # em in; X, D out (D as FP16 hi and lo, 4 bytes an element with its
+        # row scale, for the tensor-core fitting)
+        return nn * 4 * f + 4 * M * f + M * A * f + 4 + (4 if fit_mode == "tc-f16x3" else 0)
     if name == "desc_bwd":
         # X, dE/dD, em, nlist_ext in; ~91 neighbour coords (L2) ; force out
         return 4 * M * f + M * A * f + nn * 4 * f + nn * 4 + 12
@@ -1038,7 +1038,7 @@ NCU_TRAFFIC = {"desc_bwd": 133.1e6, "desc_fwd": 144.6e6, "fitting_gemm": 63.6e6}
 def roofline(name, t, nat, cfg, peaks, fit_mode):
     ms = t["ms"]
     if name == "fitting_gemm":
-        tc = fit_mode == "tc-tf32x3"
+        tc = fit_mode == "tc-f16x3"
         nl = 6 if tc else 1
         flops = _fit_flops(cfg) * nat
         ach = flops / (ms * 1e-3) / 1e12
@@ -1049,9 +1049,9 @@ def roofline(name, t, nat, cfg, peaks, fit_mode):
                "peak_src": peaks["src"] + " (dense BF16, burst)",
                "alg_flops_per_launch": flops / nl, "launches": nl, "ms_per_launch": ms / nl}
         if tc:
-            # FP32 products as 3 TF32 MMAs at half the BF16 rate: 1/6 of peak
-            out["ceiling_tf32x3_tflops"] = peak / 6
-            out["frac_of_tf32x3_ceiling"] = ach / (peak / 6)
+            # FP32 products as 3 FP16 MMAs at the BF16 rate: 1/3 of peak
+            out["ceiling_f16x3_tflops"] = peak / 3
+            out["frac_of_f16x3_ceiling"] = ach / (peak / 3)
         return out
     alg = _alg_bytes(name, cfg, fit_mode) * nat
     ach = alg / (ms * 1e-3) / 1e9

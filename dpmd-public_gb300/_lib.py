@@ -78,14 +78,14 @@ _SIGS = {
     "gbdp_table_planar_row_elems": (ctypes.c_size_t, [_I, _I]),
     "gbdp_table_to_planar_f32": (_I, [_P, _P, _I, _I, _P]),
     "gbdp_table_to_planar_f64": (_I, [_P, _P, _I, _I, _P]),
-    "gbdp_se_a_descriptor_fwd_split_f32": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P]),
+    "gbdp_se_a_descriptor_fwd_split_f32": (_I, [_P] * 9 + [_I, _P, _I, _I, _I, _I, _P]),
     "gbdp_fitting_tc_workspace_bytes": (_Z, [_I]),
-    "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
+    "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
     "gbdp_fitting_tc_status": (_I, [_P, _I, _P]),
     "gbdp_set_autotune": (None, [_I]),
     "gbdp_autotune_report": (_I, [ctypes.c_char_p, _I]),
     "gbdp_embed_tc_net_bytes": (_Z, []),
-    "gbdp_embed_fwd_tc_bf16": (_I, [_P] * 7 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
+    "gbdp_embed_fwd_tc_bf16": (_I, [_P] * 8 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
     "gbdp_embed_bwd_tc_bf16": (_I, [_P] * 8 + [_I, _P, _I, _P] + [_I] * 7 + [_P, _P]),
 }
 
@@ -96,6 +96,9 @@ class FitTcNet(ctypes.Structure):
         ("w_lo", _P * 3),
         ("wt_hi", _P * 3),
         ("wt_lo", _P * 3),
+        ("cs_fwd", _P * 3),
+        ("cs_bwd", _P * 3),
+        ("act_scale", ctypes.c_float * 5),
         ("b", _P * 3),
         ("idt", _P * 3),
         ("w_out", _P),

@@ -1,6 +1,7 @@
 // Shared device/host helpers for the GB300 (sm_103a) se_e2_a kernels.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -236,6 +237,38 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase,
     if (mbar_try_wait(bar, phase)) return true;
   raise_status(status, GBDP_STATUS_TIMEOUT);
   return false;
+}
+
+// ------------------------------------------------ FP16 hi/lo operand split --
+// The tensor-core fitting takes each FP32 operand x as two FP16 parts under
+// a power-of-two scale 2^s: hi = fp16(x 2^s), lo = fp16(x 2^s - hi).  Both
+// parts carry 11 significant bits (as TF32 does), so hi + lo holds x to
+// about 2^-22 relative, and the scale, exact in both directions, factors
+// out of every dot product.  It brings a bound on the magnitudes of the
+// block it applies to below 2^15: no part can overflow FP16 (65504), and the
+// lo parts stay normal (>= 2^-14) for every x 2^s >= 2^-3.
+
+// 2^s with bound * 2^s < 2^15 (1 for a zero or non-finite bound)
+__device__ __forceinline__ float f16_scale_for(float bound) {
+  if (!(bound > 0.f) || bound > 3.0e38f) return 1.f;
+  int e;
+  frexpf(bound, &e);  // bound < 2^e
+  e = e < -100 ? -100 : e;
+  return ldexpf(1.f, 15 - e);
+}
+
+__device__ __forceinline__ void split_f16(float x, __half& hi, __half& lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
+}
+
+// four consecutive values of a scaled row, split: 8-byte stores of 4 halves
+__device__ __forceinline__ void st_split4_f16(__half* hi, __half* lo, const float* v, float sc) {
+  __align__(8) __half h[4], l[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) split_f16(v[c] * sc, h[c], l[c]);
+  *reinterpret_cast<uint2*>(hi) = *reinterpret_cast<const uint2*>(h);
+  *reinterpret_cast<uint2*>(lo) = *reinterpret_cast<const uint2*>(l);
 }
 
 }  // namespace gbdp

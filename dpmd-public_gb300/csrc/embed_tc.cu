@@ -56,8 +56,9 @@ constexpr int kMaxTypes = 8;
 
 struct EmbArgs {
   float* X;           // [nloc, 4, N3]
-  float* D;           // [rows, N3 * A]
-  float* D_lo;        // optional TF32 remainder of D
+  void* D;            // [rows, N3 * A]: FP32, or FP16 hi with D_lo
+  void* D_lo;         // optional FP16 lo part (split for the tensor-core fitting)
+  float* D_rs;        // with D_lo: [rows] inverse scale of each D row
   const int* drow;    // D row of each atom (null: the atom index)
   const float* em;    // [nloc, nnei, 4]
   const int* units;   // [nunits, 2] atom pairs of one centre type (-1: none)
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(128, 2) k_emb_fwd(const __grid_constant__ EmbA
   uint64_t* bar = reinterpret_cast<uint64_t*>(xacc + 2 * 4 * 128);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   int* cached = reinterpret_cast<int*>(tslot + 1);        // net index held by each slot
+  __shared__ float dred[8];                               // D-row bound: [warp][k, a] maxima
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int r = tid;                       // this thread's tile row = TMEM lane
@@ -382,28 +384,58 @@ __global__ void __launch_bounds__(128, 2) k_emb_fwd(const __grid_constant__ EmbA
     // ---- X and D of the unit's atoms
     for (int ah = 0; ah < na; ++ah) {
       const int m = tid;
+      const int atom = ah ? at1 : at0;
+      const size_t row = p.drow ? (size_t)p.drow[atom] : (size_t)atom;
+      float xm[4] = {0.f, 0.f, 0.f, 0.f};
       if (m < N3) {
-        const int atom = ah ? at1 : at0;
-        float xm[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           xm[c] = xacc[(ah * 4 + c) * 128 + m] * inv_nnei;
           p.X[((size_t)atom * 4 + c) * N3 + m] = xm[c];
         }
-        const size_t row = p.drow ? (size_t)p.drow[atom] : (size_t)atom;
-        float* d = p.D + row * (size_t)N3 * p.A + (size_t)m * p.A;
-        float* dl = p.D_lo ? p.D_lo + row * (size_t)N3 * p.A + (size_t)m * p.A : nullptr;
+      }
+      if (p.D_lo) {
+        // split for the tensor-core fitting: FP16 hi / lo of c D, c = 2^s
+        // from |D_ka| <= |X_k| |X_a| (Cauchy-Schwarz over the 4 rows of X)
+        const float q = xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2] + xm[3] * xm[3];
+        float qk = q, qa = m < p.A ? q : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          qk = fmaxf(qk, __shfl_xor_sync(kFull, qk, o));
+          qa = fmaxf(qa, __shfl_xor_sync(kFull, qa, o));
+        }
+        if ((tid & 31) == 0) {
+          dred[warp * 2] = qk;
+          dred[warp * 2 + 1] = qa;
+        }
+        __syncthreads();
+        qk = fmaxf(fmaxf(dred[0], dred[2]), fmaxf(dred[4], dred[6]));
+        qa = fmaxf(fmaxf(dred[1], dred[3]), fmaxf(dred[5], dred[7]));
+        __syncthreads();  // dred is reused by the next atom
+        const float sc = f16_scale_for(sqrtf(qk * qa) * 1.0001f);
+        if (m < N3) {
+          __half* dh = static_cast<__half*>(p.D) + row * (size_t)N3 * p.A + (size_t)m * p.A;
+          __half* dl = static_cast<__half*>(p.D_lo) + row * (size_t)N3 * p.A + (size_t)m * p.A;
+          for (int a2 = 0; a2 < p.A; a2 += 4) {
+            float v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              v[j] = 0.f;
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                v[j] = fmaf(xm[c], xacc[(ah * 4 + c) * 128 + a2 + j] * inv_nnei, v[j]);
+            }
+            st_split4_f16(dh + a2, dl + a2, v, sc);
+          }
+        }
+        if (tid == 0) p.D_rs[row] = 1.f / sc;
+      } else if (m < N3) {
+        float* d = static_cast<float*>(p.D) + row * (size_t)N3 * p.A + (size_t)m * p.A;
         for (int a2 = 0; a2 < p.A; ++a2) {
           float v = 0.f;
 #pragma unroll
           for (int c = 0; c < 4; ++c) v = fmaf(xm[c], xacc[(ah * 4 + c) * 128 + a2] * inv_nnei, v);
-          if (dl) {
-            const float h = __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
-            d[a2] = h;
-            dl[a2] = __uint_as_float((__float_as_uint(v - h) + 0x1000u) & 0xFFFFE000u);
-          } else {
-            d[a2] = v;
-          }
+          d[a2] = v;
         }
       }
     }
@@ -823,9 +855,9 @@ using namespace gbdp;
 
 extern "C" size_t gbdp_embed_tc_net_bytes(void) { return (size_t)kNetBytes; }
 
-extern "C" int gbdp_embed_fwd_tc_bf16(float* X, float* D, float* D_lo, const int* drow,
-                                      const float* em, const int* atype, const int* units,
-                                      int nunits, const void* nets, int ntypes,
+extern "C" int gbdp_embed_fwd_tc_bf16(float* X, void* D, void* D_lo, float* D_rscale,
+                                      const int* drow, const float* em, const int* atype,
+                                      const int* units, int nunits, const void* nets, int ntypes,
                                       const int* sel, int type_one_side, int nloc, int nnei,
                                       int n1, int n2, int n3, int axis, int* status,
                                       gbdp_stream stream) {
@@ -837,10 +869,15 @@ extern "C" int gbdp_embed_fwd_tc_bf16(float* X, float* D, float* D_lo, const int
                "embed_fwd_tc: null pointer");
   GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && ((uintptr_t)nets & 15) == 0,
                "embed_fwd_tc: em and nets must be 16-byte aligned");
+  GBDP_REQUIRE(!D_lo || (D_rscale && axis % 4 == 0 && ((uintptr_t)D & 7) == 0 &&
+                          ((uintptr_t)D_lo & 7) == 0),
+               "embed_fwd_tc: the split D needs D_rscale, axis_neuron %% 4 == 0 and 8-byte "
+               "aligned parts");
   EmbArgs a{};
   a.X = X;
   a.D = D;
   a.D_lo = D_lo;
+  a.D_rs = D_rscale;
   a.drow = drow;
   a.em = em;
   a.units = units;

@@ -1,10 +1,23 @@
 // Fitting nets on the 5th-generation tensor cores (sm_103a): tcgen05.mma
-// kind::tf32 with operands staged in shared memory by TMA and accumulators
+// kind::f16 with operands staged in shared memory by TMA and accumulators
 // in tensor memory.  FP32-level accuracy from a split: every FP32 operand x
-// is x_hi + x_lo, x_hi = x rounded to TF32 (10 explicit mantissa bits) and
-// x_lo = x - x_hi rounded to TF32 (|x - x_hi - x_lo| <= 2^-23 |x|), and
-// each product is A_hi B_hi + A_lo B_hi + A_hi B_lo (the A_lo B_lo term is
-// below FP32 rounding).  The tensor core's FP32 accumulator does not round
+// is taken under a power-of-two scale 2^s as x 2^s = x_hi + x_lo, x_hi =
+// fp16(x 2^s) and x_lo = fp16(x 2^s - x_hi), both with 11 significant bits
+// (|x 2^s - x_hi - x_lo| <= 2^-22 |x 2^s|), and each product is
+// A_hi B_hi + A_lo B_hi + A_hi B_lo (the A_lo B_lo term is below FP32
+// rounding).  FP16 holds as many significant bits as TF32 at twice its MMA
+// rate and half its bytes; its narrow exponent range is what the scales are
+// for.  They are exact powers of two that factor out of every dot product,
+// chosen so that a bound on each block's magnitudes maps below 2^15:
+//   D rows        per row, from |D_ka| <= |X_k| |X_a| (written by the
+//                 descriptor kernel with D, as the row's inverse scale)
+//   weights       per output column of each GEMM (host, once per model)
+//   H1, H2, GZ*   per layer and type, from bounds the host derives from the
+//                 parameters (|tanh| <= 1, 0 <= 1 - T^2 <= 1, row sums of
+//                 |W|); a layer's bound may be loose by a large factor
+//                 before any precision is lost.
+// The epilogue multiplies each accumulator by its column's (and for F1 its
+// row's) inverse scale.  The tensor core's FP32 accumulator does not round
 // to nearest on every addition, so long accumulation chains are kept
 // short: the A_hi B_hi products of k-block kb go to main accumulator
 // kb % 3, the two small cross terms to a fourth accumulator, and the
@@ -17,9 +30,9 @@
 // whole per-type fitting net (deepmd/pt/model/task/fitting.py:734-899,
 // layer semantics deepmd/dpmodel/utils/network.py) is six launches:
 //   F1  T1 = tanh(D W1 + b1)                    -> H1 = T1 (split)
-//   F2  T2 = tanh(H1 W2 + b2), H2 = T2 idt2 + H1 (split)
+//   F2  T2 = tanh(H1 W2 + b2), H2 = T2 idt2 + T1 (split)
 //   F3  T3 = tanh(H2 W3 + b3), H3 = T3 idt3 + H2, e += H3 w_out,
-//       GZ3 = w_out idt3 (1 - T3^2) (split)
+//       GZ3 = w_out idt3 (1 - T3^2) (split); H2 recomputed from T1, T2
 //   B3  G2 = GZ3 W3^T + w_out, GZ2 = G2 idt2 (1 - T2^2) (split)
 //   B2  G1 = GZ2 W2^T + G2,    GZ1 = G1 (1 - T1^2) (split)
 //   B1  dE/dD = GZ1 W1^T
@@ -36,8 +49,8 @@
 namespace gbdp {
 namespace {
 
-constexpr int TBM = 128, TBK = 32;
-constexpr int A_TILE = TBM * TBK * 4;  // 16 KiB
+constexpr int TBM = 128, TBK = 64;     // a k-block: 64 FP16 = one 128-byte swizzle row
+constexpr int A_TILE = TBM * TBK * 2;  // 16 KiB
 
 // Tile configurations.  The layers are too small to fill 152 SMs with wide
 // tiles, and a CTA's TMA -> MMA pipeline is latency-bound, so narrow tiles
@@ -53,7 +66,7 @@ constexpr int A_TILE = TBM * TBK * 4;  // 16 KiB
 template <int TBN_, int STAGES_, int NACC_>
 struct TcCfg {
   static constexpr int TBN = TBN_, STAGES = STAGES_, NACC = NACC_;
-  static constexpr int B_TILE = TBN * TBK * 4;
+  static constexpr int B_TILE = TBN * TBK * 2;
   static constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;
   static constexpr uint32_t ACC_COLS = TBN <= 128 ? 128 : 256;  // TMEM columns per accumulator
   static constexpr int TMEM_COLS = (NACC + 1) * (int)ACC_COLS;   // NACC main + 1 cross-term
@@ -69,25 +82,27 @@ constexpr int FIT_W = 240;                           // hidden width this kernel
 constexpr int FIT_D = 1600;                          // descriptor width this kernel serves
 
 struct TcMaps {
-  CUtensorMap a_hi, a_lo;
+  CUtensorMap a_hi, a_lo;   // FP16 [rows, K], boxes of 64 columns x 128 rows
   CUtensorMap b_hi[2], b_lo[2];
-  CUtensorMap in[2];   // per-row epilogue inputs, boxes of 16 columns x 32 rows
-  CUtensorMap out[3];  // epilogue outputs (o0, hi, lo), same boxes
+  CUtensorMap in[2];   // FP32 per-row epilogue inputs, boxes of 16 columns x 32 rows
+  CUtensorMap out[3];  // epilogue outputs: o0 (FP32), hi, lo (FP16), same boxes
 };
 
 // Epilogue staging per warp (in the pipeline buffers, free once the last
-// MMA has completed): two input chunks and two output chunks in flight,
-// each array chunk 32 rows x 16 floats (2 KiB, rows of 64 B, 64-byte TMA
+// MMA has completed): two input chunks and two output chunks in flight.
+// An FP32 chunk is 32 rows x 16 floats (2 KiB, rows of 64 B, 64-byte TMA
+// swizzle); an FP16 chunk 32 rows x 16 halves (1 KiB, rows of 32 B, 32-byte
 // swizzle).
-constexpr int EPI_CHUNK = 32 * 16;                          // floats per array chunk
-constexpr int EPI_IN_BYTES = 2 * 2 * EPI_CHUNK * 4;         // 8 KiB
-constexpr int EPI_WARP_BYTES = EPI_IN_BYTES + 2 * 3 * EPI_CHUNK * 4;  // 20 KiB
+constexpr int EPI_CHUNK = 32 * 16;                   // elements per array chunk
+constexpr int EPI_IN_BYTES = 2 * 2 * EPI_CHUNK * 4;  // 8 KiB
+constexpr int EPI_OUT_BUF = EPI_CHUNK * 4 + 2 * EPI_CHUNK * 2;  // o0 + hi + lo: 4 KiB
+constexpr int EPI_WARP_BYTES = EPI_IN_BYTES + 2 * EPI_OUT_BUF;  // 16 KiB
 
 enum { EPI_F1 = 0, EPI_F2, EPI_F3, EPI_B3, EPI_B2, EPI_B1 };
 
 // Per-row inputs and outputs of each epilogue kind (maps.in / maps.out):
-//   F1  out T1, H1 hi/lo        F2  in H1 hi/lo; out T2, H2 hi/lo
-//   F3  in H2 hi/lo; out GZ3 hi/lo (+ energy partials)
+//   F1  out T1, H1 hi/lo        F2  in T1; out T2, H2 hi/lo
+//   F3  in T1, T2; out GZ3 hi/lo (+ energy partials)
 //   B3  in T2; out G2, GZ2 hi/lo      B2  in T1, G2; out GZ1 hi/lo
 //   B1  out dE/dD
 struct TcEpi {
@@ -99,8 +114,12 @@ struct TcEpi {
   int out_mask;     // bit a: maps.out[a] is written
   const float* bias[2];
   const float* idt[2];
+  const float* idt2[2];   // F3: idt of layer 2 (H2 = T2 idt2 + T1)
   const float* wout[2];
-  float* epart;     // [rows, ntile_n] partial energies (F3)
+  const float* cscale[2]; // [N] inverse scale of each output column
+  const float* rscale;    // F1: [rows] inverse scale of each D row
+  float oscale[2];        // 2^s of the split output (hi / lo)
+  float* epart;           // [rows, ntile_n] partial energies (F3)
   int* status;
 };
 
@@ -149,11 +168,11 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                          uint32_t acc) {
+__device__ __forceinline__ void umma_f16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
@@ -186,14 +205,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
-// x rounded to TF32: to nearest, ties away from zero, on the magnitude bits
-__device__ __forceinline__ float rn_tf32(float x) {
-  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+// 16 scaled values split into FP16 hi / lo parts, two halves per word
+// (element 2j in the low half of word j)
+__device__ __forceinline__ void pack_split16(const float* x, uint32_t* hw, uint32_t* lw) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    __half h0, l0, h1, l1;
+    split_f16(x[2 * j], h0, l0);
+    split_f16(x[2 * j + 1], h1, l1);
+    hw[j] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
+    lw[j] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
+  }
 }
 
-__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  hi = rn_tf32(x);
-  lo = rn_tf32(x - hi);
+// One thread's row (16 halves as 8 words) of a [32 rows][32 B] staging
+// chunk in the TMA 32-byte swizzle: logical 16-byte piece q of row r sits at
+// piece q ^ ((r >> 2) & 1) (address bit 4 XOR bit 7; chunks 256-byte
+// aligned).
+__device__ __forceinline__ void row_st16h(__half* chunk, int lane, const uint32_t* w) {
+  const int sw = (lane >> 2) & 1;
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    *reinterpret_cast<uint4*>(chunk + lane * 16 + ((q ^ sw) << 3)) =
+        make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
 }
 
 // One thread's row (16 floats) of a [32 rows][64 B] staging chunk in the
@@ -312,9 +346,8 @@ __global__ void __launch_bounds__(128, 1)
       issued = kb + 1 > issued ? kb + 1 : issued;
     }
   } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer: D(f32) += A(tf32, K-major) B(tf32, K-major), M 128, N 80
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TBN >> 3) << 17) |
-                           ((uint32_t)(TBM >> 4) << 24);
+    // ---- MMA issuer: D(f32) += A(f16, K-major) B(f16, K-major), M 128, N 80
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(TBN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
     const uint32_t dsmall = tmem + (uint32_t)NACC * ACC_COLS;
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % TSTAGES;
@@ -325,13 +358,13 @@ __global__ void __launch_bounds__(128, 1)
                      bl = bh + B_TILE;
       const uint32_t dmain = tmem + (uint32_t)(kb % NACC) * ACC_COLS;
 #pragma unroll
-      for (int kk = 0; kk < TBK / 8; ++kk) {
-        const uint32_t off = kk * 32;  // 8 tf32 along K within the 128-byte row
+      for (int kk = 0; kk < TBK / 16; ++kk) {
+        const uint32_t off = kk * 32;  // 16 halves along K within the 128-byte row
         const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off),
                        dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
-        umma_tf32(dmain, dah, dbh, idesc, (kb >= NACC || kk > 0) ? 1u : 0u);
-        umma_tf32(dsmall, dal, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-        umma_tf32(dsmall, dah, dbl, idesc, 1u);
+        umma_f16(dmain, dah, dbh, idesc, (kb >= NACC || kk > 0) ? 1u : 0u);
+        umma_f16(dsmall, dal, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+        umma_f16(dsmall, dah, dbl, idesc, 1u);
       }
       umma_commit(&empty[s]);
     }
@@ -352,12 +385,15 @@ __global__ void __launch_bounds__(128, 1)
   if (got) {
     static_assert(4 * EPI_WARP_BYTES <= TSTAGES * STAGE, "epilogue staging exceeds the stage buffers");
     unsigned char* wsm = smem + warp * EPI_WARP_BYTES;
-    float* inb = reinterpret_cast<float*>(wsm);                  // [2 buf][2 arr][chunk]
-    float* outb = reinterpret_cast<float*>(wsm + EPI_IN_BYTES);  // [2 buf][3 arr][chunk]
+    float* inb = reinterpret_cast<float*>(wsm);  // [2 buf][2 arr][chunk]
+    unsigned char* outb = wsm + EPI_IN_BYTES;    // [2 buf][o0 | hi | lo]
     uint64_t* ib = inbar + warp * 2;
     const int yrow = row0 + warp * 32;
     const int nin = ep.nin;
     constexpr int NCH = TBN / 16;
+    // F1: the inverse scale of this thread's D row; the split output's scale
+    const float rsc = ep.kind == EPI_F1 ? __ldg(ep.rscale + yrow + lane) : 1.f;
+    const float osc = ep.oscale[t];
     int in_issued = nin > 0 ? 1 : 0, in_done = 0;  // input chunks issued / received
     if (lane == 0 && nin > 0) {
       mbar_expect_tx(&ib[0], nin * EPI_CHUNK * 4);
@@ -389,6 +425,11 @@ __global__ void __launch_bounds__(128, 1)
       tmem_ld16(ta + (uint32_t)NACC * ACC_COLS, w);
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] += w[k];
+      const int c = n0 + c0;
+      // undo the operand scales (powers of two: exact)
+      col_ld16(ep.cscale[t] + c, w);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] = v[k] * w[k] * rsc;
       float x0[16], x1[16];
       if (nin > 0) {
         if (!__all_sync(kFull, mbar_wait_bounded(&ib[buf], (unsigned)(ci >> 1) & 1u, ep.status)))
@@ -397,26 +438,29 @@ __global__ void __launch_bounds__(128, 1)
         row_ld16(inb + (buf * 2) * EPI_CHUNK, lane, x0);
         if (nin > 1) row_ld16(inb + (buf * 2 + 1) * EPI_CHUNK, lane, x1);
       }
-      const int c = n0 + c0;
-      float o0[16], hi[16], lo[16];
+      float o0[16], sv[16];  // sv: the next operand, scaled, to be split
       if (ep.kind == EPI_B1) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) o0[k] = v[k];
       } else if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
-        float bb[16], id[16], wo[16];
+        float bb[16], id[16], wo[16], i2[16];
         col_ld16(ep.bias[t] + c, bb);
         if (ep.kind != EPI_F1) col_ld16(ep.idt[t] + c, id);
-        if (ep.kind == EPI_F3) col_ld16(ep.wout[t] + c, wo);
+        if (ep.kind == EPI_F3) {
+          col_ld16(ep.wout[t] + c, wo);
+          col_ld16(ep.idt2[t] + c, i2);
+        }
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
           const float tt = tanhf(v[k] + bb[k]);
-          float h = tt;
-          if (ep.kind != EPI_F1) h = tt * id[k] + (x0[k] + x1[k]);
+          float h = tt;                                      // F1: H1 = T1
+          if (ep.kind == EPI_F2) h = tt * id[k] + x0[k];     // H2 = T2 idt2 + T1
           if (ep.kind == EPI_F3) {
+            h = tt * id[k] + (x1[k] * i2[k] + x0[k]);        // H3 = T3 idt3 + H2
             esum += h * wo[k];
-            split_tf32(wo[k] * id[k] * (1.f - tt * tt), hi[k], lo[k]);  // GZ3
+            sv[k] = wo[k] * id[k] * (1.f - tt * tt) * osc;  // GZ3
           } else {
-            split_tf32(h, hi[k], lo[k]);
+            sv[k] = h * osc;
           }
           o0[k] = tt;
         }
@@ -431,22 +475,27 @@ __global__ void __launch_bounds__(128, 1)
           const float g = v[k] + (ep.kind == EPI_B3 ? wo[k] : x1[k]);
           o0[k] = g;
           const float tt = x0[k];
-          const float gz = (ep.kind == EPI_B3 ? g * id[k] : g) * (1.f - tt * tt);
-          split_tf32(gz, hi[k], lo[k]);
+          sv[k] = (ep.kind == EPI_B3 ? g * id[k] : g) * (1.f - tt * tt) * osc;
         }
       }
+      uint32_t hw[8], lw[8];
+      if (ep.out_mask & 6) pack_split16(sv, hw, lw);
       // the output buffer was last used by the stores of chunk ci - 2
       if (lane == 0 && ci >= 2) bulk_wait_read1();
       __syncwarp();
-      float* ob = outb + buf * 3 * EPI_CHUNK;
-      if (ep.out_mask & 1) row_st16(ob, lane, o0);
-      if (ep.out_mask & 2) row_st16(ob + EPI_CHUNK, lane, hi);
-      if (ep.out_mask & 4) row_st16(ob + 2 * EPI_CHUNK, lane, lo);
+      unsigned char* ob = outb + buf * EPI_OUT_BUF;
+      float* o0b = reinterpret_cast<float*>(ob);
+      __half* hib = reinterpret_cast<__half*>(ob + EPI_CHUNK * 4);
+      __half* lob = hib + EPI_CHUNK;
+      if (ep.out_mask & 1) row_st16(o0b, lane, o0);
+      if (ep.out_mask & 2) row_st16h(hib, lane, hw);
+      if (ep.out_mask & 4) row_st16h(lob, lane, lw);
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) {
-        for (int a = 0; a < 3; ++a)
-          if (ep.out_mask & (1 << a)) tma_store_2d(&maps.out[a], c, yrow, ob + a * EPI_CHUNK);
+        if (ep.out_mask & 1) tma_store_2d(&maps.out[0], c, yrow, o0b);
+        if (ep.out_mask & 2) tma_store_2d(&maps.out[1], c, yrow, hib);
+        if (ep.out_mask & 4) tma_store_2d(&maps.out[2], c, yrow, lob);
         bulk_commit();
       }
     }
@@ -512,38 +561,44 @@ int get_encode() {
   return GBDP_OK;
 }
 
-// [rows, cols] fp32 row-major in boxes of box_x columns x box_y rows
-int make_map_box(CUtensorMap* m, const float* base, long rows, long cols, int box_x, int box_y,
-                 CUtensorMapSwizzle swz) {
+// [rows, cols] row-major FP32 (esz 4) or FP16 (esz 2) in boxes of box_x
+// columns x box_y rows
+int make_map_box(CUtensorMap* m, const void* base, int esz, long rows, long cols, int box_x,
+                 int box_y, CUtensorMapSwizzle swz) {
   GBDP_REQUIRE(base != nullptr && ((uintptr_t)base & 15) == 0,
                "fit_tc: operand null or not 16-byte aligned");
-  GBDP_REQUIRE((cols * 4) % 16 == 0, "fit_tc: row pitch not a multiple of 16 bytes");
+  GBDP_REQUIRE((cols * esz) % 16 == 0, "fit_tc: row pitch not a multiple of 16 bytes");
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * esz};
   cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
-                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = g_encode(m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                        2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   GBDP_REQUIRE(r == CUDA_SUCCESS, "fit_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
   return GBDP_OK;
 }
 
-// MMA operand: boxes of 32 columns (128 B) x box_rows rows, 128 B swizzle
-int make_map(CUtensorMap* m, const float* base, long rows, long cols, int box_rows) {
-  return make_map_box(m, base, rows, cols, TBK, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
+// MMA operand (FP16): boxes of 64 columns (128 B) x box_rows rows, 128 B swizzle
+int make_map(CUtensorMap* m, const void* base, long rows, long cols, int box_rows) {
+  return make_map_box(m, base, 2, rows, cols, TBK, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
-// epilogue row array: boxes of 16 columns x 32 rows (one warp's chunk),
-// 64-byte swizzle (matching row_st16 / row_ld16)
-int make_epi_map(CUtensorMap* m, const float* base, long rows, long cols) {
-  return make_map_box(m, base, rows, cols, 16, 32, CU_TENSOR_MAP_SWIZZLE_64B);
+// epilogue row array: boxes of 16 columns x 32 rows (one warp's chunk);
+// FP32 with the 64-byte swizzle of row_st16 / row_ld16, FP16 with the
+// 32-byte swizzle of row_st16h
+int make_epi_map(CUtensorMap* m, const void* base, int esz, long rows, long cols) {
+  return make_map_box(m, base, esz, rows, cols, 16, 32,
+                      esz == 4 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
 }
 
 size_t a256t(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// FP32 activations (t1, t2, g2), FP16 split operands (*h, *l)
 struct TcWs {
-  float *t1, *t2, *h1h, *h1l, *h2h, *h2l, *gz3h, *gz3l, *g2, *gz2h, *gz2l, *gz1h, *gz1l, *epart;
+  float *t1, *t2, *g2, *epart;
+  __half *h1h, *h1l, *h2h, *h2l, *gz3h, *gz3l, *gz2h, *gz2l, *gz1h, *gz1l;
   size_t bytes;
 };
 
@@ -552,25 +607,27 @@ TcWs carve_tc(void* base, long rows) {
   char* b = static_cast<char*>(base);
   size_t off = 0;
   auto take = [&](size_t n) {
-    float* r = b ? reinterpret_cast<float*>(b + off) : nullptr;
+    void* r = b ? static_cast<void*>(b + off) : nullptr;
     off += a256t(n);
     return r;
   };
-  const size_t act = sizeof(float) * (size_t)rows * FIT_W;
-  w.t1 = take(act);
-  w.t2 = take(act);
-  w.h1h = take(act);
-  w.h1l = take(act);
-  w.h2h = take(act);
-  w.h2l = take(act);
-  w.gz3h = take(act);
-  w.gz3l = take(act);
-  w.g2 = take(act);
-  w.gz2h = take(act);
-  w.gz2l = take(act);
-  w.gz1h = take(act);
-  w.gz1l = take(act);
-  w.epart = take(sizeof(float) * (size_t)rows * (FIT_W / 80));
+  const size_t act = (size_t)rows * FIT_W;
+  auto f32 = [&]() { return static_cast<float*>(take(sizeof(float) * act)); };
+  auto f16 = [&]() { return static_cast<__half*>(take(sizeof(__half) * act)); };
+  w.t1 = f32();
+  w.t2 = f32();
+  w.g2 = f32();
+  w.h1h = f16();
+  w.h1l = f16();
+  w.h2h = f16();
+  w.h2l = f16();
+  w.gz3h = f16();
+  w.gz3l = f16();
+  w.gz2h = f16();
+  w.gz2l = f16();
+  w.gz1h = f16();
+  w.gz1l = f16();
+  w.epart = static_cast<float*>(take(sizeof(float) * (size_t)rows * (FIT_W / 80)));
   w.bytes = off;
   return w;
 }
@@ -584,23 +641,29 @@ extern "C" size_t gbdp_fitting_tc_workspace_bytes(int rows) {
   return carve_tc(nullptr, rows).bytes + 256;
 }
 
-extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, const float* D_lo,
-                                   int ntypes, const int* nrows, const int* row_off,
-                                   const gbdp_fit_tc_net* nets, void* workspace,
-                                   size_t workspace_bytes, gbdp_stream stream) {
+extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, const void* D_lo,
+                                   const float* D_rscale, int ntypes, const int* nrows,
+                                   const int* row_off, const gbdp_fit_tc_net* nets,
+                                   void* workspace, size_t workspace_bytes, gbdp_stream stream) {
   GBDP_REQUIRE(ntypes >= 1 && ntypes <= 2, "fit_tc: ntypes %d (1 or 2 supported)", ntypes);
-  GBDP_REQUIRE(e && dE_dD && D_hi && D_lo && nrows && row_off && nets && workspace,
+  GBDP_REQUIRE(e && dE_dD && D_hi && D_lo && D_rscale && nrows && row_off && nets && workspace,
                "fit_tc: null argument");
   const long rows = row_off[ntypes];
   for (int t = 0; t < ntypes; ++t) {
     GBDP_REQUIRE(row_off[t] % TBM == 0 && row_off[t + 1] >= row_off[t] + nrows[t],
                  "fit_tc: type %d row block not 128-aligned or too small", t);
     const gbdp_fit_tc_net& n = nets[t];
-    for (int l = 0; l < 3; ++l)
+    for (int l = 0; l < 3; ++l) {
       GBDP_REQUIRE(n.wt_hi[l] && n.wt_lo[l] && n.w_hi[l] && n.w_lo[l] && n.b[l],
                    "fit_tc: type %d layer %d weights missing", t, l);
+      GBDP_REQUIRE(n.cs_fwd[l] && n.cs_bwd[l] && ((uintptr_t)n.cs_fwd[l] & 15) == 0 &&
+                       ((uintptr_t)n.cs_bwd[l] & 15) == 0,
+                   "fit_tc: type %d layer %d column scales missing or not 16-byte aligned", t, l);
+    }
     GBDP_REQUIRE(n.idt[1] && n.idt[2] && n.w_out, "fit_tc: type %d idt / output layer missing",
                  t);
+    for (int a = 0; a < 5; ++a)
+      GBDP_REQUIRE(n.act_scale[a] > 0.f, "fit_tc: type %d act_scale[%d] not positive", t, a);
   }
   GBDP_REQUIRE(rows % TBM == 0, "fit_tc: total rows %ld not a multiple of 128", rows);
   TcWs ws = carve_tc(workspace, rows);
@@ -625,6 +688,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
   base.ntile_n = FIT_W / CfgShortK::TBN;  // F3's N tiles
   for (int t = 0; t < ntypes; ++t) {
     base.wout[t] = nets[t].w_out;
+    base.idt2[t] = nets[t].idt[1];
     const float* cols[4] = {nets[t].w_out, nets[t].b[0], nets[t].b[1], nets[t].b[2]};
     for (const float* p : cols)
       GBDP_REQUIRE(((uintptr_t)p & 15) == 0, "fit_tc: bias / w_out not 16-byte aligned");
@@ -632,31 +696,33 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
                  "fit_tc: idt not 16-byte aligned");
   }
   enum { LONGK = 0, SHORTK };
+  // act: index into act_scale of the split output (-1: none)
   struct Step {
     int kind;
-    const float *a_hi, *a_lo;
+    const void *a_hi, *a_lo;
     int K, N, layer;
     bool fwd;
     const float* in[2];
-    float* out[3];
+    void* out[3];
+    int act;
     int cfg;
   };
   static_assert(FIT_W % CfgShortK::TBN == 0 && FIT_W % CfgLongK::TBN == 0 &&
                     FIT_D % CfgShortK::TBN == 0,
                 "tile widths must divide the layer widths");
   const Step steps[6] = {
-      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l},
+      {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}, 0,
        LONGK},
-      {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.h1h, ws.h1l}, {ws.t2, ws.h2h, ws.h2l},
-       SHORTK},
-      {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true, {ws.h2h, ws.h2l},
-       {nullptr, ws.gz3h, ws.gz3l}, SHORTK},
+      {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.t1, nullptr}, {ws.t2, ws.h2h, ws.h2l},
+       1, SHORTK},
+      {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true, {ws.t1, ws.t2},
+       {nullptr, ws.gz3h, ws.gz3l}, 2, SHORTK},
       {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false, {ws.t2, nullptr},
-       {ws.g2, ws.gz2h, ws.gz2l}, SHORTK},
+       {ws.g2, ws.gz2h, ws.gz2l}, 3, SHORTK},
       {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false, {ws.t1, ws.g2},
-       {nullptr, ws.gz1h, ws.gz1l}, SHORTK},
+       {nullptr, ws.gz1h, ws.gz1l}, 4, SHORTK},
       {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false, {nullptr, nullptr},
-       {dE_dD, nullptr, nullptr}, SHORTK}};
+       {dE_dD, nullptr, nullptr}, -1, SHORTK}};
   for (const Step& sp : steps) {
     TcMaps maps;
     memset(&maps, 0, sizeof(maps));
@@ -665,8 +731,8 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     for (int t = 0; t < 2 && !rc; ++t) {
       const gbdp_fit_tc_net& n = nets[t < ntypes ? t : 0];
       // forward B = W_l^T [out, in]; backward B = W_l [in, out]: both K-major
-      const float* bh = sp.fwd ? n.wt_hi[sp.layer] : n.w_hi[sp.layer];
-      const float* bl = sp.fwd ? n.wt_lo[sp.layer] : n.w_lo[sp.layer];
+      const void* bh = sp.fwd ? n.wt_hi[sp.layer] : n.w_hi[sp.layer];
+      const void* bl = sp.fwd ? n.wt_lo[sp.layer] : n.w_lo[sp.layer];
       const int tbn = sp.cfg == LONGK ? CfgLongK::TBN : CfgShortK::TBN;
       rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, tbn);
       if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, tbn);
@@ -678,21 +744,24 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, co
     // per-row inputs and outputs are [rows, N] arrays, N = this layer's width
     for (int a = 0; a < 2 && !rc; ++a)
       if (sp.in[a]) {
-        rc = make_epi_map(&maps.in[a], sp.in[a], rows, sp.N);
+        rc = make_epi_map(&maps.in[a], sp.in[a], 4, rows, sp.N);
         ep.nin = a + 1;
       }
     for (int a = 0; a < 3 && !rc; ++a)
       if (sp.out[a]) {
-        rc = make_epi_map(&maps.out[a], sp.out[a], rows, sp.N);
+        rc = make_epi_map(&maps.out[a], sp.out[a], a == 0 ? 4 : 2, rows, sp.N);
         ep.out_mask |= 1 << a;
       }
     if (rc) return rc;
     for (int t = 0; t < ntypes; ++t) {
       ep.bias[t] = nets[t].b[sp.layer];
       ep.idt[t] = nets[t].idt[sp.layer];
+      ep.cscale[t] = sp.fwd ? nets[t].cs_fwd[sp.layer] : nets[t].cs_bwd[sp.layer];
+      ep.oscale[t] = sp.act >= 0 ? nets[t].act_scale[sp.act] : 1.f;
     }
     if (sp.kind == EPI_B3)
       for (int t = 0; t < ntypes; ++t) ep.idt[t] = nets[t].idt[1];
+    if (sp.kind == EPI_F1) ep.rscale = D_rscale;
     if (sp.kind == EPI_F3) ep.epart = ws.epart;
     // launched with programmatic stream serialization: each layer's CTAs
     // start (barriers, TMEM, weight tiles) while the previous layer drains

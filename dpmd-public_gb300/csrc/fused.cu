@@ -193,13 +193,6 @@ __device__ __forceinline__ void st_row4(double* p, const dbl4& v) {
   reinterpret_cast<double2*>(p)[1] = double2{v.z, v.w};
 }
 
-// x rounded to TF32 (10 explicit mantissa bits): to nearest, ties away from
-// zero on the magnitude bits
-__device__ __forceinline__ float rn_tf32(float x) {
-  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-__device__ __forceinline__ double rn_tf32(double x) { return x; }
-
 // Per-warp shared slot arrays: env row (or, after phase 1, dE/d em), in-row
 // offset and table row of every evaluated slot, and the count of evaluated
 // slots of each type section.
@@ -241,8 +234,8 @@ __host__ __device__ constexpr size_t fwd_warp_bytes(int nnei, int mp) {
 // lanes per neighbour, 32 / tw neighbours per instruction.
 template <typename T, int NQF, int W>
 __global__ void __launch_bounds__(W * 32)
-    k_desc_fwd(T* __restrict__ X, T* __restrict__ D, T* __restrict__ D_lo,
-               const T* __restrict__ em, const int* __restrict__ atype,
+    k_desc_fwd(T* __restrict__ X, T* __restrict__ D, void* __restrict__ D_lo,
+               float* __restrict__ D_rs, const T* __restrict__ em, const int* __restrict__ atype,
                const int* __restrict__ drow, TabSet<T> ts, int nloc, int nnei, int M, int tail_w,
                int tail_lg) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -378,7 +371,41 @@ __global__ void __launch_bounds__(W * 32)
   __syncwarp();
   const size_t r = drow ? (size_t)drow[i] : (size_t)i;
   T* d = D + r * M * kAxis;
-  T* dl = D_lo ? D_lo + r * M * kAxis : nullptr;
+  if constexpr (sizeof(T) == 4) {
+    if (D_lo) {
+      // split for the tensor-core fitting: FP16 hi / lo of c D, c = 2^s from
+      // |D_ka| <= |X_k| |X_a| (Cauchy-Schwarz over the 4 rows of X)
+      float nk = 0.f, na = 0.f;
+      for (int k = lane; k < M; k += 32) {
+        float q = 0.f;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) q += xs[m * MP + k] * xs[m * MP + k];
+        nk = fmaxf(nk, q);
+        if (k < kAxis) na = fmaxf(na, q);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        nk = fmaxf(nk, __shfl_xor_sync(kFull, nk, o));
+        na = fmaxf(na, __shfl_xor_sync(kFull, na, o));
+      }
+      const float sc = f16_scale_for(sqrtf(nk * na) * 1.0001f);
+      __half* dh = reinterpret_cast<__half*>(D) + r * M * kAxis;
+      __half* dl = static_cast<__half*>(D_lo) + r * M * kAxis;
+      for (int e = lane * 4; e < M * kAxis; e += 128) {
+        const int k = e >> 4, a0 = e & 15;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const float xk = xs[m * MP + k];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) v[c] += xk * xs[m * MP + a0 + c];
+        }
+        st_split4_f16(dh + e, dl + e, v, sc);
+      }
+      if (lane == 0) D_rs[r] = 1.f / sc;
+      return;
+    }
+  }
   for (int e = lane * 4; e < M * kAxis; e += 128) {
     const int k = e >> 4, a0 = e & 15;
     T v[4] = {T(0), T(0), T(0), T(0)};
@@ -388,27 +415,12 @@ __global__ void __launch_bounds__(W * 32)
 #pragma unroll
       for (int c = 0; c < 4; ++c) v[c] += xk * xs[m * MP + a0 + c];
     }
-    if (dl) {
-      // TF32 head and the remainder, both rounded to TF32
-      V4<T> h, l;
-      h.x = rn_tf32(v[0]);
-      h.y = rn_tf32(v[1]);
-      h.z = rn_tf32(v[2]);
-      h.w = rn_tf32(v[3]);
-      l.x = rn_tf32(v[0] - h.x);
-      l.y = rn_tf32(v[1] - h.y);
-      l.z = rn_tf32(v[2] - h.z);
-      l.w = rn_tf32(v[3] - h.w);
-      st_row4(d + e, h);
-      st_row4(dl + e, l);
-    } else {
-      V4<T> o;
-      o.x = v[0];
-      o.y = v[1];
-      o.z = v[2];
-      o.w = v[3];
-      st_row4(d + e, o);
-    }
+    V4<T> o;
+    o.x = v[0];
+    o.y = v[1];
+    o.z = v[2];
+    o.w = v[3];
+    st_row4(d + e, o);
   }
 }
 
@@ -953,9 +965,9 @@ int check_shapes(int M, int A, int nnei) {
 }
 
 template <typename T, int NQF, int W>
-void launch_fwd(size_t warp_bytes, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
-                const int* atype, const int* drow, const TabSet<T>& ts, int nloc, int nnei, int M,
-                int tail_w, int tail_lg) {
+void launch_fwd(size_t warp_bytes, cudaStream_t st, T* X, T* D, void* D_lo, float* D_rs,
+                const T* em, const int* atype, const int* drow, const TabSet<T>& ts, int nloc,
+                int nnei, int M, int tail_w, int tail_lg) {
   auto kern = k_desc_fwd<T, NQF, W>;
   const size_t smem = (size_t)W * warp_bytes;
   if (smem > 48 * 1024)
@@ -966,40 +978,40 @@ void launch_fwd(size_t warp_bytes, cudaStream_t st, T* X, T* D, T* D_lo, const T
   const int per_sm = (36 / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
-  kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(X, D, D_lo, em, atype, drow, ts, nloc,
-                                                             nnei, M, tail_w, tail_lg);
+  kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(X, D, D_lo, D_rs, em, atype, drow,
+                                                             ts, nloc, nnei, M, tail_w, tail_lg);
 }
 
 template <typename T, int W>
-void fwd_dispatch(int nqf, size_t warp_bytes, cudaStream_t st, T* X, T* D, T* D_lo, const T* em,
-                  const int* atype, const int* drow, const TabSet<T>& ts, int nloc, int nnei,
-                  int M, int tail_w, int tail_lg) {
+void fwd_dispatch(int nqf, size_t warp_bytes, cudaStream_t st, T* X, T* D, void* D_lo,
+                  float* D_rs, const T* em, const int* atype, const int* drow,
+                  const TabSet<T>& ts, int nloc, int nnei, int M, int tail_w, int tail_lg) {
   switch (nqf) {
     case 0:
-      launch_fwd<T, 0, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                          tail_lg);
+      launch_fwd<T, 0, W>(warp_bytes, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M,
+                          tail_w, tail_lg);
       break;
     case 1:
-      launch_fwd<T, 1, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                          tail_lg);
+      launch_fwd<T, 1, W>(warp_bytes, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M,
+                          tail_w, tail_lg);
       break;
     case 2:
-      launch_fwd<T, 2, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                          tail_lg);
+      launch_fwd<T, 2, W>(warp_bytes, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M,
+                          tail_w, tail_lg);
       break;
     case 3:
-      launch_fwd<T, 3, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                          tail_lg);
+      launch_fwd<T, 3, W>(warp_bytes, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M,
+                          tail_w, tail_lg);
       break;
     default:
-      launch_fwd<T, 4, W>(warp_bytes, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w,
-                          tail_lg);
+      launch_fwd<T, 4, W>(warp_bytes, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M,
+                          tail_w, tail_lg);
       break;
   }
 }
 
 template <typename T>
-int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow,
+int desc_fwd(T* X, T* D, void* D_lo, float* D_rs, const T* em, const int* atype, const int* drow,
              const T* const* tables, const T* infos, int ntypes, const int* sel, int one_side,
              int nloc, int M, int A, cudaStream_t st, int w = 0) {
   TabSet<T> ts;
@@ -1026,11 +1038,14 @@ int desc_fwd(T* X, T* D, T* D_lo, const T* em, const int* atype, const int* drow
                (size_t)kFWarps * wb);
   if (w == 0) w = tuned_warps(kTuneFwd, sizeof(T), M, nnei, nloc, kFWarps);
   if (w == 1)
-    fwd_dispatch<T, 1>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
+    fwd_dispatch<T, 1>(nqf, wb, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                         tail_lg);
   else if (w == 2)
-    fwd_dispatch<T, 2>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
+    fwd_dispatch<T, 2>(nqf, wb, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                         tail_lg);
   else
-    fwd_dispatch<T, 4>(nqf, wb, st, X, D, D_lo, em, atype, drow, ts, nloc, nnei, M, tail_w, tail_lg);
+    fwd_dispatch<T, 4>(nqf, wb, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M, tail_w,
+                         tail_lg);
   GBDP_CHECK_LAUNCH("se_a_descriptor_fwd");
   return GBDP_OK;
 }
@@ -1201,9 +1216,9 @@ extern "C" int gbdp_table_to_planar_f64(double* dst, const double* src, int nrow
     const cudaStream_t st = (cudaStream_t)stream;                                               \
     return tune_run(kTuneFwd, (int)sizeof(T), last_layer_size, sum_sel(sel, ntypes), nloc, st,  \
                     [&](int w) {                                                                \
-                      return desc_fwd<T>(X, D, nullptr, em, atype, d_row, tables, table_infos,  \
-                                         ntypes, sel, type_one_side, nloc, last_layer_size,     \
-                                         axis_neuron, st, w);                                   \
+                      return desc_fwd<T>(X, D, nullptr, nullptr, em, atype, d_row, tables,      \
+                                         table_infos, ntypes, sel, type_one_side, nloc,         \
+                                         last_layer_size, axis_neuron, st, w);                  \
                     });                                                                         \
   }                                                                                             \
   extern "C" int gbdp_se_a_descriptor_bwd_##SFX(                                                \
@@ -1229,14 +1244,16 @@ GBDP_FUSED_ENTRY(float, f32)
 GBDP_FUSED_ENTRY(double, f64)
 
 extern "C" int gbdp_se_a_descriptor_fwd_split_f32(
-    float* X, float* D_hi, float* D_lo, const float* em, const int* atype, const int* d_row,
-    const float* const* tables, const float* table_infos, int ntypes, const int* sel,
-    int type_one_side, int nloc, int last_layer_size, int axis_neuron, gbdp_stream stream) {
-  GBDP_REQUIRE(D_lo != nullptr, "se_a_descriptor_fwd_split: null D_lo");
+    float* X, void* D_hi, void* D_lo, float* D_rscale, const float* em, const int* atype,
+    const int* d_row, const float* const* tables, const float* table_infos, int ntypes,
+    const int* sel, int type_one_side, int nloc, int last_layer_size, int axis_neuron,
+    gbdp_stream stream) {
+  GBDP_REQUIRE(D_hi && D_lo && D_rscale, "se_a_descriptor_fwd_split: null D_hi / D_lo / D_rscale");
   const cudaStream_t st = (cudaStream_t)stream;
   return tune_run(kTuneFwd, 4, last_layer_size, sum_sel(sel, ntypes), nloc, st, [&](int w) {
-    return desc_fwd<float>(X, D_hi, D_lo, em, atype, d_row, tables, table_infos, ntypes, sel,
-                           type_one_side, nloc, last_layer_size, axis_neuron, st, w);
+    return desc_fwd<float>(X, static_cast<float*>(D_hi), D_lo, D_rscale, em, atype, d_row,
+                           tables, table_infos, ntypes, sel, type_one_side, nloc,
+                           last_layer_size, axis_neuron, st, w);
   });
 }
 

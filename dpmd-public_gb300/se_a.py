@@ -24,6 +24,7 @@ Energies and virials are reduced per frame in float64.
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 import torch
@@ -115,7 +116,7 @@ def _emb_tc_ok(cfg, emb) -> bool:
 
 class SeAModel:
     FIT_MODES = ("fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
-                 "native-bf16", "tc-tf32x3")
+                 "native-bf16", "tc-f16x3")
     _NATIVE = {"native-fp32": 0, "native-bf16x9": 1, "native-tf32": 2, "native-bf16": 3}
 
     def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
@@ -164,26 +165,36 @@ class SeAModel:
             flat = self.table_infos.reshape(-1)
             self._tab_infos = (ct * len(flat))(*flat.tolist())
         self._sel_c = (ctypes.c_int * cfg.ntypes)(*[int(s) for s in cfg.sel])
-        # split weights for the tensor-core fitting (tcgen05, TF32 hi/lo)
+        # weights for the tensor-core fitting (tcgen05 kind::f16): FP16 hi / lo
+        # images under per-row power-of-two scales, the matching inverse
+        # column scales, and the activation scales from parameter bounds
         self._tc_nets = None
-        if dtype == torch.float32 and self.fit_mode == "tc-tf32x3":
+        if dtype == torch.float32 and self.fit_mode == "tc-f16x3":
             nets = (L.FitTcNet * cfg.ntypes)()
             self._tc_keep = []
             for t, (hidden, wf, bf) in enumerate(self.fit):
                 if len(hidden) != 3 or [w.shape for w, *_ in hidden] != [(1600, 240), (240, 240),
                                                                            (240, 240)]:
-                    raise ValueError("tc-tf32x3 serves the 1600-240-240-240 fitting net only")
+                    raise ValueError("tc-f16x3 serves the 1600-240-240-240 fitting net only")
                 if hidden[0][2] is not None or hidden[1][2] is None or hidden[2][2] is None:
-                    raise ValueError("tc-tf32x3 expects a time step on layers 2 and 3 only")
+                    raise ValueError("tc-f16x3 expects a time step on layers 2 and 3 only")
+                wo = wf[:, 0].contiguous()
+                act = _fit_tc_act_scales(hidden, wo)
+                s_in = [1.0, act[0], act[1]]   # D rows carry their own scales
+                s_g = [act[4], act[3], act[2]]  # GZ1, GZ2, GZ3 feed layers 0, 1, 2 back
                 for l, (w, b_, idt, skip) in enumerate(hidden):
-                    wh, wl = _split_tf32(w.contiguous())
-                    wth, wtl = _split_tf32(w.t().contiguous())
-                    self._tc_keep += [wh, wl, wth, wtl]
+                    wth, wtl, inv_v = _split_f16_rows(w.t().contiguous())
+                    wh, wl, inv_u = _split_f16_rows(w.contiguous())
+                    csf = (inv_v / s_in[l]).contiguous()
+                    csb = (inv_u / s_g[l]).contiguous()
+                    self._tc_keep += [wh, wl, wth, wtl, csf, csb]
                     nets[t].w_hi[l], nets[t].w_lo[l] = wh.data_ptr(), wl.data_ptr()
                     nets[t].wt_hi[l], nets[t].wt_lo[l] = wth.data_ptr(), wtl.data_ptr()
+                    nets[t].cs_fwd[l], nets[t].cs_bwd[l] = csf.data_ptr(), csb.data_ptr()
                     nets[t].b[l] = b_.data_ptr()
                     nets[t].idt[l] = 0 if idt is None else idt.data_ptr()
-                wo = wf[:, 0].contiguous()
+                for a in range(5):
+                    nets[t].act_scale[a] = act[a]
                 self._tc_keep.append(wo)
                 nets[t].w_out = wo.data_ptr()
                 nets[t].b_out = float(bf[0])
@@ -309,7 +320,8 @@ class SeAModel:
         lib = self._lib
         if self._tc_nets is not None:
             L.check(lib.gbdp_se_a_descriptor_fwd_split_f32(
-                _ptr(b.X), _ptr(b.D), _ptr(b.D_lo), _ptr(b.env.em), _ptr(b.atype), _ptr(b.drow),
+                _ptr(b.X), _ptr(b.D), _ptr(b.D_lo), _ptr(b.D_rs), _ptr(b.env.em), _ptr(b.atype),
+                _ptr(b.drow),
                 self._tab_ptrs, self._tab_infos, cfg.ntypes, self._sel_c, int(cfg.type_one_side), n,
                 M, A, _stream()), "se_a_descriptor_fwd_split")
             self.fitting_tc(b)
@@ -338,7 +350,8 @@ class SeAModel:
         nt = self.cfg.ntypes
         nrows = (ctypes.c_int * nt)(*[c for _, c in b.type_rows])
         L.check(self._lib.gbdp_fitting_tc_f32(
-            _ptr(b.ae), _ptr(b.dD), _ptr(b.D), _ptr(b.D_lo), nt, nrows, b.row_off_c, self._tc_nets,
+            _ptr(b.ae), _ptr(b.dD), _ptr(b.D), _ptr(b.D_lo), _ptr(b.D_rs), nt, nrows, b.row_off_c,
+            self._tc_nets,
             _ptr(b.tc_ws), ctypes.c_size_t(b.tc_ws.numel()), _stream()), "fitting_tc")
         for t, (s0, cnt) in enumerate(b.type_rows):
             if cnt and float(self.params_bias[t]) != 0.0:
@@ -374,7 +387,8 @@ class SeAModel:
         n1, n2, n3 = cfg.neuron
         sel = (ctypes.c_int * cfg.ntypes)(*[int(x) for x in cfg.sel])
         L.check(self._lib.gbdp_embed_fwd_tc_bf16(
-            _ptr(b.X), _ptr(b.D), _ptr(getattr(b, "D_lo", None)), _ptr(b.drow), _ptr(em),
+            _ptr(b.X), _ptr(b.D), _ptr(getattr(b, "D_lo", None)), _ptr(getattr(b, "D_rs", None)),
+            _ptr(b.drow), _ptr(em),
             _ptr(b.atype), _ptr(b.units), b.nunits, _ptr(self._emb_tc), cfg.ntypes, sel,
             int(cfg.type_one_side), b.nloc, cfg.nnei, n1, n2, n3, cfg.axis_neuron,
             _ptr(b.emb_status), _stream()), "embed_fwd_tc")
@@ -541,6 +555,45 @@ def _split_tf32(x: torch.Tensor):
     return hi, _rn_tf32(x - hi)
 
 
+def _f16_scale(bound: float) -> float:
+    """2^s with bound * 2^s < 2^15 (1 for a zero or non-finite bound): the
+    power-of-two scale under which a block with magnitudes up to ``bound``
+    splits into FP16 hi / lo parts without overflow."""
+    if not (bound > 0.0) or not math.isfinite(bound):
+        return 1.0
+    return math.ldexp(1.0, 15 - max(math.frexp(bound)[1], -100))
+
+
+def _split_f16_rows(m: torch.Tensor):
+    """FP16 hi / lo images of m [rows, K] (FP32), row r scaled by 2^u_r
+    (``_f16_scale`` of the row's largest magnitude): hi = fp16(m 2^u),
+    lo = fp16(m 2^u - hi), both rounded to nearest; and 2^-u [rows]."""
+    mx = m.abs().amax(dim=1).double().cpu().numpy()
+    sc = torch.tensor([_f16_scale(float(v)) for v in mx], dtype=torch.float32, device=m.device)
+    x = m * sc[:, None]
+    hi = x.half()
+    lo = (x - hi.float()).half()
+    return hi.contiguous(), lo.contiguous(), 1.0 / sc
+
+
+def _fit_tc_act_scales(hidden, wo: torch.Tensor) -> list:
+    """Scales of the tensor-core fitting's split activations H1, H2, GZ3,
+    GZ2, GZ1 of one net, from bounds on their magnitudes over any input:
+    |T| <= 1 and 0 <= 1 - T^2 <= 1 for every tanh output T, and
+    |sum_j g_j W_ij| <= max|g| max_i sum_j |W_ij| for every GEMM (1 %
+    margin for FP32 rounding)."""
+    (_, _, _, _), (w2, _, idt2, _), (w3, _, idt3, _) = hidden
+    f = lambda x: float(x.double().abs().max())
+    rows = lambda w: float(w.double().abs().sum(dim=1).max())
+    b_h1 = 1.0
+    b_h2 = 1.0 + f(idt2)
+    b_gz3 = f(wo.double() * idt3.double())
+    b_g2 = b_gz3 * rows(w3) + f(wo)
+    b_gz2 = b_g2 * f(idt2)
+    b_gz1 = b_gz2 * rows(w2) + b_g2
+    return [_f16_scale(1.01 * b) for b in (b_h1, b_h2, b_gz3, b_gz2, b_gz1)]
+
+
 def energy_std_loss(E, F, V, E_ref, F_ref, V_ref, natoms: int, pref_e=0.02, pref_f=1000.0,
                     pref_v=0.02):
     """EnergyStdLoss with fixed prefactors (deepmd/pt/loss/ener.py:197-360):
@@ -689,13 +742,19 @@ class Batch:
         self.env = e
         self.X = torch.empty((n, 4, M), dtype=dt, device=dev)
         nr = self.nrows_total
-        self.D = torch.zeros((nr, M * A), dtype=dt, device=dev)
         self.dD = torch.zeros((nr, M * A), dtype=dt, device=dev)
         self.ae = torch.zeros((nr,), dtype=dt, device=dev)
         if pad > 1:
-            self.D_lo = torch.zeros((nr, M * A), dtype=dt, device=dev)
+            # D split for the tensor-core fitting: FP16 hi / lo parts of each
+            # row under its power-of-two scale, and the inverse scales
+            # (padding rows: zeros under scale 1)
+            self.D = torch.zeros((nr, M * A), dtype=torch.float16, device=dev)
+            self.D_lo = torch.zeros((nr, M * A), dtype=torch.float16, device=dev)
+            self.D_rs = torch.ones((nr,), dtype=torch.float32, device=dev)
             tcb = int(model._lib.gbdp_fitting_tc_workspace_bytes(nr))
             self.tc_ws = torch.zeros(tcb, dtype=torch.uint8, device=dev)
+        else:
+            self.D = torch.zeros((nr, M * A), dtype=dt, device=dev)
         # the step's outputs in one device buffer (energies and virials FP64,
         # then forces), so that a caller reads them back with a single copy:
         # `out` is that buffer, energy / vir / force are views into it
@@ -706,6 +765,13 @@ class Batch:
         self.energy = self.out[:nf * esz].view(torch.float64)
         self.vir = self.out[nf * esz:nf * 10 * esz].view(torch.float64).view(nf, 9)
         self.force = self.out[nf * 10 * esz:].view(dt).view(n, 3)
+
+    def descriptor_rows(self) -> torch.Tensor:
+        """D [nrows, M * axis_neuron] in the model's dtype, from the split
+        FP16 parts and row scales where the tensor-core fitting is used."""
+        if hasattr(self, "D_lo"):
+            return (self.D.float() + self.D_lo.float()) * self.D_rs[:, None]
+        return self.D
 
     def ensure_plain_tc(self, model: SeAModel):
         """Buffers of the tensor-core plain form (allocated once): atom pairs

@@ -397,32 +397,47 @@ GBDP_API int gbdp_fitting_fwd_bwd_f32(float* e, float* dD, const float* D, int n
                                       gbdp_stream stream);
 
 /* As gbdp_se_a_descriptor_fwd_f32, but D is written split for the tensor-
- * core fitting: D_hi = D rounded to TF32 (10 explicit mantissa bits, to
- * nearest), D_lo = (D - D_hi) rounded to TF32. */
+ * core fitting, as two FP16 arrays (IEEE binary16, [nrows, M * axis_neuron]
+ * each) under a power-of-two scale per row: with c = 2^s the scale of row r,
+ * D_hi = fp16(c D) and D_lo = fp16(c D - D_hi) (round to nearest), and
+ * D_rscale[r] = 1 / c.  c is chosen from the Cauchy-Schwarz bound
+ * |D_ka| <= |X_k| |X_a| so that c |D| < 2^15.  Rows no atom maps to are not
+ * written. */
 GBDP_API int gbdp_se_a_descriptor_fwd_split_f32(
-    float* X, float* D_hi, float* D_lo, const float* em, const int* atype, const int* d_row,
+    float* X, void* D_hi, void* D_lo, float* D_rscale, const float* em, const int* atype, const int* d_row,
     const float* const* tables, const float* table_infos, int ntypes, const int* sel,
     int type_one_side, int nloc, int last_layer_size, int axis_neuron, gbdp_stream stream);
 
 /* ------------------------------------------------------------------------
- * Fitting nets on the tensor cores (tcgen05, TF32 with a hi/lo split that
- * keeps FP32-level accuracy), for the se_e2_a fitting shape
- * 1600 -> 240 -> 240 -> 240 -> 1 (layers 2 and 3 with time step and skip).
+ * Fitting nets on the tensor cores (tcgen05 kind::f16, each FP32 operand as
+ * a scaled FP16 hi/lo pair, which keeps FP32-level accuracy), for the
+ * se_e2_a fitting shape 1600 -> 240 -> 240 -> 240 -> 1 (layers 2 and 3
+ * with time step and skip).
  * Rows are grouped by atom type: type t owns rows [row_off[t],
  * row_off[t] + nrows[t]) of every activation, row_off[t] a multiple of 128,
  * row_off[ntypes] the padded total (also a multiple of 128).  D is given
- * split (D_hi = D rounded to TF32, D_lo = (D - D_hi) rounded to TF32), as
- * gbdp_se_a_descriptor_fwd_split_f32 writes it; the weights are split the
- * same way.  Per type (device pointers):
- * w_hi/w_lo[l] = W_l [in, out] and wt_hi/wt_lo[l] = W_l^T [out, in], split;
- * b[l]; idt[l] (NULL for layer 0); w_out [240]; b_out on the host.
+ * split with its per-row inverse scales, as
+ * gbdp_se_a_descriptor_fwd_split_f32 writes it.  Per type (device
+ * pointers; FP16 images 16-byte aligned, FP32 arrays 16-byte aligned):
+ *   w_hi/w_lo[l]   W_l [in, out] with row i scaled by 2^u_i, split
+ *   wt_hi/wt_lo[l] W_l^T [out, in] with row j scaled by 2^v_j, split
+ *   cs_fwd[l]      [out]: 2^-(v_j + s_in(l)), s_in = 0, s_H1, s_H2
+ *   cs_bwd[l]      [in]:  2^-(u_i + s_g(l)),  s_g = s_GZ1, s_GZ2, s_GZ3
+ *   act_scale      2^s of the split activations H1, H2, GZ3, GZ2, GZ1 in
+ *                  that order, each bringing a bound on the activation's
+ *                  magnitude below 2^15 (dpmd_public_gb300.se_a builds all
+ *                  of these from the parameters)
+ *   b[l]; idt[l] (NULL for layer 0); w_out [240]; b_out on the host.
  * Outputs: e [rows] per-row energy (0 on padding rows), dE_dD [rows, 1600].
  * ---------------------------------------------------------------------- */
 typedef struct gbdp_fit_tc_net {
-  const float* w_hi[3];
-  const float* w_lo[3];
-  const float* wt_hi[3];
-  const float* wt_lo[3];
+  const void* w_hi[3];
+  const void* w_lo[3];
+  const void* wt_hi[3];
+  const void* wt_lo[3];
+  const float* cs_fwd[3];
+  const float* cs_bwd[3];
+  float act_scale[5];
   const float* b[3];
   const float* idt[3];
   const float* w_out;
@@ -430,10 +445,10 @@ typedef struct gbdp_fit_tc_net {
 } gbdp_fit_tc_net;
 
 GBDP_API size_t gbdp_fitting_tc_workspace_bytes(int rows);
-GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const float* D_hi, const float* D_lo,
-                                 int ntypes, const int* nrows, const int* row_off,
-                                 const gbdp_fit_tc_net* nets, void* workspace,
-                                 size_t workspace_bytes, gbdp_stream stream);
+GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, const void* D_lo,
+                                 const float* D_rscale, int ntypes, const int* nrows,
+                                 const int* row_off, const gbdp_fit_tc_net* nets,
+                                 void* workspace, size_t workspace_bytes, gbdp_stream stream);
 /* Synchronise `stream`; device status word of the last gbdp_fitting_tc_f32
  * run on this workspace (GBDP_OK or GBDP_STATUS_TIMEOUT). */
 GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream);
@@ -469,14 +484,18 @@ GBDP_API int gbdp_autotune_report(char* buf, int len);
  * tensor-core wait gave up.
  *
  * forward:  X [nloc, 4, n3] (sums / nnei), D [rows, n3 * axis] at row drow[i]
- *           (drow null: row i), D_lo optional TF32 remainder of D.
+ *           (drow null: row i), FP32; or, with D_lo and D_rscale given, D
+ *           split for the tensor-core fitting (D and D_lo FP16 hi / lo
+ *           parts, D_rscale per-row inverse scales, as
+ *           gbdp_se_a_descriptor_fwd_split_f32 writes them).
  * backward: from dE/dD (same rows), the gradient wrt the env matrix
  *           net_deriv [nloc, nnei, 4] (every slot written); dx_work is
  *           caller scratch of nloc * 4 * n3 floats. */
 GBDP_API size_t gbdp_embed_tc_net_bytes(void);
-GBDP_API int gbdp_embed_fwd_tc_bf16(float* X, float* D, float* D_lo, const int* drow,
-                                    const float* em, const int* atype, const int* units,
-                                    int nunits, const void* nets, int ntypes, const int* sel,
+GBDP_API int gbdp_embed_fwd_tc_bf16(float* X, void* D, void* D_lo, float* D_rscale,
+                                    const int* drow, const float* em, const int* atype,
+                                    const int* units, int nunits, const void* nets, int ntypes,
+                                    const int* sel,
                                     int type_one_side, int nloc, int nnei, int n1, int n2, int n3,
                                     int axis, int* status, gbdp_stream stream);
 GBDP_API int gbdp_embed_bwd_tc_bf16(float* net_deriv, float* dx_work, const float* dD,

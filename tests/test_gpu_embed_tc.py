@@ -29,7 +29,7 @@ def setup(gb):
     stat = [water.water_frame(4, 12.42, 1000 + s) for s in range(4)]
     m64 = se_a.build_model(cfg, 7, stat, DEV, torch.float64)
     args = (cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), DEV, torch.float32)
-    return se_a, water, cfg, m64, se_a.SeAModel(*args), se_a.SeAModel(*args, fit_mode="tc-tf32x3")
+    return se_a, water, cfg, m64, se_a.SeAModel(*args), se_a.SeAModel(*args, fit_mode="tc-f16x3")
 
 
 def _ref_x(model, em, atype):
@@ -77,9 +77,7 @@ def test_forward_x_and_d(setup, mdl_idx):
     ex = float((batch.X - Xr).abs().max() / Xr.abs().max())
     A = cfg.axis_neuron
     Dr = torch.einsum("ncm,nca->nma", Xr, Xr[:, :, :A]).reshape(batch.nloc, -1)
-    D = batch.D[batch.drow.long()]
-    if hasattr(batch, "D_lo"):
-        D = D + batch.D_lo[batch.drow.long()]
+    D = batch.descriptor_rows()[batch.drow.long()]
     ed = float((D - Dr).abs().max() / Dr.abs().max())
     print(f"X rel err {ex:.3e}, D rel err {ed:.3e}")
     assert ex <= 1e-2 and ed <= 1e-2

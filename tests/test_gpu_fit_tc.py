@@ -1,4 +1,4 @@
-"""Tensor-core fitting (tcgen05 kind::tf32, TF32 hi/lo split) against the
+"""Tensor-core fitting (tcgen05 kind::f16, scaled FP16 hi/lo split) against the
 cuBLAS FP32 path on the same descriptor rows, and the fused step with it
 against the FP64 composite.
 
@@ -34,7 +34,7 @@ def setup(gb):
 
 def test_tc_fitting_matches_fp32_gemm(setup):
     se_a, cfg, m64, mk, water = setup
-    ref, tc = mk("native-fp32"), mk("tc-tf32x3")
+    ref, tc = mk("native-fp32"), mk("tc-f16x3")
     frame = water.water_frame(5, 15.525, 8)  # 375 atoms: 125 O, 250 H (ragged 128-blocks)
     bt = tc.batch([frame[1]], frame[2][None])
     br = ref.batch([frame[1]], frame[2][None])
@@ -60,7 +60,7 @@ def test_tc_fused_step_vs_fp64(setup):
     import composite
 
     se_a, cfg, m64, mk, water = setup
-    tc = mk("tc-tf32x3")
+    tc = mk("tc-f16x3")
     frame = water.water_frame(4, 12.42, 5)
     b = tc.batch([frame[1]], frame[2][None])
     E, F, V = tc.step_fused(b, torch.tensor(frame[0], dtype=torch.float32, device=DEV))

@@ -52,17 +52,19 @@ namespace {
 constexpr int TBM = 128, TBK = 64;     // a k-block: 64 FP16 = one 128-byte swizzle row
 constexpr int A_TILE = TBM * TBK * 2;  // 16 KiB
 
-// Tile configurations.  The layers are too small to fill 152 SMs with wide
-// tiles, and a CTA's TMA -> MMA pipeline is latency-bound, so narrow tiles
-// with two CTAs per SM (one CTA's epilogue overlapping the other's main
-// loop) measured fastest on the 12,288-row step (128 x 240 tiles: the K-240
-// layers 28-37 us instead of 21-24 us; 128 x 160 for the 1600-wide layer:
-// 78 us instead of 75 us):
+// Tile configurations of the per-tile kernel k_fit_tc (128 x 80 tiles):
 //   CfgLongK   F1 (K 1600): 4 stages, 3 main accumulators, one CTA per SM
-//              (214 KB shared, 512 TMEM columns); the 3 accumulators keep
-//              the long chain FP32-accurate
+//              (214 KB shared, 512 TMEM columns).  The 3 accumulators keep
+//              the long chain FP32-accurate: one main accumulator measured
+//              2.3x the energy error and 7x the frame-virial error, its
+//              truncation errors adding up coherently over a frame.
 //   CfgShortK  K 240 layers: 2 stages, 1 main accumulator, two CTAs per SM
-//              (105 KB shared, 256 TMEM columns each)
+//              (105 KB shared, 256 TMEM columns each): with about two tiles
+//              per SM, a second CTA's epilogue overlapping the first's main
+//              loop measured faster than the persistent kernel (about 21 us
+//              against 25-27 us a layer).
+// B1 (1920 tiles of 128 x 80 on the 12,288-row step, about 12 per SM) runs
+// on the persistent kernel k_fit_pers (64 us -> 49 us).
 template <int TBN_, int STAGES_, int NACC_>
 struct TcCfg {
   static constexpr int TBN = TBN_, STAGES = STAGES_, NACC = NACC_;
@@ -264,6 +266,10 @@ __device__ __forceinline__ void col_ld16(const float* p, float* v) {
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // programmatic dependent launch: wait for the grid this one depends on (all
 // its writes visible); let the dependent grid be scheduled
 __device__ __forceinline__ void griddep_wait() {
@@ -271,6 +277,155 @@ __device__ __forceinline__ void griddep_wait() {
 }
 __device__ __forceinline__ void griddep_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Per-warp epilogue progress, carried across the tiles a CTA processes:
+// chunks done (input and output staging buffers alternate by chunk) and
+// input loads issued / received.
+struct EpiState {
+  int gci, in_issued, in_done;
+};
+
+// The epilogue of one warp's 32 rows of a tile: TBN / 16 chunks of 16
+// columns.  Accumulators at tacc (this warp's TMEM lanes, the tile's first
+// column): nmain main accumulators acc_stride columns apart and the cross
+// terms at cross_off.  Per-row inputs arrive by TMA into the warp's staging
+// (wsm, barriers ib[2]), outputs leave by TMA bulk stores.  Returns false
+// after a timeout.
+template <int TBN>
+__device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, int t, int yrow,
+                                         int n0, int lane, unsigned char* wsm, uint64_t* ib,
+                                         uint32_t tacc, int nmain, uint32_t acc_stride,
+                                         uint32_t cross_off, EpiState& es, float& esum) {
+  float* inb = reinterpret_cast<float*>(wsm);  // [2 buf][2 arr][chunk]
+  unsigned char* outb = wsm + EPI_IN_BYTES;    // [2 buf][o0 | hi | lo]
+  const int nin = ep.nin;
+  constexpr int NCH = TBN / 16;
+  // F1: the inverse scale of this thread's D row; the split output's scale
+  const float rsc = ep.kind == EPI_F1 ? __ldg(ep.rscale + yrow + lane) : 1.f;
+  const float osc = ep.oscale[t];
+  if (nin > 0) {
+    // the first chunk's inputs; their buffer was last read two chunks ago
+    const int b0 = es.gci & 1;
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) {
+      mbar_expect_tx(&ib[b0], nin * EPI_CHUNK * 4);
+      for (int a = 0; a < nin; ++a)
+        tma_2d(inb + (b0 * 2 + a) * EPI_CHUNK, &maps.in[a], n0, yrow, &ib[b0]);
+    }
+    ++es.in_issued;
+  }
+#pragma unroll 1
+  for (int ci = 0; ci < NCH; ++ci) {
+    const int c0 = ci * 16, g = es.gci + ci, buf = g & 1;
+    if (ci + 1 < NCH && nin > 0) {
+      // the other input buffer was last read by the previous chunk
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_expect_tx(&ib[buf ^ 1], nin * EPI_CHUNK * 4);
+        for (int a = 0; a < nin; ++a)
+          tma_2d(inb + ((buf ^ 1) * 2 + a) * EPI_CHUNK, &maps.in[a], n0 + c0 + 16, yrow,
+                 &ib[buf ^ 1]);
+      }
+      ++es.in_issued;
+    }
+    float v[16], w[16];
+    const uint32_t ta = tacc + (uint32_t)c0;
+    tmem_ld16(ta, v);
+    for (int a = 1; a < nmain; ++a) {
+      tmem_ld16(ta + (uint32_t)a * acc_stride, w);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] += w[k];
+    }
+    tmem_ld16(ta + cross_off, w);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] += w[k];
+    const int c = n0 + c0;
+    // undo the operand scales (powers of two: exact)
+    col_ld16(ep.cscale[t] + c, w);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = v[k] * w[k] * rsc;
+    float x0[16], x1[16];
+    if (nin > 0) {
+      if (!__all_sync(kFull, mbar_wait_bounded(&ib[buf], (unsigned)(g >> 1) & 1u, ep.status)))
+        return false;
+      ++es.in_done;
+      row_ld16(inb + (buf * 2) * EPI_CHUNK, lane, x0);
+      if (nin > 1) row_ld16(inb + (buf * 2 + 1) * EPI_CHUNK, lane, x1);
+    }
+    float o0[16], sv[16];  // sv: the next operand, scaled, to be split
+    if (ep.kind == EPI_B1) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) o0[k] = v[k];
+    } else if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
+      float bb[16], id[16], wo[16], i2[16];
+      col_ld16(ep.bias[t] + c, bb);
+      if (ep.kind != EPI_F1) col_ld16(ep.idt[t] + c, id);
+      if (ep.kind == EPI_F3) {
+        col_ld16(ep.wout[t] + c, wo);
+        col_ld16(ep.idt2[t] + c, i2);
+      }
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const float tt = tanhf(v[k] + bb[k]);
+        float h = tt;                                      // F1: H1 = T1
+        if (ep.kind == EPI_F2) h = tt * id[k] + x0[k];     // H2 = T2 idt2 + T1
+        if (ep.kind == EPI_F3) {
+          h = tt * id[k] + (x1[k] * i2[k] + x0[k]);        // H3 = T3 idt3 + H2
+          esum += h * wo[k];
+          sv[k] = wo[k] * id[k] * (1.f - tt * tt) * osc;  // GZ3
+        } else {
+          sv[k] = h * osc;
+        }
+        o0[k] = tt;
+      }
+    } else {  // B3: x0 = T2; B2: x0 = T1, x1 = G2
+      float id[16], wo[16];
+      if (ep.kind == EPI_B3) {
+        col_ld16(ep.idt[t] + c, id);
+        col_ld16(ep.wout[t] + c, wo);
+      }
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const float g = v[k] + (ep.kind == EPI_B3 ? wo[k] : x1[k]);
+        o0[k] = g;
+        const float tt = x0[k];
+        sv[k] = (ep.kind == EPI_B3 ? g * id[k] : g) * (1.f - tt * tt) * osc;
+      }
+    }
+    uint32_t hw[8], lw[8];
+    if (ep.out_mask & 6) pack_split16(sv, hw, lw);
+    // the output buffer was last used by the stores of chunk g - 2
+    if (lane == 0 && g >= 2) bulk_wait_read1();
+    __syncwarp();
+    unsigned char* ob = outb + buf * EPI_OUT_BUF;
+    float* o0b = reinterpret_cast<float*>(ob);
+    __half* hib = reinterpret_cast<__half*>(ob + EPI_CHUNK * 4);
+    __half* lob = hib + EPI_CHUNK;
+    if (ep.out_mask & 1) row_st16(o0b, lane, o0);
+    if (ep.out_mask & 2) row_st16h(hib, lane, hw);
+    if (ep.out_mask & 4) row_st16h(lob, lane, lw);
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) {
+      if (ep.out_mask & 1) tma_store_2d(&maps.out[0], c, yrow, o0b);
+      if (ep.out_mask & 2) tma_store_2d(&maps.out[1], c, yrow, hib);
+      if (ep.out_mask & 4) tma_store_2d(&maps.out[2], c, yrow, lob);
+      bulk_commit();
+    }
+  }
+  es.gci += NCH;
+  return true;
+}
+
+// Lane 0, at the end of a warp's epilogue work: its bulk stores complete and
+// no input chunk still in flight (after a timeout) lands once the CTA exits.
+__device__ __forceinline__ void epi_drain(uint64_t* ib, const EpiState& es, int* status) {
+  bulk_wait_all();
+  for (int ch = es.in_done; ch < es.in_issued; ++ch)
+    mbar_wait_bounded(&ib[ch & 1], (unsigned)(ch >> 1) & 1u, status);
 }
 
 // ------------------------------------------------------------- kernel --
@@ -384,127 +539,14 @@ __global__ void __launch_bounds__(128, 1)
   float esum = 0.f;
   if (got) {
     static_assert(4 * EPI_WARP_BYTES <= TSTAGES * STAGE, "epilogue staging exceeds the stage buffers");
-    unsigned char* wsm = smem + warp * EPI_WARP_BYTES;
-    float* inb = reinterpret_cast<float*>(wsm);  // [2 buf][2 arr][chunk]
-    unsigned char* outb = wsm + EPI_IN_BYTES;    // [2 buf][o0 | hi | lo]
     uint64_t* ib = inbar + warp * 2;
     const int yrow = row0 + warp * 32;
-    const int nin = ep.nin;
-    constexpr int NCH = TBN / 16;
-    // F1: the inverse scale of this thread's D row; the split output's scale
-    const float rsc = ep.kind == EPI_F1 ? __ldg(ep.rscale + yrow + lane) : 1.f;
-    const float osc = ep.oscale[t];
-    int in_issued = nin > 0 ? 1 : 0, in_done = 0;  // input chunks issued / received
-    if (lane == 0 && nin > 0) {
-      mbar_expect_tx(&ib[0], nin * EPI_CHUNK * 4);
-      for (int a = 0; a < nin; ++a) tma_2d(inb + a * EPI_CHUNK, &maps.in[a], n0, yrow, &ib[0]);
-    }
-#pragma unroll 1
-    for (int ci = 0; ci < NCH; ++ci) {
-      const int c0 = ci * 16, buf = ci & 1;
-      if (ci + 1 < NCH && nin > 0) {
-        // the other input buffer was last read in chunk ci - 1
-        fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-          mbar_expect_tx(&ib[buf ^ 1], nin * EPI_CHUNK * 4);
-          for (int a = 0; a < nin; ++a)
-            tma_2d(inb + ((buf ^ 1) * 2 + a) * EPI_CHUNK, &maps.in[a], n0 + c0 + 16, yrow,
-                   &ib[buf ^ 1]);
-        }
-        ++in_issued;
-      }
-      float v[16], w[16];
-      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-      tmem_ld16(ta, v);
-      for (int a = 1; a < NACC && a < nkb; ++a) {
-        tmem_ld16(ta + (uint32_t)a * ACC_COLS, w);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) v[k] += w[k];
-      }
-      tmem_ld16(ta + (uint32_t)NACC * ACC_COLS, w);
-#pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] += w[k];
-      const int c = n0 + c0;
-      // undo the operand scales (powers of two: exact)
-      col_ld16(ep.cscale[t] + c, w);
-#pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] = v[k] * w[k] * rsc;
-      float x0[16], x1[16];
-      if (nin > 0) {
-        if (!__all_sync(kFull, mbar_wait_bounded(&ib[buf], (unsigned)(ci >> 1) & 1u, ep.status)))
-          break;
-        ++in_done;
-        row_ld16(inb + (buf * 2) * EPI_CHUNK, lane, x0);
-        if (nin > 1) row_ld16(inb + (buf * 2 + 1) * EPI_CHUNK, lane, x1);
-      }
-      float o0[16], sv[16];  // sv: the next operand, scaled, to be split
-      if (ep.kind == EPI_B1) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) o0[k] = v[k];
-      } else if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
-        float bb[16], id[16], wo[16], i2[16];
-        col_ld16(ep.bias[t] + c, bb);
-        if (ep.kind != EPI_F1) col_ld16(ep.idt[t] + c, id);
-        if (ep.kind == EPI_F3) {
-          col_ld16(ep.wout[t] + c, wo);
-          col_ld16(ep.idt2[t] + c, i2);
-        }
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const float tt = tanhf(v[k] + bb[k]);
-          float h = tt;                                      // F1: H1 = T1
-          if (ep.kind == EPI_F2) h = tt * id[k] + x0[k];     // H2 = T2 idt2 + T1
-          if (ep.kind == EPI_F3) {
-            h = tt * id[k] + (x1[k] * i2[k] + x0[k]);        // H3 = T3 idt3 + H2
-            esum += h * wo[k];
-            sv[k] = wo[k] * id[k] * (1.f - tt * tt) * osc;  // GZ3
-          } else {
-            sv[k] = h * osc;
-          }
-          o0[k] = tt;
-        }
-      } else {  // B3: x0 = T2; B2: x0 = T1, x1 = G2
-        float id[16], wo[16];
-        if (ep.kind == EPI_B3) {
-          col_ld16(ep.idt[t] + c, id);
-          col_ld16(ep.wout[t] + c, wo);
-        }
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const float g = v[k] + (ep.kind == EPI_B3 ? wo[k] : x1[k]);
-          o0[k] = g;
-          const float tt = x0[k];
-          sv[k] = (ep.kind == EPI_B3 ? g * id[k] : g) * (1.f - tt * tt) * osc;
-        }
-      }
-      uint32_t hw[8], lw[8];
-      if (ep.out_mask & 6) pack_split16(sv, hw, lw);
-      // the output buffer was last used by the stores of chunk ci - 2
-      if (lane == 0 && ci >= 2) bulk_wait_read1();
-      __syncwarp();
-      unsigned char* ob = outb + buf * EPI_OUT_BUF;
-      float* o0b = reinterpret_cast<float*>(ob);
-      __half* hib = reinterpret_cast<__half*>(ob + EPI_CHUNK * 4);
-      __half* lob = hib + EPI_CHUNK;
-      if (ep.out_mask & 1) row_st16(o0b, lane, o0);
-      if (ep.out_mask & 2) row_st16h(hib, lane, hw);
-      if (ep.out_mask & 4) row_st16h(lob, lane, lw);
-      fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) {
-        if (ep.out_mask & 1) tma_store_2d(&maps.out[0], c, yrow, o0b);
-        if (ep.out_mask & 2) tma_store_2d(&maps.out[1], c, yrow, hib);
-        if (ep.out_mask & 4) tma_store_2d(&maps.out[2], c, yrow, lob);
-        bulk_commit();
-      }
-    }
-    if (lane == 0) {
-      bulk_wait_all();
-      // after a timeout: no input chunk may land once the CTA has exited
-      for (int ch = in_done; ch < in_issued; ++ch)
-        mbar_wait_bounded(&ib[ch & 1], (unsigned)(ch >> 1) & 1u, ep.status);
-    }
+    EpiState es{0, 0, 0};
+    const int nmain = NACC < nkb ? NACC : nkb;
+    epi_tile<TBN>(maps, ep, t, yrow, n0, lane, smem + warp * EPI_WARP_BYTES, ib,
+                  tmem + ((uint32_t)(warp * 32) << 16), nmain, ACC_COLS,
+                  (uint32_t)NACC * ACC_COLS, es, esum);
+    if (lane == 0) epi_drain(ib, es, ep.status);
     if (ep.kind == EPI_F3) ep.epart[(size_t)(yrow + lane) * ep.ntile_n + blockIdx.x] = esum;
   }
   // ---- drain: no bulk copy of this CTA may land after it exits
@@ -518,6 +560,204 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
                  : "memory");
+}
+
+// Persistent form of k_fit_tc for the layers with one main accumulator (the
+// K-240 layers and B1): one CTA per SM walks the layer's tiles, the N tiles
+// of a row block consecutively so that they run at the same time on
+// neighbouring SMs and share A through L2.  Warp 0 issues the TMA loads,
+// warp 1 the MMAs, warps 2-5 run the epilogue (warp w reads TMEM lanes
+// 32 (w % 4) ..).  Two tensor-memory buffers of (main, cross) accumulators
+// let the MMAs of the next tile run while the epilogue drains the last one.
+constexpr int PERS_TBN = 80, PERS_STAGES = 3;
+constexpr int PERS_STAGE = 2 * A_TILE + 2 * PERS_TBN * TBK * 2;  // 52 KiB
+constexpr int PERS_SMEM = PERS_STAGES * PERS_STAGE + 4 * EPI_WARP_BYTES + 1024 + 256;
+static_assert(PERS_SMEM <= 227 * 1024, "persistent fitting kernel shared memory");
+
+__global__ void __launch_bounds__(192, 1)
+    k_fit_pers(const __grid_constant__ TcMaps maps, const __grid_constant__ TcEpi ep, int K,
+               int ntn, int ntiles) {
+  constexpr int S = PERS_STAGES, STAGE = PERS_STAGE, B_TILE = PERS_TBN * TBK * 2;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* epi = smem + S * STAGE;  // [4 warps][EPI_WARP_BYTES]
+  uint64_t* full = reinterpret_cast<uint64_t*>(epi + 4 * EPI_WARP_BYTES);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;    // [2] accumulator buffer ready
+  uint64_t* tempty = tfull + 2;   // [2] accumulator buffer read (4 epilogue warps)
+  uint64_t* inbar = tempty + 2;   // [4 warps][2]: epilogue input chunks
+  uint64_t* mdone = inbar + 8;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nkb = (K + TBK - 1) / TBK;
+  auto tile_at = [&](int tile, int& row0, int& n0, int& nt, int& t) {
+    const int rb = tile / ntn;
+    nt = tile - rb * ntn;
+    row0 = rb * TBM;
+    n0 = nt * PERS_TBN;
+    t = 0;
+    while (t + 1 < ep.ntypes && row0 >= ep.row_off[t + 1]) ++t;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int j = 0; j < 2; ++j) {
+      mbar_init(&tfull[j], 1);
+      mbar_init(&tempty[j], 4);
+    }
+    for (int b = 0; b < 8; ++b) mbar_init(&inbar[b], 1);
+    mbar_init(mdone, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_addr(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer.  The first tile's first B tiles (weights: no
+      //      dependence on the previous layer) are requested before waiting
+      //      for that layer, its A tiles after.
+      int issued = 0, pre = 0;
+      bool ok = true;
+      if ((int)blockIdx.x < ntiles) {
+        int row0, n0, nt, t;
+        tile_at(blockIdx.x, row0, n0, nt, t);
+        pre = nkb < S ? nkb : S;
+        for (int kb = 0; kb < pre; ++kb) {
+          unsigned char* st = smem + kb * STAGE;
+          mbar_expect_tx(&full[kb], STAGE);
+          tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[kb]);
+          tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[kb]);
+        }
+        griddep_wait();
+        for (int kb = 0; kb < pre; ++kb) {
+          unsigned char* st = smem + kb * STAGE;
+          tma_2d(st, &maps.a_hi, kb * TBK, row0, &full[kb]);
+          tma_2d(st + A_TILE, &maps.a_lo, kb * TBK, row0, &full[kb]);
+        }
+        issued = pre;
+      } else {
+        griddep_wait();
+      }
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+        int row0, n0, nt, t;
+        tile_at(tile, row0, n0, nt, t);
+        for (int kb = (it == 0 ? pre : 0); kb < nkb; ++kb) {
+          const int st_i = issued % S;
+          if (issued >= S &&
+              !mbar_wait_bounded(&empty[st_i], ((issued / S) & 1u) ^ 1u, ep.status)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = smem + st_i * STAGE;
+          mbar_expect_tx(&full[st_i], STAGE);
+          tma_2d(st + 2 * A_TILE, &maps.b_hi[t], kb * TBK, n0, &full[st_i]);
+          tma_2d(st + 2 * A_TILE + B_TILE, &maps.b_lo[t], kb * TBK, n0, &full[st_i]);
+          tma_2d(st, &maps.a_hi, kb * TBK, row0, &full[st_i]);
+          tma_2d(st + A_TILE, &maps.a_lo, kb * TBK, row0, &full[st_i]);
+          ++issued;
+        }
+      }
+      // no bulk copy of this CTA may land after it exits
+      for (int k = (issued > S ? issued - S : 0); k < issued; ++k)
+        mbar_wait_bounded(&full[k % S], (k / S) & 1u, ep.status);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: D(f32) += A(f16, K-major) B(f16, K-major), M 128, N 80
+      const uint32_t idesc =
+          (1u << 4) | ((uint32_t)(PERS_TBN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+      int cons = 0, use[2] = {0, 0}, seen[2] = {0, 0};
+      bool ok = true;
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+        const int j = it & 1;
+        while (ok && seen[j] < use[j]) {
+          ok = mbar_wait_bounded(&tempty[j], seen[j] & 1u, ep.status);
+          ++seen[j];
+        }
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t dm = tmem + (uint32_t)(j * 256), dc = dm + 128u;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int st_i = cons % S;
+          if (!mbar_wait_bounded(&full[st_i], (cons / S) & 1u, ep.status)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ah = smem_addr(smem + st_i * STAGE), al = ah + A_TILE,
+                         bh = ah + 2 * A_TILE, bl = bh + B_TILE;
+#pragma unroll
+          for (int kk = 0; kk < TBK / 16; ++kk) {
+            const uint32_t off = kk * 32;
+            const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off),
+                           dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
+            const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+            umma_f16(dm, dah, dbh, idesc, acc);
+            umma_f16(dc, dal, dbh, idesc, acc);
+            umma_f16(dc, dah, dbl, idesc, 1u);
+          }
+          umma_commit(&empty[st_i]);
+          ++cons;
+        }
+        if (ok) {
+          umma_commit(&tfull[j]);
+          ++use[j];
+        }
+      }
+      // every MMA issued complete before TMEM is released
+      umma_commit(mdone);
+      mbar_wait_bounded(mdone, 0, ep.status);
+    }
+  } else {
+    // ---- epilogue warps: this warp's rows of each tile
+    griddep_wait();  // the previous layer's outputs visible to this thread
+    const int ew = warp - 2, q = warp & 3;
+    unsigned char* wsm = epi + ew * EPI_WARP_BYTES;
+    uint64_t* ib = inbar + ew * 2;
+    EpiState es{0, 0, 0};
+    int seen[2] = {0, 0};
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int j = it & 1;
+      if (!__all_sync(kFull, mbar_wait_bounded(&tfull[j], seen[j] & 1u, ep.status))) break;
+      ++seen[j];
+      tc_fence_after();
+      // the next layer may start filling SMs once this CTA's last tile drains
+      if (tile + (int)gridDim.x >= ntiles) griddep_launch_dependents();
+      int row0, n0, nt, t;
+      tile_at(tile, row0, n0, nt, t);
+      const int yrow = row0 + q * 32;
+      float esum = 0.f;
+      const bool ok = epi_tile<PERS_TBN>(maps, ep, t, yrow, n0, lane, wsm, ib,
+                                         tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(j * 256),
+                                         1, 0u, 128u, es, esum);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[j]);
+      if (ep.kind == EPI_F3) ep.epart[(size_t)(yrow + lane) * ep.ntile_n + nt] = esum;
+      if (!ok) break;
+    }
+    if (lane == 0) epi_drain(ib, es, ep.status);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 }
 
 // per-row energy: e = sum of the F3 partials + b_out; padding rows get 0
@@ -680,12 +920,20 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
                        CfgLongK::SMEM);
   cudaFuncSetAttribute(k_fit_tc<CfgShortK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        CfgShortK::SMEM);
+  cudaFuncSetAttribute(k_fit_pers, cudaFuncAttributeMaxDynamicSharedMemorySize, PERS_SMEM);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 1;
+  }
   GBDP_REQUIRE(rows / TBM <= 65535, "fit_tc: %ld rows exceed the grid limit", rows);
   TcEpi base{};
   base.ntypes = ntypes;
   for (int t = 0; t <= ntypes; ++t) base.row_off[t] = row_off[t];
   base.status = status;
-  base.ntile_n = FIT_W / CfgShortK::TBN;  // F3's N tiles
+  base.ntile_n = FIT_W / PERS_TBN;  // F3's N tiles
   for (int t = 0; t < ntypes; ++t) {
     base.wout[t] = nets[t].w_out;
     base.idt2[t] = nets[t].idt[1];
@@ -695,7 +943,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
     GBDP_REQUIRE(((uintptr_t)nets[t].idt[1] & 15) == 0 && ((uintptr_t)nets[t].idt[2] & 15) == 0,
                  "fit_tc: idt not 16-byte aligned");
   }
-  enum { LONGK = 0, SHORTK };
+  enum { LONGK = 0, SHORTK, PERSIST };
   // act: index into act_scale of the split output (-1: none)
   struct Step {
     int kind;
@@ -708,7 +956,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
     int cfg;
   };
   static_assert(FIT_W % CfgShortK::TBN == 0 && FIT_W % CfgLongK::TBN == 0 &&
-                    FIT_D % CfgShortK::TBN == 0,
+                    FIT_D % PERS_TBN == 0 && CfgShortK::TBN == PERS_TBN,
                 "tile widths must divide the layer widths");
   const Step steps[6] = {
       {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}, 0,
@@ -722,7 +970,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
       {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false, {ws.t1, ws.g2},
        {nullptr, ws.gz1h, ws.gz1l}, 4, SHORTK},
       {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false, {nullptr, nullptr},
-       {dE_dD, nullptr, nullptr}, -1, SHORTK}};
+       {dE_dD, nullptr, nullptr}, -1, PERSIST}};
   for (const Step& sp : steps) {
     TcMaps maps;
     memset(&maps, 0, sizeof(maps));
@@ -733,7 +981,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
       // forward B = W_l^T [out, in]; backward B = W_l [in, out]: both K-major
       const void* bh = sp.fwd ? n.wt_hi[sp.layer] : n.w_hi[sp.layer];
       const void* bl = sp.fwd ? n.wt_lo[sp.layer] : n.w_lo[sp.layer];
-      const int tbn = sp.cfg == LONGK ? CfgLongK::TBN : CfgShortK::TBN;
+      const int tbn = sp.cfg == LONGK ? CfgLongK::TBN : sp.cfg == SHORTK ? CfgShortK::TBN : PERS_TBN;
       rc = make_map(&maps.b_hi[t], bh, sp.N, sp.K, tbn);
       if (!rc) rc = make_map(&maps.b_lo[t], bl, sp.N, sp.K, tbn);
     }
@@ -778,10 +1026,17 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
       lc.gridDim = dim3(sp.N / CfgLongK::TBN, (unsigned)(rows / TBM));
       lc.dynamicSmemBytes = CfgLongK::SMEM;
       le = cudaLaunchKernelEx(&lc, k_fit_tc<CfgLongK>, maps, ep, sp.K);
-    } else {
+    } else if (sp.cfg == SHORTK) {
       lc.gridDim = dim3(sp.N / CfgShortK::TBN, (unsigned)(rows / TBM));
       lc.dynamicSmemBytes = CfgShortK::SMEM;
       le = cudaLaunchKernelEx(&lc, k_fit_tc<CfgShortK>, maps, ep, sp.K);
+    } else {
+      // one CTA per SM walking the layer's tiles
+      const int ntn = sp.N / PERS_TBN, ntiles = ntn * (int)(rows / TBM);
+      lc.gridDim = dim3((unsigned)(ntiles < nsm ? ntiles : nsm));
+      lc.blockDim = dim3(192);
+      lc.dynamicSmemBytes = PERS_SMEM;
+      le = cudaLaunchKernelEx(&lc, k_fit_pers, maps, ep, sp.K, ntn, ntiles);
     }
     if (le != cudaSuccess) return cuda_status(le, "fit_tc gemm launch");
     GBDP_CHECK_LAUNCH("fit_tc gemm");

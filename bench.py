@@ -1031,8 +1031,8 @@ PART_KERNEL = {"env_nlist": "k_nlist_env (+ cell build and ghost fill)",
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
 # of the 12,288-atom step (profiles/k_desc_fwd_bwd_12288.md,
-# profiles/k_fit_tc_12288.md: the six k_fit_tc launches averaged)
-NCU_TRAFFIC = {"desc_bwd": 133.1e6, "desc_fwd": 144.6e6, "fitting_gemm": 63.6e6}
+# profiles/k_fit_tc_12288.md: the six fitting GEMM launches averaged)
+NCU_TRAFFIC = {"desc_bwd": 133.1e6, "desc_fwd": 65.7e6, "fitting_gemm": 40.6e6}
 
 
 def roofline(name, t, nat, cfg, peaks, fit_mode):
@@ -1043,7 +1043,7 @@ def roofline(name, t, nat, cfg, peaks, fit_mode):
         flops = _fit_flops(cfg) * nat
         ach = flops / (ms * 1e-3) / 1e12
         peak = peaks["bf16_tflops"]
-        out = {"kernel": "k_fit_tc" if tc else f"cuBLAS ({fit_mode}) + k_fit_*", "bound": "tensor",
+        out = {"kernel": "k_fit_tc + k_fit_pers" if tc else f"cuBLAS ({fit_mode}) + k_fit_*", "bound": "tensor",
                "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                "traffic": NCU_TRAFFIC.get(name) if tc else None,
                "peak_src": peaks["src"] + " (dense BF16, burst)",

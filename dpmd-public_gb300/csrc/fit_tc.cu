@@ -266,10 +266,6 @@ __device__ __forceinline__ void col_ld16(const float* p, float* v) {
   }
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
 // programmatic dependent launch: wait for the grid this one depends on (all
 // its writes visible); let the dependent grid be scheduled
 __device__ __forceinline__ void griddep_wait() {

@@ -653,7 +653,7 @@ template <typename T>
 void launch_vir_reduce(T* virial, const T* atom_virial, const ProdWs& w, int nall, int nframes,
                        cudaStream_t st) {
   const int nchunk = (nall + kVirChunk - 1) / kVirChunk;
-  if (nchunk == 0) return;  // no atoms: the virial stays at its zero fill
+  if (nchunk == 0) return;  // not reached: callers with no atoms return before
   k_vir_partial<T><<<dim3(nchunk, nframes), 256, 0, st>>>(w.vir_part, atom_virial, nall);
   k_vir_final<T><<<nframes, 32, 0, st>>>(virial, w.vir_part, nchunk);
 }
@@ -670,8 +670,8 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
   GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_force/virial: workspace %zu < %zu", ws_bytes, w.bytes);
   if (force) cudaMemsetAsync(force, 0, sizeof(T) * (size_t)nframes * nall * 3, st);
   if (atom_virial) cudaMemsetAsync(atom_virial, 0, sizeof(T) * (size_t)nframes * nall * 9, st);
-  if (virial) cudaMemsetAsync(virial, 0, sizeof(T) * (size_t)nframes * 9, st);
   if (nframes == 0 || nloc == 0 || nnei == 0) {
+    if (virial) cudaMemsetAsync(virial, 0, sizeof(T) * (size_t)nframes * 9, st);
     GBDP_CHECK_LAUNCH("prod_force/virial");
     return GBDP_OK;
   }
@@ -679,11 +679,15 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
                "prod_force/virial: null input pointer");
   GBDP_REQUIRE(((uintptr_t)net & 15) == 0 && ((uintptr_t)dR & 15) == 0,
                "prod_force/virial: net_deriv and env_deriv must be 16-byte aligned");
+  // every word of `virial` is written below (k_vir_finish, or the fixed-order
+  // reduction), so it needs no zero fill; the double accumulators of the
+  // atomic mode only where a virial is asked for
   if (!det) {
-    cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
+    if (atom_virial) cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
     launch_atomic<T>(force, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
                      nframes, st);
-    if (virial) k_vir_finish<T><<<1, 256, 0, st>>>(virial, w.vir_acc, 9 * nframes);
+    if (virial) k_vir_finish<T><<<(unsigned)((9 * nframes + 255) / 256), 256, 0, st>>>(
+        virial, w.vir_acc, 9 * nframes);
   } else {
     int rc = build_reverse(w, nlist, nloc, nall, nnei, nframes, st);
     if (rc) return rc;
@@ -718,8 +722,8 @@ int prod_virial_impl(T* virial, T* atom_virial, const T* net, const T* dR, const
   GBDP_REQUIRE(ws != nullptr, "prod_virial_a: null workspace");
   GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_virial_a: workspace %zu < %zu", ws_bytes, w.bytes);
   cudaMemsetAsync(atom_virial, 0, sizeof(T) * (size_t)nframes * nall * 9, st);
-  cudaMemsetAsync(virial, 0, sizeof(T) * (size_t)nframes * 9, st);
   if (nframes == 0 || nloc == 0 || nnei == 0) {
+    cudaMemsetAsync(virial, 0, sizeof(T) * (size_t)nframes * 9, st);
     GBDP_CHECK_LAUNCH("prod_virial_a");
     return GBDP_OK;
   }
@@ -730,7 +734,8 @@ int prod_virial_impl(T* virial, T* atom_virial, const T* net, const T* dR, const
     cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
     launch_atomic<T>(nullptr, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
                      nframes, st);
-    k_vir_finish<T><<<1, 256, 0, st>>>(virial, w.vir_acc, 9 * nframes);
+    k_vir_finish<T><<<(unsigned)((9 * nframes + 255) / 256), 256, 0, st>>>(virial, w.vir_acc,
+                                                                             9 * nframes);
   } else {
     int rc = build_reverse(w, nlist, nloc, nall, nnei, nframes, st);
     if (rc) return rc;

@@ -117,3 +117,27 @@ def test_force_autograd_second_order(gb, oracle):
     (f * w).sum().backward()
     go = oracle.prod_force_grad_a(w.cpu().numpy().reshape(-1), emd, nl, nloc, nnei)
     np.testing.assert_allclose(netT.grad.cpu().numpy().reshape(-1), go, atol=1e-10)
+
+
+@pytest.mark.parametrize("det", [False, True])
+def test_many_frames_virial(gb, oracle, det):
+    """40 frames in one call (9 x 40 = 360 virial words, more than one
+    256-thread block): every frame's virial and atom virial against the
+    oracle, nothing left at a zero fill."""
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    nloc, nnei, net, emd, rij, nl = _water_case(gb, oracle, torch.float64, n=2, L=6.2, seed=21)
+    nf = 40
+    rng = np.random.default_rng(3)
+    nets = rng.normal(0, 1, (nf, net.size))
+    natoms = torch.tensor([nloc, nloc, 0, 0], dtype=torch.int32)
+    rep = lambda a: torch.tensor(np.tile(a.reshape(1, -1), (nf, 1)), device=DEV)
+    v, av = ops.prod_virial_se_a_impl(torch.tensor(nets, device=DEV), rep(emd), rep(rij), rep(nl),
+                                      natoms, nnei, 0, det)
+    f = ops.prod_force_se_a_impl(torch.tensor(nets, device=DEV), rep(emd), rep(nl), natoms, nnei,
+                                 0, det)
+    for k in (0, 17, nf - 1):
+        vo, avo = oracle.prod_virial_a(nets[k], emd, rij, nl, nloc, nloc, nnei)
+        fo = oracle.prod_force_a(nets[k], emd, nl, nloc, nloc, nnei)
+        np.testing.assert_allclose(v[k].cpu().numpy(), np.reshape(vo, -1), atol=1e-9, rtol=1e-10)
+        np.testing.assert_allclose(av[k].cpu().numpy(), np.reshape(avo, -1), atol=1e-10, rtol=1e-10)
+        np.testing.assert_allclose(f[k].cpu().numpy(), np.reshape(fo, -1), atol=1e-10, rtol=1e-10)

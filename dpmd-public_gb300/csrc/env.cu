@@ -830,6 +830,7 @@ struct EnvWs {
   int* ext_cnt;
   int* ghost_start;
   void* xs;
+  size_t zero_bytes;  // status .. cell_fill: zeroed before every build
   size_t bytes;
 };
 
@@ -842,11 +843,13 @@ EnvWs carve(const gbdp_nbr_plan& p, void* base, int fp64) {
     off += align256(n);
     return r;
   };
+  // status, cell_count and cell_fill first and adjacent: one zero fill
   w.status = reinterpret_cast<int*>(take(256));
-  w.atom_frame = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
-  w.atom_cell = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
   w.cell_count = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
   w.cell_fill = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
+  w.zero_bytes = off;
+  w.atom_frame = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.atom_cell = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
   w.cell_start = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
   w.bucket = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
   w.cell_atoms = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
@@ -887,9 +890,7 @@ int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_co
   GBDP_REQUIRE(si.nnei > 0, "prod_env_mat_a: sum(sel) must be positive");
   const int nl = plan->nloc_total;
   if (nl == 0) return GBDP_OK;
-  cudaMemsetAsync(w.status, 0, 256, stream);
-  cudaMemsetAsync(w.cell_count, 0, sizeof(int) * plan->ncell_total, stream);
-  cudaMemsetAsync(w.cell_fill, 0, sizeof(int) * plan->ncell_total, stream);
+  cudaMemsetAsync(w.status, 0, w.zero_bytes, stream);
   const int tb = 256;
   k_localize<T><<<(nl + tb - 1) / tb, tb, 0, stream>>>(frames, plan->nframes, nl, coord, atype,
                                                        ext_coord, ext_type, ext_map,

@@ -72,7 +72,8 @@ struct TcCfg {
   static constexpr int STAGE = 2 * A_TILE + 2 * B_TILE;
   static constexpr uint32_t ACC_COLS = TBN <= 128 ? 128 : 256;  // TMEM columns per accumulator
   static constexpr int TMEM_COLS = (NACC + 1) * (int)ACC_COLS;   // NACC main + 1 cross-term
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;       // + alignment slack + barriers
+  static constexpr int COLP = ((5 * TBN * 4) + 127) & ~127;       // per-column epilogue parameters
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + COLP;  // + alignment slack + barriers
   static_assert(TBN % 16 == 0 && TBN <= 256, "tcgen05 M=128 needs N % 16 == 0, N <= 256");
   // CTAs that fit an SM by shared memory must also fit its 512 TMEM columns
   static_assert((228 * 1024 / SMEM) * TMEM_COLS <= 512, "TMEM over-subscribed");
@@ -220,6 +221,48 @@ __device__ __forceinline__ void pack_split16(const float* x, uint32_t* hw, uint3
   }
 }
 
+// Two 16-column TMEM loads (this warp's lanes) with a single wait
+__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float* v, float* w) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%32];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, "
+      "%25, %26, %27, %28, %29, %30, %31}, [%33];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(ta), "r"(tb)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    v[k] = __uint_as_float(r[k]);
+    w[k] = __uint_as_float(r[16 + k]);
+  }
+}
+
+// 16 per-column parameters from shared or global memory (16-byte aligned)
+__device__ __forceinline__ void colp_ld16(const float* p, float* v) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 u = reinterpret_cast<const float4*>(p)[q];
+    v[q * 4] = u.x;
+    v[q * 4 + 1] = u.y;
+    v[q * 4 + 2] = u.z;
+    v[q * 4 + 3] = u.w;
+  }
+}
+
+// The epilogue's per-column parameters of one tile (each pointer at the
+// tile's first column): inverse column scale, bias, time step, the layer-2
+// time step (F3), output weights; unused ones may be null
+struct ColP {
+  const float *cs, *bias, *idt, *idt2, *wout;
+};
+
 // One thread's row (16 halves as 8 words) of a [32 rows][32 B] staging
 // chunk in the TMA 32-byte swizzle: logical 16-byte piece q of row r sits at
 // piece q ^ ((r >> 2) & 1) (address bit 4 XOR bit 7; chunks 256-byte
@@ -254,17 +297,6 @@ __device__ __forceinline__ void row_ld16(const float* chunk, int lane, float* v)
     v[q * 4 + 3] = u.w;
   }
 }
-// 16 per-column parameters (64-byte aligned)
-__device__ __forceinline__ void col_ld16(const float* p, float* v) {
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float4 u = __ldg(reinterpret_cast<const float4*>(p) + q);
-    v[q * 4] = u.x;
-    v[q * 4 + 1] = u.y;
-    v[q * 4 + 2] = u.z;
-    v[q * 4 + 3] = u.w;
-  }
-}
 
 // programmatic dependent launch: wait for the grid this one depends on (all
 // its writes visible); let the dependent grid be scheduled
@@ -292,7 +324,8 @@ template <int TBN>
 __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, int t, int yrow,
                                          int n0, int lane, unsigned char* wsm, uint64_t* ib,
                                          uint32_t tacc, int nmain, uint32_t acc_stride,
-                                         uint32_t cross_off, EpiState& es, float& esum) {
+                                         uint32_t cross_off, const ColP& cp, EpiState& es,
+                                         float& esum) {
   float* inb = reinterpret_cast<float*>(wsm);  // [2 buf][2 arr][chunk]
   unsigned char* outb = wsm + EPI_IN_BYTES;    // [2 buf][o0 | hi | lo]
   const int nin = ep.nin;
@@ -329,18 +362,22 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
     }
     float v[16], w[16];
     const uint32_t ta = tacc + (uint32_t)c0;
-    tmem_ld16(ta, v);
-    for (int a = 1; a < nmain; ++a) {
-      tmem_ld16(ta + (uint32_t)a * acc_stride, w);
+    if (nmain == 1) {
+      tmem_ld16x2(ta, ta + cross_off, v, w);
+    } else {
+      tmem_ld16(ta, v);
+      for (int a = 1; a < nmain; ++a) {
+        tmem_ld16(ta + (uint32_t)a * acc_stride, w);
 #pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] += w[k];
+        for (int k = 0; k < 16; ++k) v[k] += w[k];
+      }
+      tmem_ld16(ta + cross_off, w);
     }
-    tmem_ld16(ta + cross_off, w);
 #pragma unroll
     for (int k = 0; k < 16; ++k) v[k] += w[k];
     const int c = n0 + c0;
     // undo the operand scales (powers of two: exact)
-    col_ld16(ep.cscale[t] + c, w);
+    colp_ld16(cp.cs + c0, w);
 #pragma unroll
     for (int k = 0; k < 16; ++k) v[k] = v[k] * w[k] * rsc;
     float x0[16], x1[16];
@@ -357,11 +394,11 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
       for (int k = 0; k < 16; ++k) o0[k] = v[k];
     } else if (ep.kind == EPI_F1 || ep.kind == EPI_F2 || ep.kind == EPI_F3) {
       float bb[16], id[16], wo[16], i2[16];
-      col_ld16(ep.bias[t] + c, bb);
-      if (ep.kind != EPI_F1) col_ld16(ep.idt[t] + c, id);
+      colp_ld16(cp.bias + c0, bb);
+      if (ep.kind != EPI_F1) colp_ld16(cp.idt + c0, id);
       if (ep.kind == EPI_F3) {
-        col_ld16(ep.wout[t] + c, wo);
-        col_ld16(ep.idt2[t] + c, i2);
+        colp_ld16(cp.wout + c0, wo);
+        colp_ld16(cp.idt2 + c0, i2);
       }
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
@@ -380,8 +417,8 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
     } else {  // B3: x0 = T2; B2: x0 = T1, x1 = G2
       float id[16], wo[16];
       if (ep.kind == EPI_B3) {
-        col_ld16(ep.idt[t] + c, id);
-        col_ld16(ep.wout[t] + c, wo);
+        colp_ld16(cp.idt + c0, id);
+        colp_ld16(cp.wout + c0, wo);
       }
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
@@ -446,6 +483,21 @@ __global__ void __launch_bounds__(128, 1)
   int t = 0;
   while (t + 1 < ep.ntypes && row0 >= ep.row_off[t + 1]) ++t;
   const int nkb = (K + TBK - 1) / TBK;
+  // the tile's per-column epilogue parameters, staged once (weights: no
+  // dependence on the previous layer) so that the epilogue reads them as
+  // shared-memory broadcasts
+  float* colp = reinterpret_cast<float*>(smem + TSTAGES * STAGE + 256);
+  {
+    for (int u = threadIdx.x; u < 5 * TBN; u += blockDim.x) {
+      const int a = u / TBN, c = u - a * TBN;
+      const float* src = a == 0   ? ep.cscale[t]
+                         : a == 1 ? ep.bias[t]
+                         : a == 2 ? ep.idt[t]
+                         : a == 3 ? ep.idt2[t]
+                                  : ep.wout[t];
+      colp[u] = src ? __ldg(src + n0 + c) : 0.f;
+    }
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TSTAGES; ++s) {
@@ -539,9 +591,10 @@ __global__ void __launch_bounds__(128, 1)
     const int yrow = row0 + warp * 32;
     EpiState es{0, 0, 0};
     const int nmain = NACC < nkb ? NACC : nkb;
+    const ColP cp{colp, colp + TBN, colp + 2 * TBN, colp + 3 * TBN, colp + 4 * TBN};
     epi_tile<TBN>(maps, ep, t, yrow, n0, lane, smem + warp * EPI_WARP_BYTES, ib,
                   tmem + ((uint32_t)(warp * 32) << 16), nmain, ACC_COLS,
-                  (uint32_t)NACC * ACC_COLS, es, esum);
+                  (uint32_t)NACC * ACC_COLS, cp, es, esum);
     if (lane == 0) epi_drain(ib, es, ep.status);
     if (ep.kind == EPI_F3) ep.epart[(size_t)(yrow + lane) * ep.ntile_n + blockIdx.x] = esum;
   }
@@ -739,9 +792,10 @@ __global__ void __launch_bounds__(192, 1)
       tile_at(tile, row0, n0, nt, t);
       const int yrow = row0 + q * 32;
       float esum = 0.f;
+      const ColP cp{ep.cscale[t] + n0, nullptr, nullptr, nullptr, nullptr};  // B1: scales only
       const bool ok = epi_tile<PERS_TBN>(maps, ep, t, yrow, n0, lane, wsm, ib,
                                          tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(j * 256),
-                                         1, 0u, 128u, es, esum);
+                                         1, 0u, 128u, cp, es, esum);
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[j]);

@@ -122,9 +122,13 @@ class SeAModel:
     def __init__(self, cfg: mdl.SeAConfig, params: dict, davg: np.ndarray, dstd: np.ndarray,
                  device, dtype=torch.float32, tables=None, table_infos=None, fit_mode="fp32"):
         """fit_mode selects the fitting GEMMs: "fp32" (cuBLAS SGEMM),
-        "tf32x3" (each operand split into a TF32 head and a remainder, three
-        tensor-core products, FP32-level accuracy) or "bf16" (BF16 tensor
-        cores with FP32 accumulation, a stated larger error)."""
+        "tf32x3" (torch GEMMs, each operand split into a TF32 head and a
+        remainder, three tensor-core products, FP32-level accuracy), "bf16"
+        (BF16 tensor cores with FP32 accumulation, a stated larger error),
+        "native-*" (the library's cuBLAS call with that compute type) or
+        "tc-f16x3" (the library's tcgen05 kernels: scaled FP16 hi / lo
+        operand pairs, three MMAs per product, FP32-level accuracy; FP32
+        models with the 1600-240-240-240 fitting net)."""
         if fit_mode not in self.FIT_MODES:
             raise ValueError(f"fit_mode must be one of {self.FIT_MODES}")
         self.fit_mode = fit_mode if dtype == torch.float32 else "fp32"

@@ -4,8 +4,8 @@ against the FP64 composite.
 
 Stated tolerances: per-atom energy and dE/dD within 1e-5 relative to the
 largest magnitude (split products with short tensor-core accumulation
-chains; measured 4.4e-6 to 5.1e-6 and 1.7e-6 on this net); forces
-<= 1e-5 eV/A vs FP64."""
+chains; measured 3.0e-6 and 1.2e-6 on this net); forces <= 1e-5 eV/A vs
+FP64."""
 
 import importlib
 

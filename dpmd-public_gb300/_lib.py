@@ -170,7 +170,9 @@ def set_autotune(on: bool) -> None:
 
 def autotune_report() -> list[str]:
     """One line per tuned shape key: kernel, dtype, sizes, the chosen warps
-    per CTA and the measured milliseconds of 1, 2 and 4 warps."""
+    per CTA (and for the backward the neighbours in flight per 16-lane group)
+    and the measured milliseconds of every choice (forward: 1, 2, 4 warps;
+    backward: 1, 2, 4 warps at 1 neighbour, then at 2).""" 
     lib = load()
     n = lib.gbdp_autotune_report(None, 0)
     buf = ctypes.create_string_buffer(n + 1)

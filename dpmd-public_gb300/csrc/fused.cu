@@ -474,9 +474,9 @@ __host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
 
 // Phase 1 runs 16 lanes per neighbour.
 // NK = ceil(M / 16): outputs per lane in phase 1; NQ = ceil(M / 32); U:
-// neighbours in flight per 16-lane group (measured on the 12,288-atom water
-// step: U = 1 at 7 CTAs per SM is faster than U = 2 at 6).
-constexpr int kBwdU = 1;
+// neighbours in flight per 16-lane group, 1 (28 resident warps) or 2 (more
+// loads in flight per warp, 24 resident warps), chosen by the autotuner
+// together with the warps per CTA (default 1).
 template <typename T, int NQ, int NK, int U, int W>
 __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / W : 1)
     k_desc_bwd(T* __restrict__ force, double* __restrict__ vir_acc,
@@ -869,20 +869,28 @@ int make_tabset(TabSet<T>& ts, const T* const* tables, const T* infos, int ntype
 }
 
 // ------------------------------------------------------------- autotune --
-// Warps per CTA of the fused descriptor kernels (1, 2 or 4 centre atoms per
-// CTA; per-warp shared memory, so only the launch shape changes): a small
-// batch fills more SMs with smaller CTAs.  With autotuning on
-// (gbdp_set_autotune), the first call for a shape key (kernel, dtype, M,
-// nnei, floor(log2 nloc)) that is not under stream capture times every
-// choice with CUDA events on the caller's stream (three runs each, the
-// minimum) and keeps the fastest; later calls with that key use it.  The
-// cache is the library's only mutable global state and sits behind a mutex.
-// Without a tuned entry the choice is 4 warps.
+// Launch shapes of the fused descriptor kernels, as a shape code: bits 0-2
+// the warps per CTA (1, 2 or 4 centre atoms per CTA; per-warp shared memory,
+// so only the launch shape changes: a small batch fills more SMs with
+// smaller CTAs), bits 3-4 for the backward the neighbours in flight per
+// 16-lane group minus one (1 or 2: more loads in flight per warp against
+// fewer resident warps).  With autotuning on (gbdp_set_autotune), the first
+// call for a shape key (kernel, dtype, M, nnei, floor(log2 nloc)) that is
+// not under stream capture times every choice with CUDA events on the
+// caller's stream (three runs each, the minimum) and keeps the fastest;
+// later calls with that key use it.  The cache is the library's only mutable
+// global state and sits behind a mutex.  Without a tuned entry the choice is
+// 4 warps, 1 neighbour in flight.
 enum { kTuneFwd = 0, kTuneBwd = 1 };
-constexpr int kTuneW[3] = {1, 2, 4};
+constexpr int kTuneMax = 6;
+constexpr int kTuneFwdCodes[3] = {1, 2, 4};
+constexpr int kTuneBwdCodes[6] = {1, 2, 4, 1 | 8, 2 | 8, 4 | 8};
+inline int code_warps(int c) { return c & 7; }
+inline int code_nbrs(int c) { return (c >> 3) + 1; }
 struct TuneEntry {
-  int w;
-  float ms[3];
+  int code;
+  int n;
+  float ms[kTuneMax];
 };
 std::mutex g_tune_mu;
 std::map<std::array<int, 5>, TuneEntry> g_tune;
@@ -894,13 +902,13 @@ std::array<int, 5> tune_key(int kid, int tsize, int M, int nnei, int nloc) {
   return {kid, tsize, M, nnei, lg};
 }
 
-int tuned_warps(int kid, int tsize, int M, int nnei, int nloc, int dflt) {
+int tuned_code(int kid, int tsize, int M, int nnei, int nloc, int dflt) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   const auto it = g_tune.find(tune_key(kid, tsize, M, nnei, nloc));
-  return it == g_tune.end() ? dflt : it->second.w;
+  return it == g_tune.end() ? dflt : it->second.code;
 }
 
-// run(w): one whole call with w warps per CTA (0: the tuned or default
+// run(c): one whole call with shape code c (0: the tuned or default
 // choice), returning a status.  Tunes first when that is on and possible.
 template <typename F>
 int tune_run(int kid, int tsize, int M, int nnei, int nloc, cudaStream_t st, F&& run) {
@@ -914,18 +922,21 @@ int tune_run(int kid, int tsize, int M, int nnei, int nloc, cudaStream_t st, F&&
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (!have && cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
         cs == cudaStreamCaptureStatusNone) {
+      const int* codes = kid == kTuneFwd ? kTuneFwdCodes : kTuneBwdCodes;
+      // the FP64 backward is built for one neighbour in flight only
+      const int nc = kid == kTuneFwd ? 3 : (tsize == 4 ? 6 : 3);
       cudaEvent_t e0, e1;
       cudaEventCreate(&e0);
       cudaEventCreate(&e1);
-      TuneEntry te{4, {0.f, 0.f, 0.f}};
+      TuneEntry te{4, nc, {}};
       float best = 1e30f;
       int rc = GBDP_OK;
-      for (int c = 0; c < 3 && rc == GBDP_OK; ++c) {
-        rc = run(kTuneW[c]);  // warm-up
+      for (int c = 0; c < nc && rc == GBDP_OK; ++c) {
+        rc = run(codes[c]);  // warm-up
         float t = 1e30f;
         for (int rep = 0; rep < 3 && rc == GBDP_OK; ++rep) {
           cudaEventRecord(e0, st);
-          rc = run(kTuneW[c]);
+          rc = run(codes[c]);
           cudaEventRecord(e1, st);
           if (cudaEventSynchronize(e1) != cudaSuccess) rc = cuda_status(cudaGetLastError(), "autotune");
           float ms = 0.f;
@@ -935,7 +946,7 @@ int tune_run(int kid, int tsize, int M, int nnei, int nloc, cudaStream_t st, F&&
         te.ms[c] = t;
         if (t < best) {
           best = t;
-          te.w = kTuneW[c];
+          te.code = codes[c];
         }
       }
       cudaEventDestroy(e0);
@@ -1036,7 +1047,7 @@ int desc_fwd(T* X, T* D, void* D_lo, float* D_rs, const T* em, const int* atype,
   GBDP_REQUIRE((size_t)kFWarps * wb <= 200 * 1024,
                "se_a descriptor fwd: nnei %d needs %zu bytes of shared memory", nnei,
                (size_t)kFWarps * wb);
-  if (w == 0) w = tuned_warps(kTuneFwd, sizeof(T), M, nnei, nloc, kFWarps);
+  if (w == 0) w = tuned_code(kTuneFwd, sizeof(T), M, nnei, nloc, kFWarps);
   if (w == 1)
     fwd_dispatch<T, 1>(nqf, wb, st, X, D, D_lo, D_rs, em, atype, drow, ts, nloc, nnei, M, tail_w,
                          tail_lg);
@@ -1061,8 +1072,8 @@ void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, l
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   // the smallest shared-memory carveout that holds the resident CTAs (28
-  // warps): the rest of the unified L1 caches table rows
-  const int per_sm = (28 / W) * (int)(smem + 1024);
+  // warps at U = 1, 24 at U = 2): the rest of the unified L1 caches table rows
+  const int per_sm = ((U == 1 ? 28 : 24) / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
   kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(
@@ -1070,7 +1081,7 @@ void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, l
       geo, ts, rmin, rmax, nloc, nnei, M);
 }
 
-template <typename T, int W>
+template <typename T, int W, int U>
 void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc,
                   long long* force_fx, const T* X,
                   const T* dD, const int* drow, const T* em, const int* nlist_ext,
@@ -1078,7 +1089,7 @@ void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc,
                   BwdGeom geo, const TabSet<T>& ts, T rmin, T rmax, int nloc, int nnei, int M) {
 #define GBDP_BWD_CASE(NKV)                                                                    \
   case NKV:                                                                                   \
-    launch_bwd<T, (NKV + 1) / 2, NKV, kBwdU, W>(wb, st, force, vir_acc, force_fx, X, dD, drow, \
+    launch_bwd<T, (NKV + 1) / 2, NKV, U, W>(wb, st, force, vir_acc, force_fx, X, dD, drow,     \
                                                 em,                                         \
                                                 nlist_ext, ext_coord, ext_map, atype,       \
                                                 inv_std, geo, ts, rmin, rmax, nloc, nnei, M); \
@@ -1092,7 +1103,7 @@ void bwd_dispatch(int nk, size_t wb, cudaStream_t st, T* force, double* vir_acc,
     GBDP_BWD_CASE(6)
     GBDP_BWD_CASE(7)
     default:
-      launch_bwd<T, 4, 8, kBwdU, W>(wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext,
+      launch_bwd<T, 4, 8, U, W>(wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext,
                                     ext_coord,
                                     ext_map, atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
       break;
@@ -1138,16 +1149,33 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
                (size_t)kBWarps * wb);
   const T rmin = (T)rcut_smth, rmax = (T)rcut;
   const int nk = (M + 15) / 16;
-  if (w == 0) w = tuned_warps(kTuneBwd, sizeof(T), M, nnei, nloc, kBWarps);
-  if (w == 1)
-    bwd_dispatch<T, 1>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
-                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
-  else if (w == 2)
-    bwd_dispatch<T, 2>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
-                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
-  else
-    bwd_dispatch<T, 4>(nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map,
-                       atype, inv_std, geo, ts, rmin, rmax, nloc, nnei, M);
+  if (w == 0) w = tuned_code(kTuneBwd, sizeof(T), M, nnei, nloc, kBWarps);
+  // the FP64 backward is built for one neighbour in flight only
+  const bool u2 = sizeof(T) == 4 && code_nbrs(w) == 2;
+#define GBDP_BWD_ARGS                                                                         \
+  nk, wb, st, force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, \
+      inv_std, geo, ts, rmin, rmax, nloc, nnei, M
+  switch (code_warps(w) * (u2 ? -1 : 1)) {
+    case 1:
+      bwd_dispatch<T, 1, 1>(GBDP_BWD_ARGS);
+      break;
+    case 2:
+      bwd_dispatch<T, 2, 1>(GBDP_BWD_ARGS);
+      break;
+    case -1:
+      if constexpr (sizeof(T) == 4) bwd_dispatch<T, 1, 2>(GBDP_BWD_ARGS);
+      break;
+    case -2:
+      if constexpr (sizeof(T) == 4) bwd_dispatch<T, 2, 2>(GBDP_BWD_ARGS);
+      break;
+    case -4:
+      if constexpr (sizeof(T) == 4) bwd_dispatch<T, 4, 2>(GBDP_BWD_ARGS);
+      break;
+    default:
+      bwd_dispatch<T, 4, 1>(GBDP_BWD_ARGS);
+      break;
+  }
+#undef GBDP_BWD_ARGS
   if (force_fx) {
     const size_t nf = 3 * (size_t)nloc;
     k_fx_finish<T><<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(force, force_fx, nf,
@@ -1267,9 +1295,14 @@ extern "C" int gbdp_autotune_report(char* buf, int len) {
       char line[256];
       const auto& k = kv.first;
       const auto& e = kv.second;
-      snprintf(line, sizeof(line), "%s f%d M=%d nnei=%d nloc=2^%d warps=%d ms=%.4f,%.4f,%.4f\n",
-               k[0] == kTuneFwd ? "se_a_descriptor_fwd" : "se_a_descriptor_bwd", 8 * k[1], k[2],
-               k[3], k[4], e.w, e.ms[0], e.ms[1], e.ms[2]);
+      int w = snprintf(line, sizeof(line), "%s f%d M=%d nnei=%d nloc=2^%d warps=%d",
+                       k[0] == kTuneFwd ? "se_a_descriptor_fwd" : "se_a_descriptor_bwd",
+                       8 * k[1], k[2], k[3], k[4], code_warps(e.code));
+      if (k[0] == kTuneBwd) w += snprintf(line + w, sizeof(line) - w, " nbrs=%d", code_nbrs(e.code));
+      w += snprintf(line + w, sizeof(line) - w, " ms=");
+      for (int c = 0; c < e.n; ++c)
+        w += snprintf(line + w, sizeof(line) - w, c ? ",%.4f" : "%.4f", e.ms[c]);
+      snprintf(line + w, sizeof(line) - w, "\n");
       out += line;
     }
   }

@@ -455,12 +455,14 @@ GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream
 
 /* ---- launch-shape autotuning ----------------------------------------------
  * The fused descriptor kernels (the gbdp_se_a_descriptor_ fwd and bwd entry
- * points) run 1, 2 or 4 centre atoms per CTA.  With autotuning on, the first
+ * points) run 1, 2 or 4 centre atoms per CTA, and the FP32 backward 1 or 2
+ * neighbours in flight per 16-lane group.  With autotuning on, the first
  * call for a shape key
  * (kernel, dtype, last_layer_size, nnei, floor(log2 nloc)) that is not under
  * stream capture times every choice on the caller's stream (it synchronises
  * that stream) and keeps the fastest in a mutex-guarded cache; later calls
- * with that key, captured or not, use it.  Off by default (4 per CTA).
+ * with that key, captured or not, use it.  Off by default (4 per CTA, 1
+ * neighbour in flight).
  * No reference counterpart.  gbdp_autotune_report writes one line per tuned
  * key into buf (NUL-terminated, at most len bytes) and returns the full
  * length. */

@@ -200,8 +200,9 @@ def test_reference_model_testcase(mods, dtype, compressed, tol):
 
 def test_autotuned_launch_shape(mods, built):
     """Launch-shape autotuning of the fused descriptor kernels: the first
-    uncaptured call of a new shape times 1, 2 and 4 centres per CTA and keeps
-    the fastest; the step's results do not depend on the choice, and a CUDA
+    uncaptured call of a new shape times 1, 2 and 4 centres per CTA (and for
+    the backward 1 or 2 neighbours in flight per 16-lane group) and keeps the
+    fastest; the step's results do not depend on the choice, and a CUDA
     graph captured afterwards uses the tuned shape."""
     L = __import__("dpmd_public_gb300._lib", fromlist=["x"])
     se_a, mdl, water = mods
@@ -220,6 +221,9 @@ def test_autotuned_launch_shape(mods, built):
     assert {l.split()[0] for l in mine} == {"se_a_descriptor_fwd", "se_a_descriptor_bwd"}, rep
     for l in mine:
         assert int(l.split("warps=")[1].split()[0]) in (1, 2, 4)
+        if l.startswith("se_a_descriptor_bwd"):  # neighbours in flight per 16-lane group
+            assert int(l.split("nbrs=")[1].split()[0]) in (1, 2)
+            assert len(l.split("ms=")[1].split(",")) == 6
     assert torch.allclose(E1, E0, rtol=1e-6, atol=1e-6)
     assert torch.allclose(F1, F0, rtol=1e-5, atol=1e-6)
     g = torch.cuda.CUDAGraph()

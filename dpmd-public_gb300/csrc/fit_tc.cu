@@ -971,13 +971,13 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
   cudaFuncSetAttribute(k_fit_tc<CfgShortK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        CfgShortK::SMEM);
   cudaFuncSetAttribute(k_fit_pers, cudaFuncAttributeMaxDynamicSharedMemorySize, PERS_SMEM);
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
+  // SM count of the device (initialised once, thread-safe)
+  static const int nsm = [] {
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (nsm <= 0) nsm = 1;
-  }
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
   GBDP_REQUIRE(rows / TBM <= 65535, "fit_tc: %ld rows exceed the grid limit", rows);
   TcEpi base{};
   base.ntypes = ntypes;

@@ -26,6 +26,36 @@ def test_library_exports_every_declared_symbol(gb):
     assert sorted(gb._lib.declared_symbols()) == names
 
 
+def _declared_params():
+    """name -> (return type, number of parameters) of every GBDP_API function."""
+    src = open(os.path.join(ROOT, "include", "gbdp.h")).read()
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    out = {}
+    for m in re.finditer(r"GBDP_API\s+([\w\s\*]+?)\b(gbdp_\w+)\s*\(([^;]*?)\)\s*;", src, flags=re.S):
+        ret, name, params = m.group(1).strip(), m.group(2), " ".join(m.group(3).split())
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        out[name] = (ret, n)
+    return out
+
+
+def test_binding_signatures_match_the_header(gb):
+    """Every ctypes signature in the binding has the header's parameter count
+    and a matching return kind, so that an ABI change on one side cannot go
+    unnoticed on the other."""
+    sigs = gb._lib._SIGS
+    decl = _declared_params()
+    assert set(decl) == set(sigs)
+    for name, (ret, n) in decl.items():
+        restype, argtypes = sigs[name]
+        assert len(argtypes) == n, (name, len(argtypes), n)
+        if ret == "void":
+            assert restype is None, name
+        elif ret == "int":
+            assert restype is ctypes.c_int, name
+        elif ret == "size_t":
+            assert restype is ctypes.c_size_t, name
+
+
 def test_version_and_error_string(gb):
     lib = gb._lib.load()
     assert lib.gbdp_version() >= 100

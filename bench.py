@@ -28,6 +28,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -67,14 +68,17 @@ def _stat_frames():
 
 # ---------------------------------------------------------------- clocks --
 class Clocks:
+    """nvidia-smi samples of one GPU's clocks and throttle reasons, every
+    200 ms, into a temporary CSV that the bench parses."""
+
     def __init__(self, index: int):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix=f"clocks_{os.getpid()}_", suffix=".csv")
+        os.close(fd)
         self.index = index
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index),

@@ -1,7 +1,7 @@
 """End-to-end energy / force / virial of the three GPU forms against the FP64
 CPU composite (oracle/composite.py, the reference's op sequence).
 
-Stated tolerances (the spec bar is a force error <= 1e-5 eV/A vs FP64):
+Stated tolerances (the FP32 bar is a force error <= 1e-5 eV/A vs FP64):
   fp64 GPU: |dF| <= 1e-9 eV/A, |dE| / natoms <= 1e-10 eV, |dV| <= 1e-8 eV
   fp32 GPU: |dF| <= 1e-5 eV/A, |dE| / natoms <= 1e-6 eV, |dV| <= 1e-3 eV
 """

@@ -122,3 +122,46 @@ def test_workspace_sizes(gb):
     assert L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 0) > 0
     assert (L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 1)
             > L.load().gbdp_prod_workspace_bytes(1, 192, 192, 138, 0))
+
+
+def test_fitting_tc_argument_errors(gb):
+    """The tensor-core fitting's argument checks run before any device work:
+    a row block that is not 128-aligned, missing column scales, a non-positive
+    activation scale and a null D row-scale array are reported, not raised."""
+    L = gb._lib
+    lib = L.load()
+    nets = (L.FitTcNet * 1)()
+    fake = ctypes.c_void_p(256)  # never dereferenced: the checks fail first
+    for l in range(3):
+        nets[0].w_hi[l] = nets[0].w_lo[l] = nets[0].wt_hi[l] = nets[0].wt_lo[l] = fake
+        nets[0].b[l] = fake
+        nets[0].cs_fwd[l] = nets[0].cs_bwd[l] = fake
+    nets[0].idt[1] = nets[0].idt[2] = nets[0].w_out = fake
+    for a in range(5):
+        nets[0].act_scale[a] = 1.0
+    nrows = (ctypes.c_int * 1)(100)
+    ws = ctypes.c_void_p(512)
+
+    def call(row_off, rscale=fake):
+        ro = (ctypes.c_int * 2)(*row_off)
+        return lib.gbdp_fitting_tc_f32(fake, fake, fake, fake, rscale, 1, nrows, ro, nets, ws,
+                                       ctypes.c_size_t(1 << 30), None)
+
+    assert call([0, 100]) != 0 and b"multiple of 128" in lib.gbdp_last_error()
+    assert call([0, 128], rscale=None) != 0 and b"null argument" in lib.gbdp_last_error()
+    nets[0].act_scale[2] = 0.0
+    assert call([0, 128]) != 0 and b"act_scale" in lib.gbdp_last_error()
+    nets[0].act_scale[2] = 1.0
+    nets[0].cs_bwd[1] = None
+    assert call([0, 128]) != 0 and b"column scales" in lib.gbdp_last_error()
+
+
+def test_descriptor_split_needs_row_scales(gb):
+    lib = gb._lib.load()
+    fake = ctypes.c_void_p(256)
+    sel = (ctypes.c_int * 2)(46, 92)
+    info = (ctypes.c_float * 12)(*([0, 1, 2, 0.1, 0.1, -1] * 2))
+    tabs = (ctypes.c_void_p * 2)(fake, fake)
+    rc = lib.gbdp_se_a_descriptor_fwd_split_f32(fake, fake, fake, None, fake, fake, None, tabs,
+                                               info, 2, sel, 1, 8, 100, 16, None)
+    assert rc != 0 and b"D_rscale" in lib.gbdp_last_error()

@@ -611,8 +611,10 @@ __global__ void __launch_bounds__(128, 1)
                  : "memory");
 }
 
-// Persistent form of k_fit_tc for the layers with one main accumulator (the
-// K-240 layers and B1): one CTA per SM walks the layer's tiles, the N tiles
+// Persistent form of k_fit_tc for a layer with one main accumulator, used for
+// B1 (20 N tiles of 80 per row block: about 12 tiles per SM on the
+// 12,288-row step; the K-240 layers have about two and run faster as two
+// per-tile CTAs per SM): one CTA per SM walks the layer's tiles, the N tiles
 // of a row block consecutively so that they run at the same time on
 // neighbouring SMs and share A through L2.  Warp 0 issues the TMA loads,
 // warp 1 the MMAs, warps 2-5 run the epilogue (warp w reads TMEM lanes

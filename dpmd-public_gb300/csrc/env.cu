@@ -861,13 +861,21 @@ EnvWs carve(const gbdp_nbr_plan& p, void* base, int fp64) {
   return w;
 }
 
+// Shared-memory bytes of k_nlist_env: per warp the candidate keys and the
+// formatted row.
+inline size_t nlist_env_smem(int max_cand, int nnei) {
+  return (size_t)kEnvWarps * max_cand * 9 + (size_t)kEnvWarps * ((nnei + 3) & ~3) * 4;
+}
+
+// Every argument check of the periodic env-mat pipeline that needs no
+// workspace: run before any device work (the allocation-free entry point
+// calls it before it copies its frame table).  Fills the section table.
 template <typename T>
-int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
-               int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
-               const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
-               const gbdp_nbr_frame* frames, float rcut_smth, const int* sel, int ntypes,
-               void* workspace, size_t ws_bytes, cudaStream_t stream) {
-  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a: null plan/frames/workspace");
+int env_check_args(const T* em, const T* em_deriv, const int* nlist, const T* ext_coord,
+                   const int* ext_type, const int* ext_map, const int* ext_nall, const T* coord,
+                   const int* atype, const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
+                   const int* sel, int ntypes, SecInfo* si) {
+  GBDP_REQUIRE(plan, "prod_env_mat_a: null plan");
   GBDP_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, "prod_env_mat_a: ntypes %d out of [1,%d]",
                ntypes, kMaxTypes);
   GBDP_REQUIRE(em && nlist && ext_coord && ext_type && ext_map && ext_nall && coord && atype &&
@@ -875,19 +883,34 @@ int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_co
                "prod_env_mat_a: null required pointer");
   GBDP_REQUIRE(((uintptr_t)em & 15) == 0 && (!em_deriv || ((uintptr_t)em_deriv & 15) == 0),
                "prod_env_mat_a: em / em_deriv must be 16-byte aligned");
+  si->ntypes = ntypes;
+  si->sec[0] = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    GBDP_REQUIRE(sel[t] >= 0, "prod_env_mat_a: negative sel");
+    si->sec[t + 1] = si->sec[t] + sel[t];
+  }
+  si->nnei = si->sec[ntypes];
+  GBDP_REQUIRE(si->nnei > 0, "prod_env_mat_a: sum(sel) must be positive");
+  GBDP_REQUIRE(nlist_env_smem(plan->max_cand, si->nnei) <= 200 * 1024,
+               "prod_env_mat_a: max_cand %d needs too much shared memory", plan->max_cand);
+  return GBDP_OK;
+}
+
+template <typename T>
+int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
+               int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
+               const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
+               const gbdp_nbr_frame* frames, float rcut_smth, const int* sel, int ntypes,
+               void* workspace, size_t ws_bytes, cudaStream_t stream) {
+  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a: null plan/frames/workspace");
+  SecInfo si;
+  const int chk = env_check_args<T>(em, em_deriv, nlist, ext_coord, ext_type, ext_map, ext_nall,
+                                    coord, atype, avg, stdv, plan, sel, ntypes, &si);
+  if (chk) return chk;
   const int fp64 = sizeof(T) == 8;
   EnvWs w = carve(*plan, workspace, fp64);
   GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_env_mat_a: workspace %zu < %zu bytes", ws_bytes,
                w.bytes);
-  SecInfo si;
-  si.ntypes = ntypes;
-  si.sec[0] = 0;
-  for (int t = 0; t < ntypes; ++t) {
-    GBDP_REQUIRE(sel[t] >= 0, "prod_env_mat_a: negative sel");
-    si.sec[t + 1] = si.sec[t] + sel[t];
-  }
-  si.nnei = si.sec[ntypes];
-  GBDP_REQUIRE(si.nnei > 0, "prod_env_mat_a: sum(sel) must be positive");
   const int nl = plan->nloc_total;
   if (nl == 0) return GBDP_OK;
   cudaMemsetAsync(w.status, 0, w.zero_bytes, stream);
@@ -909,9 +932,7 @@ int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_co
       w.ghost_start, ext_coord, ext_type, ext_map,
       static_cast<typename XsOf<T>::type*>(w.xs));
   const int mc = plan->max_cand;
-  const size_t smem = (size_t)kEnvWarps * mc * 9 + (size_t)kEnvWarps * ((si.nnei + 3) & ~3) * 4;
-  GBDP_REQUIRE(smem <= 200 * 1024, "prod_env_mat_a: max_cand %d needs too much shared memory",
-               mc);
+  const size_t smem = nlist_env_smem(mc, si.nnei);
   auto kern = k_nlist_env<T>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
@@ -1131,7 +1152,12 @@ GBDP_ENV_NLIST_ENTRY(double, f64)
 // The last kNoAllocFrameBytes hold the copied frame table.
 namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
-constexpr size_t kNoAllocFrameBytes = size_t(64) << 10;    // 64 KiB (315 frames)
+constexpr size_t kNoAllocFrameBytes = size_t(64) << 10;    // 64 KiB
+// frame records the table holds: 65536 / 280 = 234
+constexpr int kNoAllocMaxFrames = (int)(kNoAllocFrameBytes / sizeof(gbdp_nbr_frame));
+static_assert(sizeof(gbdp_nbr_frame) == 280, "gbdp_nbr_frame layout changed: update the "
+              "documented frame limit of the allocation-free entry point");
+static_assert(kNoAllocMaxFrames == 234, "documented frame limit of the allocation-free entry");
 constexpr int kNoAllocMaxDevices = 64;
 }  // namespace
 
@@ -1143,15 +1169,20 @@ void* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 // Device address of the scratch array for the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
-int noalloc_scratch_address(void** out) {
+// with the device current: again on every call made outside stream capture
+// (so that a context created after cudaDeviceReset gets its own address),
+// and from the per-device cache while `stream` is capturing.
+int noalloc_scratch_address(cudaStream_t stream, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: cudaGetDevice");
   GBDP_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices,
                "prod_env_mat_a_noalloc: device ordinal %d above %d", dev, kNoAllocMaxDevices - 1);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
+  if (cap == cudaStreamCaptureStatusNone || g_noalloc_addr[dev] == nullptr) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_env_noalloc_scratch);
     if (e != cudaSuccess)
@@ -1170,20 +1201,25 @@ extern "C" int gbdp_prod_env_mat_a_noalloc_f32(
     const gbdp_nbr_frame* frames_host, float rcut_smth, const int* sel, int ntypes,
     gbdp_stream stream) {
   GBDP_REQUIRE(plan && frames_host && status, "prod_env_mat_a_noalloc: null plan/frames/status");
+  GBDP_REQUIRE(plan->nframes >= 1 && plan->nframes <= kNoAllocMaxFrames,
+               "prod_env_mat_a_noalloc: %d frames exceed the built-in frame table (%d frames)",
+               plan->nframes, kNoAllocMaxFrames);
   const size_t need = carve(*plan, nullptr, 0).bytes;
   const size_t room = kNoAllocScratchBytes - kNoAllocFrameBytes;
   GBDP_REQUIRE(need <= room,
                "prod_env_mat_a_noalloc: this batch needs %zu scratch bytes, the built-in "
                "scratch holds %zu (use gbdp_prod_env_mat_a_f32 with a workspace)",
                need, room);
-  const size_t fbytes = sizeof(gbdp_nbr_frame) * (size_t)plan->nframes;
-  GBDP_REQUIRE(fbytes <= kNoAllocFrameBytes,
-               "prod_env_mat_a_noalloc: %d frames exceed the built-in frame table (%zu)",
-               plan->nframes, kNoAllocFrameBytes / sizeof(gbdp_nbr_frame));
-  void* base = nullptr;
-  int rc = noalloc_scratch_address(&base);
+  // every check of the launch before the shared frame table is overwritten
+  SecInfo si;
+  int rc = env_check_args<float>(em, em_deriv, nlist, ext_coord, ext_type, ext_map, ext_nall,
+                                 coord, atype, avg, std, plan, sel, ntypes, &si);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  void* base = nullptr;
+  rc = noalloc_scratch_address(st, &base);
+  if (rc) return rc;
+  const size_t fbytes = sizeof(gbdp_nbr_frame) * (size_t)plan->nframes;
   unsigned char* frames_dev = static_cast<unsigned char*>(base) + room;
   cudaError_t e = cudaMemcpyAsync(frames_dev, frames_host, fbytes, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_status(e, "prod_env_mat_a_noalloc: frame table copy");

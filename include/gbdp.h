@@ -220,16 +220,22 @@ GBDP_API int gbdp_prod_env_mat_a_nlist_f64(double* em, double* em_deriv, double*
  * built-in 16 MiB device scratch array that every GPU loading the library
  * holds until exit (enough for a batch of roughly 100k atoms at water
  * density); a batch whose workspace would exceed 16 MiB - 64 KiB, or with
- * more than 315 frames, is rejected with GBDP_ERR_INVALID and a message.
+ * more than 234 frames (the 64 KiB frame table holds 234 records of 280
+ * bytes), is rejected with GBDP_ERR_INVALID and a message before any device
+ * work, as is every argument gbdp_prod_env_mat_a_f32 would reject.
  * The frame table is passed on the HOST (frames_host) and copied into the
- * scratch; `status` is a caller-provided device int that receives the
- * device status word (GBDP_OK or a GBDP_STATUS_* code) in stream order.
- * Other arguments and outputs are those of gbdp_prod_env_mat_a_f32.
- * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture.  All calls share the one array and it keeps
- * the last call's contents (counters are cleared at the start of every
- * call): calls that overlap on the GPU, on any stream, race with each
+ * scratch in stream order; `status` is a caller-provided device int that
+ * receives the device status word (GBDP_OK or a GBDP_STATUS_* code) in
+ * stream order.  Other arguments and outputs are those of
+ * gbdp_prod_env_mat_a_f32.
+ * Every call made outside stream capture looks up the scratch array's
+ * device address for the current device (cudaGetSymbolAddress); a call
+ * under capture reuses the address of the last uncaptured call on that
+ * device, so make one call on each device before capturing.  A captured
+ * call re-reads frames_host on every replay: it must then be pinned host
+ * memory that outlives the graph.  All calls share the one array and it
+ * keeps the last call's contents (counters are cleared at the start of
+ * every call): calls that overlap on the GPU, on any stream, race with each
  * other.  The function itself never calls cudaMalloc or cudaFree. */
 GBDP_API int gbdp_prod_env_mat_a_noalloc_f32(
     float* em, float* em_deriv, float* rij, int* nlist, int* nlist_ext, float* ext_coord,

@@ -25,6 +25,7 @@ Two sources, both read only here (the fixtures travel; the reference does not):
    shuffled order, as an MD engine hands it over.
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
+        (or DPMD_REFERENCE=/path/to/reference python tests/golden/make_golden.py)
 """
 
 from __future__ import annotations
@@ -40,7 +41,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DPMD_REFERENCE", "")
+if __name__ == "__main__" and not os.path.isdir(os.path.join(REF, "source")):
+    sys.exit("make_golden.py: give the reference root as an argument or in DPMD_REFERENCE")
 
 LIB_TESTS = [
     "test_env_mat_a.cc",

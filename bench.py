@@ -1,21 +1,33 @@
 #!/usr/bin/env python
 """Benchmark: MD atom-steps/s of compressed se_e2_a on GB300.
 
-Workload (one "step" = one energy + force + virial evaluation with the
-neighbour list rebuilt): 4096 H2O (12,288 atoms) in a 49.68 A periodic box,
-the 16^3 lattice of the seeded water generator, compressed se_e2_a in FP32
-(rcut 6, rcut_smth 0.5, sel [46, 92], embedding [25, 50, 100] tabulated at
-stride 0.01 / 0.1, extrapolate 5, axis 16, fitting [240, 240, 240]), seeded
-random weights, davg/dstd from 16 seeded 192-atom frames.
+Default workload (the ragged-batch configuration the target is quoted on):
+512 independent water frames with 8..512 molecules each (24..1536 atoms,
+398,850 atoms in all), each in its own cubic box at 1.0 g/cm^3, built by the
+seeded water generator; compressed se_e2_a in FP32 (rcut 6, rcut_smth 0.5,
+sel [46, 92], embedding [25, 50, 100] tabulated at stride 0.01 / 0.1,
+extrapolate 5, axis 16, fitting [240, 240, 240]), seeded random weights,
+davg/dstd from 16 seeded 192-atom frames.  One "step" = energy + force +
+virial of all 512 frames with every neighbour list rebuilt.
 
-  value   chosen form (fused kernels, CUDA graph), inputs resident in HBM
-  e2e     same step through the public API with pinned host coordinates
-          copied in and energy / force / virial copied out every step
-  plain   the uncompressed drop-in (embedding nets as matmuls), eager
+  value   chosen form: all frames packed in one batch, the fused kernels
+          captured in one CUDA graph, inputs resident in HBM
+  e2e     the same step through the public API (se_a.CapturedStep): host
+          coordinates copied in and every frame's energy / force / virial
+          copied out, every step
+  plain   the plain single-frame drop-in (uncompressed embedding as
+          matmuls, operator form, eager), frame by frame over the batch
+The 12,288-atom single frame (4096 H2O, 49.68 A box) is reported under
+"water12k" with its own value, e2e, roofline and operator-kernel numbers.
 Errors are stated against the FP64 CPU composite of the reference's op
-sequence on the same frame.
+sequence on the same frames.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload ragged512|water12k|md786k|train8x192]
+
+With --gpus N > 1 outside a torch.distributed launch, the script re-launches
+itself under torch.distributed.run with N ranks (one GPU each); every rank
+takes its own 512 ragged frames (weak scaling, no collective in the step).
 """
 
 from __future__ import annotations
@@ -38,9 +50,14 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "MD atom-steps/s on 1 GB300, chosen vs plain form at stated force error vs FP64"
-WORKLOAD = ("4096 H2O (12288 atoms), 49.68 A PBC box, compressed se_e2_a FP32, "
-            "nlist rebuilt every step, energy+force+virial")
+WORKLOAD_RAGGED = ("512 ragged water frames, 8-512 molecules each (24-1536 atoms, 398850 atoms), "
+                   "1.0 g/cm3 cubic PBC boxes, compressed se_e2_a FP32, every nlist rebuilt every "
+                   "step, energy+force+virial of all frames in one packed graph-captured step")
+WORKLOAD_12K = ("4096 H2O (12288 atoms), 49.68 A PBC box, compressed se_e2_a FP32, "
+                "nlist rebuilt every step, energy+force+virial")
 N_SIDE, BOX, SEED = 16, 49.68, 20261203
+N_FRAMES, MOL_LO, MOL_HI = 512, 8, 512
+CPU_SAMPLE_FRAMES = 64
 
 
 def _dist():
@@ -50,13 +67,28 @@ def _dist():
     return ws, rank, local
 
 
-def _frame():
+def _pkg():
     from __graft_entry__ import load_package
+
+    return load_package()
+
+
+def _frame():
     import importlib
 
-    load_package()
+    _pkg()
     water = importlib.import_module("dpmd_public_gb300.water")
     return water.water_frame(N_SIDE, BOX, SEED)
+
+
+def _ragged_frames(rank: int = 0):
+    """The 512 ragged frames of one rank (rank 0: the single-GPU workload;
+    rank r > 0 draws its own frames from the same distribution)."""
+    import importlib
+
+    _pkg()
+    water = importlib.import_module("dpmd_public_gb300.water")
+    return water.ragged_frames(N_FRAMES, seed=SEED + 7919 * rank, lo=MOL_LO, hi=MOL_HI)
 
 
 def _stat_frames():
@@ -64,6 +96,53 @@ def _stat_frames():
 
     water = importlib.import_module("dpmd_public_gb300.water")
     return [water.water_frame(4, 12.42, 5000 + s) for s in range(16)]
+
+
+def _by_size(frames, k):
+    """k frame indices spread over the size order (smallest and largest
+    included)."""
+    order = np.argsort([len(f[1]) for f in frames], kind="stable")
+    pick = np.unique(np.round(np.linspace(0, len(order) - 1, k)).astype(int))
+    return [int(order[p]) for p in pick]
+
+
+def _cpu_sample(frames, n: int = CPU_SAMPLE_FRAMES):
+    """A CPU timing sample of n frames evenly spaced in size order (every
+    eighth frame for n = 64 of 512), so that it keeps the batch's size
+    distribution."""
+    order = np.argsort([len(f[1]) for f in frames], kind="stable")
+    step = max(1, len(frames) // n)
+    return [int(i) for i in order[step // 2::step]]
+
+
+def _np_model(m64, cfg):
+    return (cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), m64.tables_np,
+            m64.infos_np)
+
+
+def _cpu_model():
+    """The model of the GPU arms rebuilt on the host alone (oracle env
+    matrix for the statistics), for the CPU-only reference arm."""
+    import importlib
+
+    import oracle as O
+
+    _pkg()
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    cfg = mdl.SeAConfig()
+    params = mdl.init_params(cfg, SEED)
+    ems, ats, mind = [], [], np.inf
+    for c, t, b in _stat_frames():
+        em, emd, rij, nl = O.prod_env_mat_a_pbc(c, t, b, np.zeros((2, cfg.nnei * 4)),
+                                                np.ones((2, cfg.nnei * 4)), cfg.rcut, cfg.rcut_smth,
+                                                list(cfg.sel))
+        ems.append(em)
+        ats.append(t)
+        r = np.linalg.norm(rij.reshape(-1, 3), axis=1)
+        mind = min(mind, r[nl >= 0].min())
+    davg, dstd = mdl.stats_from_env(ems, ats, cfg)
+    tabs, infos = mdl.build_tables(params, davg, dstd, mind, cfg)
+    return cfg, params, davg, dstd, tabs, infos
 
 
 # ---------------------------------------------------------------- clocks --
@@ -147,63 +226,108 @@ class Clocks:
 
 
 # ----------------------------------------------------------- CPU baseline --
-def cpu_baseline(frame, model_np, steps: int = 2, dtype=np.float32, warmup: int = 1):
-    """The reference's CPU op sequence (oracle composite: env mat with the
-    brute-force build, tabulate, BLAS fitting, tabulate grad, force, virial)
-    on the full frame, timed on this host's cores."""
+
+
+# ----------------------------------------------------------- CPU baseline --
+def cpu_time_frames(frames, idx, model_np, passes: int, warmup: int = 1, cell_list=True,
+                    dtype=np.float32):
+    """Seconds per pass of the reference's CPU op sequence (oracle
+    composite: copy_coord, candidate build, format, env mat, tabulate, BLAS
+    fitting, tabulate grad, force, virial) over frames[idx], frame by frame
+    as the reference processes them."""
     import composite
-    import oracle as O
 
     cfg, params, davg, dstd, tabs, infos = model_np
-    c, t, b = frame
-    for _ in range(warmup):
-        composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype)
+    for k in idx[:max(0, warmup)]:
+        c, t, b = frames[k]
+        composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype,
+                                      cell_list=cell_list)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype)
-    dt = (time.perf_counter() - t0) / steps
-    return {"value": len(t) / dt, "unit": "atom-steps/s", "cores": O.num_threads(),
-            "kind": "port", "s_per_step": dt,
-            "sample": f"full 12288-atom frame, {steps} steps after {warmup} warm-up, FP32, "
-                      f"oracle composite of the reference's CPU op sequence"}
+    for _ in range(passes):
+        for k in idx:
+            c, t, b = frames[k]
+            composite.energy_force_virial(cfg, params, davg, dstd, c, t, b, tabs, infos, dtype,
+                                          cell_list=cell_list)
+    return (time.perf_counter() - t0) / passes
+
+
+def cpu_baseline_ragged(frames, model_np, passes: int = 2):
+    """The reference's CPU path on a bounded sample of the ragged batch
+    (64 of the 512 frames, spread over the size order), with its O(N)
+    cell-list neighbour build; the O(N^2) build_nlist_cpu variant alongside."""
+    import oracle as O
+
+    idx = _cpu_sample(frames)
+    nat = sum(len(frames[k][1]) for k in idx)
+    s = cpu_time_frames(frames, idx, model_np, passes)
+    s_bf = cpu_time_frames(frames, idx, model_np, 1, warmup=0, cell_list=False)
+    return {"value": nat / s, "unit": "atom-steps/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{len(idx)} of the 512 frames (every 8th in size order, {nat} atoms), "
+                      f"{passes} passes after 1 warm-up frame, FP32, oracle composite of the "
+                      f"reference's CPU op sequence with the cell-list build_nlist",
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS", "unset"),
+            "cpu_model": _cpu_model_name(),
+            "brute_force_nlist_value": nat / s_bf}
+
+
+def cpu_baseline_12k(frame, model_np, steps: int = 2):
+    import oracle as O
+
+    s = cpu_time_frames([frame], [0], model_np, steps)
+    return {"value": len(frame[1]) / s, "unit": "atom-steps/s", "cores": O.num_threads(),
+            "kind": "port",
+            "sample": f"full 12288-atom frame, {steps} steps after 1 warm-up, FP32, oracle "
+                      f"composite of the reference's CPU op sequence with the cell-list build_nlist"}
+
+
+def _cpu_model_name() -> str:
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                k = line.split(":")[0].strip().lower()
+                if k in ("model name", "cpu part", "hardware"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
 
 
 def reference_arm(args):
+    """The reference's CPU implementation of the path (oracle port of its
+    op sequence, all host threads) on the same workload, metric and unit:
+    each step a bounded sample (the 64-frame sample of the ragged batch, or
+    the full 12,288-atom frame)."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
     import oracle as O
-    from __graft_entry__ import load_package
-    import importlib
 
-    load_package()
-    mdl = importlib.import_module("dpmd_public_gb300.model")
-    cfg = mdl.SeAConfig()
-    params = mdl.init_params(cfg, SEED)
-    frame = _frame()
-    ems, ats, mind = [], [], np.inf
-    for c, t, b in _stat_frames():
-        em, emd, rij, nl = O.prod_env_mat_a_pbc(c, t, b, np.zeros((2, cfg.nnei * 4)),
-                                                np.ones((2, cfg.nnei * 4)), cfg.rcut, cfg.rcut_smth,
-                                                list(cfg.sel))
-        ems.append(em)
-        ats.append(t)
-        r = np.linalg.norm(rij.reshape(-1, 3), axis=1)
-        mind = min(mind, r[nl >= 0].min())
-    davg, dstd = mdl.stats_from_env(ems, ats, cfg)
-    tabs, infos = mdl.build_tables(params, davg, dstd, mind, cfg)
-    # each step is the full frame (about 0.45 s on 16 host cores): K and W as
-    # asked, K capped at 200 so the run stays within a few minutes
+    model_np = _cpu_model()
+    if args.workload == "water12k":
+        frames, idx, workload = [_frame()], [0], WORKLOAD_12K
+        sample = "full 12288-atom frame per step"
+    else:
+        frames = _ragged_frames(0)
+        idx, workload = _cpu_sample(frames, 32), WORKLOAD_RAGGED
+        sample = (f"{len(idx)} of the 512 frames per step (every 16th in size order), "
+                  f"frame by frame")
+    nat = sum(len(frames[k][1]) for k in idx)
     steps = max(1, min(args.steps, 200))
-    cb = cpu_baseline(frame, (cfg, params, davg, dstd, tabs, infos), steps=steps,
-                      warmup=args.warmup)
-    line = {"metric": METRIC, "value": cb["value"], "unit": "atom-steps/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": cb["s_per_step"] * 1e3,
+    cpu_time_frames(frames, idx, model_np, max(1, args.warmup), warmup=0)
+    s = cpu_time_frames(frames, idx, model_np, steps, warmup=0)
+    value = nat / s
+    line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "atoms": len(frame[1]), "form": "reference CPU op sequence"},
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-            "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+            "data": "synthetic (seeded water generator, random-init weights)", "impl": "reference",
+            "config": {"workload": workload, "atoms_per_step": nat,
+                       "form": "reference CPU op sequence (oracle port), cell-list build_nlist"},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": O.num_threads(),
+                             "kind": "port", "sample": f"{sample}, {nat} atoms, FP32",
+                             "cpu_model": _cpu_model_name()},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -220,164 +344,198 @@ def main():
     ap.add_argument("--fit-mode", default=None,
                     choices=["fp32", "tf32x3", "bf16", "native-fp32", "native-bf16x9", "native-tf32",
                              "native-bf16", "tc-f16x3"],
-                    help="fitting net: tc-f16x3 (tcgen05 kernel, scaled FP16 hi/lo split; default on "
-                         "one GPU), torch GEMMs (fp32, split tf32x3, bf16) or the native call with a "
-                         "cuBLAS compute type (native-*; native-bf16x9 is the default when "
+                    help="fitting net: tc-f16x3 (tcgen05 kernel, scaled FP16 hi/lo split; default "
+                         "on one GPU), torch GEMMs (fp32, split tf32x3, bf16) or the native call "
+                         "with a cuBLAS compute type (native-*; native-bf16x9 is the default when "
                          "WORLD_SIZE > 1)")
-    ap.add_argument("--workload", default="water12k",
-                    choices=["water12k", "ragged512", "md786k", "train8x192"],
-                    help="water12k: the headline config; ragged512: 512 ragged frames, batched "
-                         "fused graph vs the plain per-frame loop; md786k: 786,432-atom NVE MD")
+    ap.add_argument("--workload", default="ragged512",
+                    choices=["ragged512", "water12k", "md786k", "train8x192"],
+                    help="ragged512: 512 ragged frames in one packed graph step (the default line, "
+                         "with the 12,288-atom frame as an extra key); water12k: the 12,288-atom "
+                         "frame alone; md786k: 786,432-atom NVE MD; train8x192: training step")
+    ap.add_argument("--no-12k", action="store_true",
+                    help="ragged512: leave out the extra 12,288-atom measurements")
     ap.add_argument("--md-steps", type=int, default=1000)
+    ap.add_argument("--md-skin", type=float, default=2.0,
+                    help="md786k: neighbour-list skin in A (0: rebuild every step)")
+    ap.add_argument("--md-rebuild", type=int, default=10,
+                    help="md786k: steps between neighbour-list rebuilds")
     ap.add_argument("--md-out-scale", type=float, default=0.01,
                     help="md786k: scale of the random fitting output layer (physical force range)")
     ap.add_argument("--profile", action="store_true",
-                    help="profiling run: set up, then 2 fused steps, 1 operator-form step and "
-                         "1 plain tensor-core step between cudaProfilerStart/Stop (for ncu "
-                         "--profile-from-start off)")
+                    help="profiling run: set up, then 2 fused steps between "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--profile-frames", type=int, default=N_FRAMES,
+                    help="--profile with ragged512: frames of the profiled batch (the first k "
+                         "of the 512)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    ws, rank, _ = _dist()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return _relaunch(args.gpus)
     if args.fit_mode is None:
-        # the tensor-core fitting stages operands with TMA, which jobs on two or
-        # more GPUs keep out of: replicas there take the cuBLAS BF16x9 fitting
-        args.fit_mode = "tc-f16x3" if _dist()[0] == 1 else "native-bf16x9"
+        # the tensor-core fitting stages operands with TMA, which jobs on two
+        # or more GPUs keep out of: replicas there take the cuBLAS BF16x9 fitting
+        args.fit_mode = "tc-f16x3" if ws == 1 else "native-bf16x9"
     if args.impl == "reference":
         return reference_arm(args)
-    if args.workload == "ragged512":
-        return ragged_workload(args)
     if args.workload == "md786k":
         return md_workload(args)
     if args.workload == "train8x192":
         return train_workload(args)
+    if args.workload == "water12k":
+        return water12k_main(args)
+    return ragged_main(args)
 
+
+def _relaunch(n: int) -> int:
+    """Run this script under torch.distributed.run with n ranks (one GPU
+    each, rendezvous on 127.0.0.1)."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)]
+    cmd += sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def _init_dist(ws, local):
     import torch
 
-    ws, rank, local = _dist()
     if ws > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    torch.backends.cuda.matmul.allow_tf32 = False
-    torch.backends.cudnn.allow_tf32 = False
+    return torch.device("cuda", local)
 
-    from __graft_entry__ import load_package
+
+def _barrier(ws):
+    import torch
+
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+
+def _max_over_ranks(x: float, ws: int, dev) -> float:
+    import torch
+
+    if ws == 1:
+        return x
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t)
+
+
+def time_captured(step, flush, steps: int, warmup: int, ws: int, clk=None):
+    """Device time per step of a captured step (CUDA events on the launching
+    stream, L2 flushed between steps outside the events); the clock sampler,
+    when given, brackets the timed steps under the same load.  Returns
+    (ms per step, wall seconds of the timed region)."""
+    import torch
+
+    for _ in range(warmup):
+        step.replay()
+    _barrier(ws)
+    st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    if clk is not None:
+        clk.load(step.replay, after_s=None)  # pre-roll until the first clock sample
+        _barrier(ws)
+    wall0 = time.perf_counter()
+    for k in range(steps):
+        flush()
+        st[k].record()
+        step.replay()
+        en[k].record()
+    _barrier(ws)
+    wall = time.perf_counter() - wall0
+    if clk is not None:
+        clk.load(step.replay)  # post-roll under the same load
+    return sum(s.elapsed_time(e) for s, e in zip(st, en)) / steps, wall
+
+
+def time_e2e(step, host_coord, flush, steps: int, ws: int):
+    """The public call with host buffers: pinned host coordinates copied in,
+    the graph replayed, the packed energies / virials / forces copied out,
+    all inside the events of each step."""
+    import torch
+
+    for _ in range(3):
+        step(host_coord)
+    _barrier(ws)
+    st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush()
+        st[k].record()
+        step.h2d(step.h_coord)
+        step.replay()
+        step.d2h()
+        en[k].record()
+    _barrier(ws)
+    return sum(s.elapsed_time(e) for s, e in zip(st, en)) / steps
+
+
+def ragged_main(args):
+    """The default line: 512 ragged frames in one packed, graph-captured
+    fused step."""
     import importlib
 
-    pkg = load_package()
-    pkg.load_library()
-    se_a = importlib.import_module("dpmd_public_gb300.se_a")
-    mdl = importlib.import_module("dpmd_public_gb300.model")
-    L = importlib.import_module("dpmd_public_gb300._lib")
-    L.set_autotune(True)  # launch shapes tuned during the (untimed) warm-up
-    cfg = mdl.SeAConfig()
-    c, t, b = _frame()
-    nat = len(t)
-    m64 = se_a.build_model(cfg, SEED, _stat_frames(), dev, torch.float64)
-    model = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
-                          torch.float32, m64.tables_np, m64.infos_np, fit_mode=args.fit_mode)
-    batch = model.batch([t], b[None])
-    coord = torch.tensor(c, dtype=torch.float32, device=dev)
+    import torch
 
+    ws, rank, local = _dist()
+    dev = _init_dist(ws, local)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    torch.backends.cudnn.allow_tf32 = False
+    se_a, cfg, m64, model, plain = _setup_models(dev, args.fit_mode)
+    L = importlib.import_module("dpmd_public_gb300._lib")
+    frames = _ragged_frames(rank)
     if args.profile:
-        for _ in range(3):
-            model.step_fused(batch, coord)
-        model.step_ops(batch, coord, compressed=True)
-        mpt = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(),
-                            dev, torch.float32, fit_mode=args.fit_mode)
-        bpt = mpt.batch([t], b[None])
-        mpt.step_plain_tc(bpt, coord)
-        torch.cuda.synchronize()
+        frames = frames[:args.profile_frames]
+    nat = sum(len(f[1]) for f in frames)
+    batch = model.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    host_coord = np.concatenate([f[0] for f in frames]).astype(np.float32)
+    step = se_a.CapturedStep(model, batch)
+    step.coord.copy_(torch.from_numpy(host_coord))
+    step.replay()
+    torch.cuda.synchronize()
+    if batch.status() != 0:
+        raise RuntimeError(f"neighbour build status {batch.status()}")
+    if args.profile:
         torch.cuda.profiler.start()
         for _ in range(2):
-            model.step_fused(batch, coord)
-        model.step_ops(batch, coord, compressed=True)
-        mpt.step_plain_tc(bpt, coord)
+            step.replay()
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
-        print(json.dumps({"profile": "ok", "status": batch.status()}))
+        print(json.dumps({"profile": "ok", "frames": len(frames), "atoms": nat,
+                          "status": batch.status()}))
         return 0
-
-    # ---- capture the fused step in a CUDA graph
-    side = torch.cuda.Stream()
-    side.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(side):
-        for _ in range(3):
-            model.step_fused(batch, coord)
-    torch.cuda.current_stream().wait_stream(side)
-    torch.cuda.synchronize()
-    st = batch.status()
-    if st != 0:
-        raise RuntimeError(f"neighbour build status {st}")
-    graph = _new_graph()
-    with torch.cuda.graph(graph):
-        E_g, F_g, V_g = model.step_fused(batch, coord)
-    launches = graph_kernels(graph)
-    if hasattr(graph, "instantiate"):
-        graph.instantiate()
+    launches = graph_kernels(step.graph)
     flush = L2Flush(dev)
-
-    def barrier():
-        if ws > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    for _ in range(args.warmup):
-        graph.replay()
-    barrier()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with Clocks(local) as clk:
-        clk.load(graph.replay, after_s=None)  # pre-roll until the first clock sample
-        barrier()
-        wall0 = time.perf_counter()
-        for k in range(args.steps):
-            flush()  # L2 flush between timed steps, outside the events
-            starts[k].record()
-            graph.replay()
-            ends[k].record()
-        barrier()
-        wall = time.perf_counter() - wall0
-        clk.load(graph.replay)  # post-roll under the same load
-    step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
-    if ws > 1:
-        tt = torch.tensor([step_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(tt)
+        step_ms, wall = time_captured(step, flush, args.steps, args.warmup, ws, clk)
+    step_ms = _max_over_ranks(step_ms, ws, dev)
     value = ws * nat / (step_ms * 1e-3)
     if batch.status() != 0:
         raise RuntimeError("neighbour build reported a device status during the timed steps")
+    E_dev = batch.energy.clone()
+    V_dev = batch.vir.clone()
+    F_dev = batch.force.clone()
 
-    # ---- e2e through the public API: pinned host coords in, E/F/V out
-    h_coord = torch.tensor(c, dtype=torch.float32).pin_memory()
-    # E, V and F live in one device buffer (batch.out): one D2H copy a step
-    h_out = torch.empty(batch.out.numel(), dtype=torch.uint8).pin_memory()
-    e_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    for _ in range(3):
-        coord.copy_(h_coord, non_blocking=True)
-        graph.replay()
-    barrier()
-    for k in range(args.steps):
-        flush()
-        e_st[k].record()
-        coord.copy_(h_coord, non_blocking=True)
-        graph.replay()
-        h_out.copy_(batch.out, non_blocking=True)
-        e_en[k].record()
-    barrier()
-    e2e_ms = sum(s.elapsed_time(e) for s, e in zip(e_st, e_en)) / args.steps
-    if ws > 1:
-        tt = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt)
+    e2e_ms = _max_over_ranks(time_e2e(step, host_coord, flush, args.steps, ws), ws, dev)
     e2e = {"value": ws * nat / (e2e_ms * 1e-3), "unit": "atom-steps/s",
-           "h2d_bytes_per_step": h_coord.numel() * 4,
-           "d2h_bytes_per_step": h_out.numel()}
+           "h2d_bytes_per_step": step.h_coord.numel() * step.h_coord.element_size(),
+           "d2h_bytes_per_step": step.h_out.numel()}
+    # the e2e outputs are the resident step's outputs (same coordinates)
+    same = bool(torch.equal(step.h_force, F_dev.cpu()))
 
-    # ---- per-kernel times of the fused step (eager, events on the stream)
-    kt = kernel_times(model, batch, coord, flush, reps=max(3, min(args.steps, 10)))
+    reps = max(3, min(args.steps, 10))
+    kt = kernel_times(model, batch, step.coord, flush, reps=reps)
     dom = max(kt, key=lambda k: kt[k]["ms"])
     peaks = _peaks()
     roof = roofline(dom, kt[dom], nat, cfg, peaks, args.fit_mode)
@@ -387,97 +545,246 @@ def main():
         roof_parts[k] = {x: rp[x] for x in ("kernel", "bound", "achieved", "unit", "frac",
                                             "ms_per_launch", "launches", "traffic") if x in rp}
 
-    opk = op_kernel_times(model, batch, coord, flush, peaks, reps=max(3, min(args.steps, 10)))
-
-    # ---- the same step with floating-point atomic sums (the FP32 default is
-    #      the deterministic fixed-point mode), graph-replayed
-    side = torch.cuda.Stream()
-    side.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(side):
-        for _ in range(2):
-            model.step_fused(batch, coord, deterministic=False)
-    torch.cuda.current_stream().wait_stream(side)
+    # the plain single-frame drop-in, frame by frame over the same batch
+    pb = [(plain.batch([f[1]], f[2][None]), torch.tensor(f[0], dtype=torch.float32, device=dev))
+          for f in frames]
+    for b_, c_ in pb[:8]:
+        plain.step_ops(b_, c_, compressed=False)
     torch.cuda.synchronize()
-    gdet = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(gdet):
-        model.step_fused(batch, coord, deterministic=False)
-    for _ in range(3):
-        gdet.replay()
-    det_ts = []
-    for _ in range(max(3, min(args.steps, 10))):
-        flush()
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record()
-        gdet.replay()
-        s1.record()
-        torch.cuda.synchronize()
-        det_ts.append(s0.elapsed_time(s1))
-    det_ms = statistics.median(det_ts)
-    del gdet
-
-    # ---- plain (uncompressed) drop-in, eager, same frame
-    mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
-                       torch.float32)
-    for _ in range(2):
-        mp.step_ops(batch, coord, compressed=False)
+    t0 = time.perf_counter()
+    for b_, c_ in pb:
+        plain.step_ops(b_, c_, compressed=False)
     torch.cuda.synchronize()
-    p0 = time.perf_counter()
-    n_plain = max(2, min(args.steps, 5))
-    for _ in range(n_plain):
-        Ep, Fp, Vp = mp.step_ops(batch, coord, compressed=False)
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    # the same drop-in with the compressed tables (tabulate_fusion_se_a op)
+    cb = [(model.batch([f[1]], f[2][None]), c_) for f, (_, c_) in zip(frames, pb)]
+    for b_, c_ in cb[:8]:
+        model.step_ops(b_, c_, compressed=True)
     torch.cuda.synchronize()
-    plain_ms = (time.perf_counter() - p0) / n_plain * 1e3
+    t0 = time.perf_counter()
+    for b_, c_ in cb:
+        model.step_ops(b_, c_, compressed=True)
+    torch.cuda.synchronize()
+    comp_ms = (time.perf_counter() - t0) * 1e3
+    del pb, cb
 
-    plain_tc = plain_tc_times(se_a, cfg, m64, args.fit_mode, t, b, coord, flush, ws)
+    tos = type_one_side_false(se_a, cfg, frames, dev, args, flush)
 
     out = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded water generator, random-init weights)",
-           "config": {"workload": WORKLOAD, "atoms": nat,
-                      "form": "fused compressed, CUDA graph, deterministic (fixed-point) sums",
-                      "fitting_gemm": args.fit_mode,
-                      "l2": L2Flush.DESC, "parallelism": f"replicas x{ws}",
+           "config": {"workload": WORKLOAD_RAGGED, "frames": len(frames), "atoms": nat,
+                      "form": "fused compressed, all frames packed in one CUDA graph, "
+                              "deterministic (fixed-point) sums",
+                      "fitting_gemm": args.fit_mode, "l2": L2Flush.DESC,
+                      "parallelism": f"replicas x{ws} (each rank its own 512 frames)",
                       "wall_s": wall},
            "e2e": e2e,
            "gpu_launches": None if launches is None else launches["ours"] * args.steps,
            "graph_kernels_per_step": launches,
-           "plain": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                     "form": "uncompressed drop-in (env op + matmul embedding + autograd + force/virial ops), eager"},
-           "plain_tc": plain_tc,
-           "atomic_sums": {"value": ws * nat / (det_ms * 1e-3), "ms_per_step": det_ms,
-                           "form": "the fused step with floating-point atomic force / virial / "
-                                   "energy sums instead of the default fixed-point (bitwise "
-                                   "reproducible) sums, CUDA graph"},
+           "plain_per_frame": {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                               "form": "plain single-frame drop-in: uncompressed operator form "
+                                       "(env op, embedding matmuls, autograd, force/virial ops), "
+                                       "eager, one frame at a time"},
+           "chosen_over_plain": plain_ms / step_ms,
+           "compressed_per_frame": {"value": ws * nat / (comp_ms * 1e-3), "ms_per_step": comp_ms,
+                                    "form": "compressed operator form (tabulate_fusion_se_a), "
+                                            "eager, one frame at a time"},
+           "chosen_over_compressed_per_frame": comp_ms / step_ms,
+           "type_one_side_false": tos,
            "kernels_ms": {k: v["ms"] for k, v in kt.items()},
-           "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
+           "roofline": roof, "roofline_parts": roof_parts,
            "autotune": L.autotune_report(),
-           "clocks": clk.summary()}
+           "clocks": clk.summary(),
+           "e2e_outputs_equal_resident": same}
     if rank == 0:
-        import oracle as O
         import composite
 
-        np_model = (cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), m64.tables_np,
-                    m64.infos_np)
-        E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t, b, np_model[4], np_model[5])
-        Fn = F_g.detach().cpu().numpy().astype(np.float64)
+        np_model = _np_model(m64, cfg)
+        errs = []
+        for k in _by_size(frames, 8):
+            c, t, b = frames[k]
+            a0 = int(batch.plan.atom_off[k])
+            n = len(t)
+            E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t, b, np_model[4],
+                                                             np_model[5], cell_list=True)
+            Fn = F_dev[a0:a0 + n].cpu().numpy().astype(np.float64)
+            errs.append({"frame": k, "atoms": n,
+                         "force_max_abs_eV_per_A": float(np.abs(Fn - F64).max()),
+                         "energy_per_atom_eV": abs(float(E_dev[k]) - E64) / n,
+                         "virial_max_abs_eV": float(np.abs(V_dev[k].cpu().numpy() - V64).max())})
         out["errors_vs_fp64"] = {
-            "force_max_abs_eV_per_A": float(np.abs(Fn - F64).max()),
-            "force_rms_eV_per_A": float(np.sqrt(((Fn - F64) ** 2).mean())),
-            "energy_per_atom_eV": abs(float(E_g[0]) - E64) / nat,
-            "virial_max_abs_eV": float(np.abs(V_g[0].cpu().numpy() - V64).max()),
-            "plain_force_max_abs_eV_per_A": float(np.abs(Fp.detach().cpu().numpy() - F64).max()),
-            "plain_tc_force_max_abs_eV_per_A_vs_plain_fp64": plain_tc.pop("_force_err_fn")(
-                composite, np_model, c, t, b),
-            "reference": "FP64 CPU composite (oracle) of the compressed model"}
+            "force_max_abs_eV_per_A": max(e["force_max_abs_eV_per_A"] for e in errs),
+            "energy_per_atom_eV": max(e["energy_per_atom_eV"] for e in errs),
+            "virial_max_abs_eV": max(e["virial_max_abs_eV"] for e in errs),
+            "frames": errs,
+            "reference": "FP64 CPU composite (oracle) of the compressed model, 8 frames spread "
+                         "over the size order (smallest and largest included)"}
         if not args.no_cpu:
-            out["cpu_baseline"] = {k: v for k, v in cpu_baseline((c, t, b), np_model, steps=2).items()
-                                   if k != "s_per_step"}
+            out["cpu_baseline"] = cpu_baseline_ragged(frames, np_model)
+    if not args.no_12k:
+        del step
+        out["water12k"] = water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, flush,
+                                       full=False)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def type_one_side_false(se_a, cfg, frames, dev, args, flush):
+    """The reference's argcheck default type_one_side = False (one table per
+    (neighbour type, centre type) pair: four tables) on the same ragged
+    batch: step time and the force error of the largest frame vs FP64."""
+    import dataclasses
+
+    import torch
+
+    import composite
+
+    cfg2 = dataclasses.replace(cfg, type_one_side=False)
+    m64 = se_a.build_model(cfg2, SEED, _stat_frames(), dev, torch.float64)
+    m = se_a.SeAModel(cfg2, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
+                      torch.float32, m64.tables_np, m64.infos_np, fit_mode=args.fit_mode)
+    b = m.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    step = se_a.CapturedStep(m, b)
+    step.coord.copy_(torch.from_numpy(np.concatenate([f[0] for f in frames]).astype(np.float32)))
+    ms, _ = time_captured(step, flush, max(3, min(args.steps, 10)), 3, 1)
+    k = _by_size(frames, 2)[-1]
+    c, t, bx = frames[k]
+    a0 = int(b.plan.atom_off[k])
+    np_model = _np_model(m64, cfg2)
+    E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t, bx, np_model[4],
+                                                     np_model[5], cell_list=True)
+    err = float(np.abs(b.force[a0:a0 + len(t)].cpu().numpy().astype(np.float64) - F64).max())
+    nat = sum(len(f[1]) for f in frames)
+    return {"value": nat / (ms * 1e-3), "ms_per_step": ms, "tables": len(m64.tables_np),
+            "force_max_abs_eV_per_A_largest_frame": err,
+            "form": "as the headline (fused, one packed CUDA graph) with type_one_side = False"}
+
+
+def water12k_main(args):
+    import torch
+
+    ws, rank, local = _dist()
+    dev = _init_dist(ws, local)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    torch.backends.cudnn.allow_tf32 = False
+    se_a, cfg, m64, model, _ = _setup_models(dev, args.fit_mode)
+    out = water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, L2Flush(dev), full=True)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, flush, full: bool):
+    """The 12,288-atom single frame: value, e2e, per-part times and roofline,
+    the operator-contract kernels' HBM fractions, errors vs FP64; with
+    ``full`` also the atomic-sum variant, the plain forms and the CPU
+    baseline (a line of its own)."""
+    import importlib
+
+    import torch
+
+    L = importlib.import_module("dpmd_public_gb300._lib")
+    c, t, b = _frame()
+    nat = len(t)
+    batch = model.batch([t], b[None])
+    step = se_a.CapturedStep(model, batch)
+    step.coord.copy_(torch.tensor(c, dtype=torch.float32))
+    step.replay()
+    torch.cuda.synchronize()
+    if batch.status() != 0:
+        raise RuntimeError(f"neighbour build status {batch.status()}")
+    launches = graph_kernels(step.graph)
+    with Clocks(local) as clk:
+        step_ms, wall = time_captured(step, flush, args.steps, args.warmup, ws, clk)
+    step_ms = _max_over_ranks(step_ms, ws, dev)
+    E_g, F_g, V_g = batch.energy.clone(), batch.force.clone(), batch.vir.clone()
+    host_coord = c.astype(np.float32)
+    e2e_ms = _max_over_ranks(time_e2e(step, host_coord, flush, args.steps, ws), ws, dev)
+    e2e = {"value": ws * nat / (e2e_ms * 1e-3), "unit": "atom-steps/s",
+           "h2d_bytes_per_step": step.h_coord.numel() * 4, "d2h_bytes_per_step": step.h_out.numel()}
+    reps = max(3, min(args.steps, 10))
+    kt = kernel_times(model, batch, step.coord, flush, reps=reps)
+    dom = max(kt, key=lambda k: kt[k]["ms"])
+    peaks = _peaks()
+    roof = roofline(dom, kt[dom], nat, cfg, peaks, args.fit_mode)
+    roof_parts = {}
+    for k in kt:
+        rp = roofline(k, kt[k], nat, cfg, peaks, args.fit_mode)
+        roof_parts[k] = {x: rp[x] for x in ("kernel", "bound", "achieved", "unit", "frac",
+                                            "ms_per_launch", "launches", "traffic") if x in rp}
+    opk = op_kernel_times(model, batch, step.coord, flush, peaks, reps=reps)
+    out = {"metric": METRIC, "value": ws * nat / (step_ms * 1e-3), "unit": "atom-steps/s",
+           "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded water generator, random-init weights)",
+           "config": {"workload": WORKLOAD_12K, "atoms": nat,
+                      "form": "fused compressed, CUDA graph, deterministic (fixed-point) sums",
+                      "fitting_gemm": args.fit_mode, "l2": L2Flush.DESC,
+                      "parallelism": f"replicas x{ws}", "wall_s": wall},
+           "e2e": e2e,
+           "gpu_launches": None if launches is None else launches["ours"] * args.steps,
+           "graph_kernels_per_step": launches,
+           "kernels_ms": {k: v["ms"] for k, v in kt.items()},
+           "roofline": roof, "roofline_parts": roof_parts, "op_kernels": opk,
+           "clocks": clk.summary()}
+    Fp = None
+    if full:
+        # the same step with floating-point atomic sums
+        s2 = se_a.CapturedStep(model, batch, deterministic=False)
+        s2.coord.copy_(step.coord)
+        det_ms, _ = time_captured(s2, flush, reps, 3, 1)
+        del s2
+        out["atomic_sums"] = {"value": ws * nat / (det_ms * 1e-3), "ms_per_step": det_ms,
+                              "form": "the fused step with floating-point atomic force / virial / "
+                                      "energy sums instead of the default fixed-point (bitwise "
+                                      "reproducible) sums, CUDA graph"}
+        mp = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
+                           torch.float32)
+        for _ in range(2):
+            mp.step_ops(batch, step.coord, compressed=False)
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        n_plain = max(2, min(args.steps, 5))
+        for _ in range(n_plain):
+            Ep, Fp, Vp = mp.step_ops(batch, step.coord, compressed=False)
+        torch.cuda.synchronize()
+        plain_ms = (time.perf_counter() - p0) / n_plain * 1e3
+        out["plain"] = {"value": ws * nat / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                        "form": "uncompressed drop-in (env op + matmul embedding + autograd + "
+                                "force/virial ops), eager"}
+        out["plain_tc"] = plain_tc_times(se_a, cfg, m64, args.fit_mode, t, b, step.coord, flush, ws)
+    if rank == 0:
+        import composite
+
+        np_model = _np_model(m64, cfg)
+        E64, F64, V64, _ = composite.energy_force_virial(*np_model[:4], c, t, b, np_model[4],
+                                                         np_model[5], cell_list=True)
+        Fn = F_g.cpu().numpy().astype(np.float64)
+        out["errors_vs_fp64"] = {
+            "force_max_abs_eV_per_A": float(np.abs(Fn - F64).max()),
+            "force_rms_eV_per_A": float(np.sqrt(((Fn - F64) ** 2).mean())),
+            "energy_per_atom_eV": abs(float(E_g[0]) - E64) / nat,
+            "virial_max_abs_eV": float(np.abs(V_g[0].cpu().numpy() - V64).max()),
+            "reference": "FP64 CPU composite (oracle) of the compressed model"}
+        if full:
+            errs = out["errors_vs_fp64"]
+            errs["plain_force_max_abs_eV_per_A"] = float(np.abs(Fp.detach().cpu().numpy() - F64).max())
+            errs["plain_tc_force_max_abs_eV_per_A_vs_plain_fp64"] = out["plain_tc"].pop(
+                "_force_err_fn")(composite, np_model, c, t, b)
+            if not args.no_cpu:
+                out["cpu_baseline"] = cpu_baseline_12k((c, t, b), np_model)
+    if not full:
+        for k in ("metric", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling",
+                  "vs_baseline", "dtype", "data"):
+            out.pop(k, None)
+    return out
 
 
 def _setup_models(dev, fit_mode):
@@ -563,67 +870,6 @@ def train_workload(args):
                "grad_cosine_vs_fp32": float((g16.double() @ g32.double())
                                             / (g16.double().norm() * g32.double().norm())),
                "grad_max_abs_diff_vs_fp32": float((g16 - g32).abs().max())}}
-    print(json.dumps(out))
-    return 0
-
-
-def ragged_workload(args):
-    """512 independent water frames with 8..512 molecules each: one packed,
-    graph-captured fused step vs the plain (uncompressed) drop-in run frame
-    by frame."""
-    import importlib
-
-    import torch
-
-    torch.backends.cuda.matmul.allow_tf32 = False
-    dev = torch.device("cuda", 0)
-    se_a, cfg, m64, model, plain = _setup_models(dev, args.fit_mode)
-    water = importlib.import_module("dpmd_public_gb300.water")
-    frames = water.ragged_frames(512, seed=SEED, lo=8, hi=512)
-    nat = sum(len(f[1]) for f in frames)
-    batch = model.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
-    coord = torch.tensor(np.concatenate([f[0] for f in frames]), dtype=torch.float32, device=dev)
-    s = torch.cuda.Stream()
-    s.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(s):
-        for _ in range(3):
-            model.step_fused(batch, coord)
-    torch.cuda.current_stream().wait_stream(s)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        model.step_fused(batch, coord)
-    for _ in range(args.warmup):
-        g.replay()
-    torch.cuda.synchronize()
-    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    st.record()
-    for _ in range(args.steps):
-        g.replay()
-    en.record()
-    torch.cuda.synchronize()
-    fused_ms = st.elapsed_time(en) / args.steps
-    assert batch.status() == 0
-    # plain per-frame loop (one pass over all 512 frames per step)
-    pb = [(plain.batch([f[1]], f[2][None]), torch.tensor(f[0], dtype=torch.float32, device=dev))
-          for f in frames]
-    for b_, c_ in pb[:8]:
-        plain.step_ops(b_, c_, compressed=False)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for b_, c_ in pb:
-        plain.step_ops(b_, c_, compressed=False)
-    torch.cuda.synchronize()
-    plain_ms = (time.perf_counter() - t0) * 1e3
-    out = {"metric": METRIC, "value": nat / (fused_ms * 1e-3), "unit": "atom-steps/s", "n_gpus": 1,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": fused_ms,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic", "config": {
-               "workload": "512 ragged water frames, 8-512 molecules each (24-1536 atoms), "
-                           "1.0 g/cm3, compressed FP32, one packed graph-captured step",
-               "atoms": nat, "frames": 512, "fitting_gemm": args.fit_mode},
-           "plain_per_frame": {"value": nat / (plain_ms * 1e-3), "ms_per_step": plain_ms},
-           "chosen_over_plain": plain_ms / fused_ms,
-           "autotune": sys.modules["dpmd_public_gb300._lib"].autotune_report()}
     print(json.dumps(out))
     return 0
 
@@ -1033,10 +1279,14 @@ def _fit_flops(cfg):
 PART_KERNEL = {"env_nlist": "k_nlist_env (+ cell build and ghost fill)",
                "desc_fwd": "k_desc_fwd", "desc_bwd": "k_desc_bwd"}
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
-# of the 12,288-atom step (profiles/k_desc_fwd_bwd_12288.md,
-# profiles/k_fit_tc_12288.md: the six fitting GEMM launches averaged)
-NCU_TRAFFIC = {"desc_bwd": 133.1e6, "desc_fwd": 65.7e6, "fitting_gemm": 40.6e6}
+# dram__bytes_read.sum + dram__bytes_write.sum per local atom, from one ncu
+# capture of the 12,288-atom step (profiles/k_desc_fwd_bwd_12288.md,
+# profiles/k_fit_tc_12288.md: the six fitting GEMM launches summed), scaled
+# to a launch by the atoms it processes (the traffic of these kernels grows
+# in proportion to the atoms)
+NCU_TRAFFIC_ATOM = {"desc_bwd": 133.1e6 / 12288, "desc_fwd": 65.7e6 / 12288,
+                    "fitting_gemm": 6 * 40.6e6 / 12288}
+NCU_TRAFFIC_SRC = "ncu capture of the 12,288-atom step, scaled by atoms"
 
 
 def roofline(name, t, nat, cfg, peaks, fit_mode):
@@ -1049,7 +1299,8 @@ def roofline(name, t, nat, cfg, peaks, fit_mode):
         peak = peaks["bf16_tflops"]
         out = {"kernel": "k_fit_tc + k_fit_pers" if tc else f"cuBLAS ({fit_mode}) + k_fit_*", "bound": "tensor",
                "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-               "traffic": NCU_TRAFFIC.get(name) if tc else None,
+               "traffic": NCU_TRAFFIC_ATOM[name] * nat / nl if tc else None,
+               "traffic_src": NCU_TRAFFIC_SRC if tc else None,
                "peak_src": peaks["src"] + " (dense BF16, burst)",
                "alg_flops_per_launch": flops / nl, "launches": nl, "ms_per_launch": ms / nl}
         if tc:
@@ -1061,7 +1312,9 @@ def roofline(name, t, nat, cfg, peaks, fit_mode):
     ach = alg / (ms * 1e-3) / 1e9
     return {"kernel": PART_KERNEL.get(name, name), "bound": "hbm", "achieved": ach,
             "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-            "traffic": NCU_TRAFFIC.get(name), "peak_src": peaks["src"],
+            "traffic": (NCU_TRAFFIC_ATOM[name] * nat) if name in NCU_TRAFFIC_ATOM else None,
+            "traffic_src": NCU_TRAFFIC_SRC if name in NCU_TRAFFIC_ATOM else None,
+            "peak_src": peaks["src"],
             "alg_bytes_per_launch": alg, "launches": 1, "ms_per_launch": ms}
 
 

@@ -833,6 +833,74 @@ class Batch:
         return L.load().gbdp_env_status(_ptr(self.plan.workspace), _stream())
 
 
+class CapturedStep:
+    """The chosen form's step for one batch, captured once in a CUDA graph.
+
+    ``replay()`` runs the step on the coordinates already in ``coord`` (a
+    device buffer); calling the object with host coordinates [nloc_total, 3]
+    copies them in, replays the graph and copies the packed outputs back
+    into one pinned host buffer, returning host views (E [nframes] f64,
+    F [nloc_total, 3], virial [nframes, 9] f64) that stay valid until the
+    next call.  The graph reads and writes fixed buffers, so the batch and
+    the model must outlive this object."""
+
+    def __init__(self, model: SeAModel, b: "Batch", warmup: int = 3, deterministic=None):
+        self.model, self.batch = model, b
+        dev = model.device
+        self.coord = torch.zeros((b.nloc, 3), dtype=model.dtype, device=dev)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(max(1, warmup)):
+                model.step_fused(b, self.coord, deterministic)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        try:
+            self.graph = torch.cuda.CUDAGraph(keep_graph=True)
+        except TypeError:  # torch builds without keep_graph
+            self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            model.step_fused(b, self.coord, deterministic)
+        if hasattr(self.graph, "instantiate"):
+            try:
+                self.graph.instantiate()
+            except RuntimeError:
+                pass
+        self.h_coord = torch.empty((b.nloc, 3), dtype=model.dtype).pin_memory()
+        self.h_out = torch.empty(b.out.numel(), dtype=torch.uint8).pin_memory()
+        nf = b.nframes
+        esz = 8
+        self.h_energy = self.h_out[:nf * esz].view(torch.float64)
+        self.h_vir = self.h_out[nf * esz:nf * 10 * esz].view(torch.float64).view(nf, 9)
+        self.h_force = self.h_out[nf * 10 * esz:].view(model.dtype).view(b.nloc, 3)
+
+    def replay(self):
+        self.graph.replay()
+
+    def h2d(self, host_coord):
+        """Stage host coordinates (numpy or a CPU tensor) through the pinned
+        buffer and enqueue their copy to the device."""
+        if not isinstance(host_coord, torch.Tensor):
+            host_coord = torch.from_numpy(np.ascontiguousarray(host_coord))
+        if host_coord.data_ptr() != self.h_coord.data_ptr():
+            self.h_coord.copy_(host_coord.reshape(-1, 3))
+        self.coord.copy_(self.h_coord, non_blocking=True)
+
+    def d2h(self):
+        self.h_out.copy_(self.batch.out, non_blocking=True)
+
+    def __call__(self, host_coord, sync: bool = True):
+        self.h2d(host_coord)
+        self.graph.replay()
+        self.d2h()
+        if sync:
+            torch.cuda.current_stream(self.model.device).synchronize()
+        return self.h_energy, self.h_force, self.h_vir
+
+    def status(self) -> int:
+        return self.batch.status()
+
+
 def build_model(cfg: mdl.SeAConfig, seed: int, stat_frames, device, dtype=torch.float32,
                 compressed: bool = True):
     """Seeded parameters, davg/dstd from ``stat_frames`` (list of (coord,

@@ -73,9 +73,11 @@ def fitting_energy_and_grad(fit, bias, D):
 
 
 def energy_force_virial(cfg, params, davg, dstd, coord, atype, box, tables=None,
-                        table_infos=None, dtype=np.float64):
+                        table_infos=None, dtype=np.float64, cell_list=False):
     """One frame.  tables given -> compressed (tabulate ops); else plain
-    embedding nets.  Returns (energy, force [nloc,3], virial [9],
+    embedding nets.  cell_list: O(N) cell-list candidate build (the
+    reference's build_nlist) instead of the O(N^2) build_nlist_cpu; the
+    results are identical.  Returns (energy, force [nloc,3], virial [9],
     atom_energy [nloc])."""
     sel = list(cfg.sel)
     nnei = cfg.nnei
@@ -85,7 +87,8 @@ def energy_force_virial(cfg, params, davg, dstd, coord, atype, box, tables=None,
     nloc = len(atype)
     em, emd, rij, nl = O.prod_env_mat_a_pbc(
         np.asarray(coord, dtype).reshape(-1), atype, np.asarray(box, dtype).reshape(-1),
-        np.asarray(davg, dtype), np.asarray(dstd, dtype), cfg.rcut, cfg.rcut_smth, sel)
+        np.asarray(davg, dtype), np.asarray(dstd, dtype), cfg.rcut, cfg.rcut_smth, sel,
+        cell_list=cell_list)
     em3 = em.reshape(nloc, nnei, 4)
     X = np.zeros((nloc, 4, M), dtype)
     saved = []

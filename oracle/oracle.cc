@@ -228,6 +228,74 @@ void build_nlist(std::vector<std::vector<int>>& jlist, const T* c, int nloc,
   }
 }
 
+// The O(N) cell-list candidate build of source/lib/src/neighbor_list.cc:303-420
+// (build_nlist with build_clist / build_nlist_cell), on the extended
+// coordinates: extended atoms are binned into cells at least rcut (1 + 1e-3)
+// wide over their bounding box, and each local atom tests the atoms of its
+// own and the 26 adjacent cells with the predicate of build_nlist_cpu
+// (r^2 < rc^2 in the coordinate type, diff = c_i - c_j).  Every pair within
+// rcut lies in adjacent cells, so the candidate SET equals the brute-force
+// build's; the formatting sorts it, so the formatted list is identical.
+template <typename T>
+void build_nlist_cells(std::vector<std::vector<int>>& jlist, const T* c, int nloc,
+                       int nall, float rcut) {
+  const T rc2 = rcut * rcut;
+  jlist.assign(nloc, {});
+  if (nall == 0) return;
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) lo[d] = hi[d] = (double)c[d];
+  for (int j = 1; j < nall; ++j)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], (double)c[j * 3 + d]);
+      hi[d] = std::max(hi[d], (double)c[j * 3 + d]);
+    }
+  const double cs = (double)rcut * (1.0 + 1e-3);
+  int nc[3];
+  for (int d = 0; d < 3; ++d) nc[d] = std::max(1, (int)((hi[d] - lo[d]) / cs));
+  auto cell_of = [&](int j, int* k) {
+    for (int d = 0; d < 3; ++d) {
+      // cells of width (hi - lo) / nc >= cs; the last cell takes the top edge
+      int v = (int)(((double)c[j * 3 + d] - lo[d]) / (hi[d] - lo[d] + 1e-300) * nc[d]);
+      k[d] = v < 0 ? 0 : (v >= nc[d] ? nc[d] - 1 : v);
+    }
+  };
+  const long ncell = (long)nc[0] * nc[1] * nc[2];
+  std::vector<int> start(ncell + 1, 0), order(nall);
+  std::vector<int> cell(nall);
+  for (int j = 0; j < nall; ++j) {
+    int k[3];
+    cell_of(j, k);
+    cell[j] = (k[0] * nc[1] + k[1]) * nc[2] + k[2];
+    ++start[cell[j] + 1];
+  }
+  for (long q = 0; q < ncell; ++q) start[q + 1] += start[q];
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int j = 0; j < nall; ++j) order[fill[cell[j]]++] = j;  // ascending j per cell
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int ii = 0; ii < nloc; ++ii) {
+    int k[3];
+    cell_of(ii, k);
+    std::vector<int>& out = jlist[ii];
+    for (int a = std::max(0, k[0] - 1); a <= std::min(nc[0] - 1, k[0] + 1); ++a)
+      for (int b = std::max(0, k[1] - 1); b <= std::min(nc[1] - 1, k[1] + 1); ++b)
+        for (int e = std::max(0, k[2] - 1); e <= std::min(nc[2] - 1, k[2] + 1); ++e) {
+          const long q = ((long)a * nc[1] + b) * nc[2] + e;
+          for (int p = start[q]; p < start[q + 1]; ++p) {
+            const int jj = order[p];
+            if (jj == ii) continue;
+            T d0 = c[ii * 3 + 0] - c[jj * 3 + 0];
+            T d1 = c[ii * 3 + 1] - c[jj * 3 + 1];
+            T d2 = c[ii * 3 + 2] - c[jj * 3 + 2];
+            T r2 = d0 * d0 + d1 * d1 + d2 * d2;
+            if (r2 < rc2) out.push_back(jj);
+          }
+        }
+    std::sort(out.begin(), out.end());
+  }
+}
+
 // source/lib/src/fmt_nlist.cc:14-26 (NeighborInfo ordering) and :98-143
 // (format_nlist_i_cpu): keep j with float r^2 <= float rc^2 where
 // diff = (float)x_j - (float)x_i; order by (type, float r^2, index); fill
@@ -604,7 +672,7 @@ int prod_env_mat_a_pbc(T* em, T* em_deriv, T* rij, int* nlist, const T* coord,
                        const T* std_, int nloc, float rcut, float rcut_smth,
                        const int* sec, int ntypes, int map_to_local,
                        int* nall_out, T* ext_coord, int* ext_type,
-                       int* ext_map, int ext_cap) {
+                       int* ext_map, int ext_cap, int cell_list = 0) {
   std::vector<T> c(coord, coord + (size_t)nloc * 3);
   normalize_coord(c.data(), nloc, box);
   std::vector<T> cc;
@@ -617,7 +685,10 @@ int prod_env_mat_a_pbc(T* em, T* em_deriv, T* rij, int* nlist, const T* coord,
     std::copy(map.begin(), map.end(), ext_map);
   }
   std::vector<std::vector<int>> cand;
-  build_nlist(cand, cc.data(), nloc, nall, rcut);
+  if (cell_list)
+    build_nlist_cells(cand, cc.data(), nloc, nall, rcut);
+  else
+    build_nlist(cand, cc.data(), nloc, nall, rcut);
   prod_env_mat_a(em, em_deriv, rij, nlist, cc.data(), ct.data(), cand, avg, std_,
                  nloc, rcut, rcut_smth, sec, ntypes);
   const int nnei = sec[ntypes];
@@ -741,6 +812,17 @@ void env_mat_a_nlist(T* em, T* em_deriv, T* rij, const T* ext, const int* etype,
                               std_, nloc, rcut, rcut_smth, sec, ntypes,        \
                               map_to_local, nall_out, ext_coord, ext_type,     \
                               ext_map, ext_cap);                               \
+  }                                                                            \
+  OR_EXPORT int or_prod_env_mat_a_pbc_cells_##SFX(                             \
+      T* em, T* em_deriv, T* rij, int* nlist, const T* coord, const int* type, \
+      const T* box, const T* avg, const T* std_, int nloc, float rcut,         \
+      float rcut_smth, const int* sec, int ntypes, int map_to_local,           \
+      int* nall_out, T* ext_coord, int* ext_type, int* ext_map,                \
+      int ext_cap) {                                                           \
+    return prod_env_mat_a_pbc(em, em_deriv, rij, nlist, coord, type, box, avg, \
+                              std_, nloc, rcut, rcut_smth, sec, ntypes,        \
+                              map_to_local, nall_out, ext_coord, ext_type,     \
+                              ext_map, ext_cap, 1);                            \
   }                                                                            \
   OR_EXPORT void or_format_nlist_pt_##SFX(int* out, const T* ext,              \
                                           const int* etype, const int* nl_in,  \

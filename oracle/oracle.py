@@ -178,10 +178,14 @@ def env_mat_a_nlist(ext_coord, ext_type, fmt, nloc, avg, std, rcut, rcut_smth, s
 
 
 def prod_env_mat_a_pbc(coord, atype, box, avg, std, rcut, rcut_smth, sel,
-                       map_to_local=True, kind="oracle", return_ext=False):
+                       map_to_local=True, kind="oracle", return_ext=False, cell_list=False):
     """The TF ProdEnvMatA op in its internal-PBC (mesh of 6) mode for ONE
-    frame: normalise, copy ghosts, brute-force build, format, env mat,
+    frame: normalise, copy ghosts, candidate build, format, env mat,
     normalise by davg/dstd and (optionally) map indices to local atoms.
+    The candidate build is build_nlist_cpu's brute force
+    (neighbor_list.cc:873-916), or with ``cell_list`` (oracle only) the O(N)
+    cell list of build_nlist (neighbor_list.cc:303-420): the same candidate
+    set, so the same outputs.
     Returns flat (descrpt, descrpt_deriv, rij, nlist) as the op does."""
     c = _c(coord).reshape(-1)
     dt = c.dtype
@@ -201,7 +205,10 @@ def prod_env_mat_a_pbc(coord, atype, box, avg, std, rcut, rcut_smth, sel,
     ec = np.zeros(max(cap, 1) * 3, dt)
     et = np.zeros(max(cap, 1), np.int32)
     emap = np.zeros(max(cap, 1), np.int32)
-    _fn(kind, "prod_env_mat_a_pbc_" + _sfx(dt))(
+    name = "prod_env_mat_a_pbc_cells_" if cell_list else "prod_env_mat_a_pbc_"
+    if cell_list and kind != "oracle":
+        raise ValueError("the cell-list build is an oracle restatement only")
+    _fn(kind, name + _sfx(dt))(
         _ptr(em), _ptr(emd), _ptr(rij), _ptr(nl), _ptr(c), _ptr(t), _ptr(b), _ptr(a),
         _ptr(s), _I(nloc), _F(rcut), _F(rcut_smth), _ptr(sec), _I(len(sel)),
         _I(1 if map_to_local else 0), ctypes.byref(nall),

@@ -184,3 +184,39 @@ def test_composite_reproduces_reference_model_testcase(gb, oracle):
         np.testing.assert_allclose(ae, ae_ref, rtol=0, atol=1e-12)
         np.testing.assert_allclose(F, f_ref, rtol=0, atol=1e-12)
         np.testing.assert_allclose(V.reshape(-1), v_ref, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["w24", "w192", "w1536"])
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+def test_cell_list_build_matches_the_reference_nlist(oracle, golden_water, name, dt):
+    """The O(N) cell-list candidate build (the reference's build_nlist) gives
+    the neighbour list the reference library produced with its brute-force
+    build_nlist_cpu, element by element, and the same env matrix."""
+    g = golden_water
+    dtype = np.float64 if dt == "f64" else np.float32
+    sel = [int(s) for s in g["sel"]]
+    c = g[f"{name}_coord"].astype(dtype)
+    em, emd, rij, nl = oracle.prod_env_mat_a_pbc(
+        c, g[f"{name}_atype"], g[f"{name}_box"].astype(dtype), g["avg"].astype(dtype),
+        g["std"].astype(dtype), float(g["rcut"]), float(g["rcut_smth"]), sel, cell_list=True)
+    np.testing.assert_array_equal(nl, g[f"{name}_{dt}_nlist"].astype(np.int32))
+    n = g[f"{name}_{dt}_em"].size
+    np.testing.assert_array_equal(em[:n], g[f"{name}_{dt}_em"])
+
+
+def test_cell_list_build_matches_brute_force_on_ragged_frames(oracle, gb):
+    """Frames of 8..512 molecules at 1 g/cm3 (boxes from 6 to 25 A, so one to
+    four cells per edge): both candidate builds give the same list."""
+    water = __import__("dpmd_public_gb300.water", fromlist=["x"])
+    sel = [46, 92]
+    avg = np.zeros((2, 552))
+    std = np.ones((2, 552))
+    for c, t, b in water.ragged_frames(6, seed=91, lo=8, hi=512):
+        for dtype in (np.float64, np.float32):
+            a = oracle.prod_env_mat_a_pbc(c.astype(dtype), t, b.astype(dtype), avg.astype(dtype),
+                                          std.astype(dtype), 6.0, 0.5, sel, map_to_local=False)
+            b2 = oracle.prod_env_mat_a_pbc(c.astype(dtype), t, b.astype(dtype), avg.astype(dtype),
+                                           std.astype(dtype), 6.0, 0.5, sel, map_to_local=False,
+                                           cell_list=True)
+            np.testing.assert_array_equal(a[3], b2[3])
+            np.testing.assert_array_equal(a[0], b2[0])

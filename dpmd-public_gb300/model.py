@@ -171,16 +171,24 @@ def build_tables(params: dict, davg: np.ndarray, dstd: np.ndarray, min_nbor_dist
     """Fifth-order tables of every embedding net (DPTabulate.build for the
     "A" descriptor, deepmd/utils/tabulate.py:67-370, :468-486).
 
-    Range: lower = floor(-davg_r / dstd_r), upper = ceil((sw(rmin)/rmin -
-    davg_r) / dstd_r) per centre type (the min / max over centre types for a
-    one-side net); rows of width stride0 on [lower, upper) and stride1 on
-    [upper, extrapolate * upper); each row holds, per output k, the six
-    coefficients of the quintic Hermite interpolant matching value, first and
-    second derivative at both ends.
+    Range, as the PyTorch descriptor's compression computes it: DescrptSeA
+    keeps davg / dstd as [ntypes, nnei, 4] and DPTabulate.build
+    (deepmd/utils/tabulate.py:90-95, :468-486) takes, per centre type, the
+    four columns c of the first slot, lower_c = floor(-davg_c / dstd_c) and
+    upper_c = ceil((sw(rmin) / rmin - davg_c) / dstd_c), and reduces them
+    with min / max over c (so the angular columns, davg 0 and a smaller
+    dstd, usually set the upper bound); a one-side net then takes the min /
+    max over the centre types with a non-empty sel.  Rows of width stride0
+    on [lower, upper) and stride1 on [upper, extrapolate * upper); each row
+    holds, per output k, the six coefficients of the quintic Hermite
+    interpolant matching value, first and second derivative at both ends.
+    davg / dstd: [ntypes, nnei * 4] (or [ntypes, nnei, 4]).
     Returns (tables [n_emb] float64 [nspline, 6 M], infos [n_emb, 6])."""
     sw = _spline5_switch(min_nbor_dist, cfg.rcut_smth, cfg.rcut)
-    lo_t = np.floor(-davg[:, 0] / dstd[:, 0])
-    up_t = np.ceil(((1.0 / min_nbor_dist) * sw - davg[:, 0]) / dstd[:, 0])
+    a0 = np.asarray(davg, np.float64).reshape(cfg.ntypes, -1, 4)[:, 0, :]
+    s0 = np.asarray(dstd, np.float64).reshape(cfg.ntypes, -1, 4)[:, 0, :]
+    lo_t = np.floor(-a0 / s0).min(axis=1)
+    up_t = np.ceil(((1.0 / min_nbor_dist) * sw - a0) / s0).max(axis=1)
     tables, infos = [], []
     M = cfg.neuron[-1]
     for k in range(cfg.n_emb):

@@ -24,6 +24,16 @@ Two sources, both read only here (the fixtures travel; the reference does not):
    frame whose candidate list is every extended atom within rcut + 2 A in a
    shuffled order, as an MD engine hands it over.
 
+5. ``ref_tabulate.npz``: compression tables built by the reference's own
+   ``DPTabulate`` (``deepmd/utils/tabulate_math.py`` on
+   ``deepmd/utils/tabulate.py``, executed from their source with the numpy
+   array namespace) for seeded se_e2_a embedding nets and statistics laid out
+   as the PyTorch descriptor keeps them ([ntypes, nnei, 4]): a small net
+   (widths 2-4-8, coarse strides) stored whole, and the bench-shaped net
+   (25-50-100, strides 0.01 / 0.1, extrapolate 5) for both type_one_side
+   settings stored as lower / upper / nspline, per-column sums and a sample
+   of rows.
+
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
         (or DPMD_REFERENCE=/path/to/reference python tests/golden/make_golden.py)
 """
@@ -238,6 +248,130 @@ def reference_format_nlist_fixture(path_out: str) -> None:
     np.savez_compressed(path_out, **data)
 
 
+def _reference_tabulate_module():
+    """deepmd.utils.tabulate and deepmd.utils.tabulate_math executed from the
+    reference sources, with the numpy array namespace standing in for
+    array_api_compat and the two dpmodel helpers they import."""
+    import types
+
+    saved = {k: sys.modules.get(k) for k in (
+        "array_api_compat", "deepmd", "deepmd.dpmodel", "deepmd.dpmodel.common",
+        "deepmd.dpmodel.utils", "deepmd.dpmodel.utils.network", "deepmd.utils",
+        "deepmd.utils.tabulate", "deepmd.utils.tabulate_math")}
+    aac = types.ModuleType("array_api_compat")
+    aac.array_namespace = lambda *xs: np
+    aac.device = lambda x: "cpu"
+    sys.modules["array_api_compat"] = aac
+    for name in ("deepmd", "deepmd.dpmodel", "deepmd.dpmodel.utils", "deepmd.utils"):
+        m = types.ModuleType(name)
+        m.__path__ = []
+        sys.modules[name] = m
+    common = types.ModuleType("deepmd.dpmodel.common")
+    common.to_numpy_array = lambda x: None if x is None else np.asarray(x)
+    sys.modules["deepmd.dpmodel.common"] = common
+    net = types.ModuleType("deepmd.dpmodel.utils.network")
+    net.get_activation_fn = lambda name: {"tanh": np.tanh}[name]
+    sys.modules["deepmd.dpmodel.utils.network"] = net
+    mods = {}
+    for name, rel in (("deepmd.utils.tabulate", "deepmd/utils/tabulate.py"),
+                      ("deepmd.utils.tabulate_math", "deepmd/utils/tabulate_math.py")):
+        spec = importlib.util.spec_from_file_location(name, os.path.join(REF, rel))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+        mods[name] = mod
+    tm = mods["deepmd.utils.tabulate_math"]
+    for k, v in saved.items():
+        if v is None:
+            sys.modules.pop(k, None)
+        else:
+            sys.modules[k] = v
+    return tm
+
+
+def reference_tabulate_fixture(path_out: str) -> None:
+    sys.path.insert(0, ROOT)
+    from __graft_entry__ import load_package  # noqa: E402
+
+    load_package()
+    import dataclasses
+
+    import dpmd_public_gb300.model as mdl  # noqa: E402
+
+    tm = _reference_tabulate_module()
+
+    class _SeA:
+        """The descriptor interface DPTabulate reads (get_sel, get_rcut,
+        get_rcut_smth, get_ntypes, serialize), over seeded parameters."""
+
+        def __init__(self, cfg, params, davg, dstd):
+            self.cfg = cfg
+            nets = [{"layers": [{"@variables": {"w": np.asarray(l["w"]), "b": np.asarray(l["b"])}}
+                                for l in net]} for net in params["emb"]]
+            self.ser = {"type": "se_e2_a",
+                        "@variables": {"davg": davg.reshape(cfg.ntypes, cfg.nnei, 4),
+                                       "dstd": dstd.reshape(cfg.ntypes, cfg.nnei, 4)},
+                        "embeddings": {"networks": nets}}
+
+        def get_sel(self):
+            return list(self.cfg.sel)
+
+        def get_rcut(self):
+            return self.cfg.rcut
+
+        def get_rcut_smth(self):
+            return self.cfg.rcut_smth
+
+        def get_ntypes(self):
+            return self.cfg.ntypes
+
+        def serialize(self):
+            return self.ser
+
+    def stats(cfg, seed):
+        rng = np.random.default_rng(seed)
+        nn = cfg.nnei
+        davg = np.zeros((cfg.ntypes, nn * 4))
+        davg[:, 0::4] = rng.uniform(0.03, 0.08, (cfg.ntypes, 1))
+        dstd = np.ones((cfg.ntypes, nn * 4))
+        dstd[:, 0::4] = rng.uniform(0.11, 0.15, (cfg.ntypes, 1))
+        dstd[:, 1::4] = dstd[:, 2::4] = dstd[:, 3::4] = rng.uniform(0.07, 0.09, (cfg.ntypes, 1))
+        return davg, dstd
+
+    data = {}
+    cases = {
+        "small": (dataclasses.replace(mdl.SeAConfig(), neuron=(2, 4, 8), stride0=0.1, stride1=1.0),
+                  0.9, 101),
+        "bench_one_side": (mdl.SeAConfig(), 0.78, 20261203),
+        "bench_pair": (dataclasses.replace(mdl.SeAConfig(), type_one_side=False), 0.78, 20261203),
+    }
+    rng = np.random.default_rng(77)
+    for tag, (cfg, rmin, seed) in cases.items():
+        params = mdl.init_params(cfg, seed)
+        davg, dstd = stats(cfg, seed + 1)
+        tab = tm.DPTabulate(_SeA(cfg, params, davg, dstd), list(cfg.neuron),
+                            type_one_side=cfg.type_one_side)
+        lower, upper = tab.build(rmin, cfg.extrapolate, cfg.stride0, cfg.stride1)
+        data[f"{tag}_davg"], data[f"{tag}_dstd"], data[f"{tag}_rmin"] = davg, dstd, rmin
+        data[f"{tag}_seed"] = seed
+        names = list(tab.data)
+        data[f"{tag}_nets"] = np.array(names)
+        for k, name in enumerate(names):
+            t = np.asarray(tab.data[name], np.float64)
+            data[f"{tag}_{k}_lower"] = float(lower[name])
+            data[f"{tag}_{k}_upper"] = float(upper[name])
+            data[f"{tag}_{k}_nspline"] = t.shape[0]
+            data[f"{tag}_{k}_colsum"] = np.abs(t).reshape(t.shape[0], -1, 6).sum(axis=(0, 1))
+            if tag == "small":
+                data[f"{tag}_{k}_table"] = t
+            else:
+                rows = np.unique(np.concatenate([[0, t.shape[0] - 1],
+                                                 rng.integers(0, t.shape[0], 10)]))
+                data[f"{tag}_{k}_rows"] = rows
+                data[f"{tag}_{k}_sample"] = t[rows]
+    np.savez_compressed(path_out, **data)
+
+
 def main() -> None:
     lib = {}
     for f in LIB_TESTS:
@@ -251,6 +385,7 @@ def main() -> None:
     reference_water_fixture(os.path.join(HERE, "ref_water.npz"))
     reference_format_nlist_fixture(os.path.join(HERE, "pt_format_nlist.npz"))
     reference_model_fixture(os.path.join(HERE, "ref_deeppot_sea.npz"))
+    reference_tabulate_fixture(os.path.join(HERE, "ref_tabulate.npz"))
     print("fixtures:", sorted(os.listdir(HERE)))
 
 

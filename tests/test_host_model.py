@@ -104,3 +104,68 @@ def test_composite_force_is_minus_energy_gradient(m):
             Ep = composite.energy_force_virial(cfg, p, davg, dstd, cp, t, b, tb, inf)[0]
             Em = composite.energy_force_virial(cfg, p, davg, dstd, cm, t, b, tb, inf)[0]
             assert abs(-(Ep - Em) / (2 * h) - F[a, d]) < 1e-8
+
+
+@pytest.mark.parametrize("tag", ["small", "bench_one_side", "bench_pair"])
+def test_tables_match_reference_dptabulate(m, tag):
+    """build_tables against tables the reference's own DPTabulate built
+    (tests/golden/ref_tabulate.npz, made by make_golden.py from the
+    reference sources) for the same seeded nets and statistics: the range
+    (lower, upper, row count) exactly; each row's value, slope and curvature
+    coefficients to 1e-13 of their column's scale, and the row polynomial
+    and its slope inside the interval to 1e-13 / 1e-11 (the whole table for
+    the small net, sampled rows and per-column sums for the 25-50-100
+    nets)."""
+    import dataclasses
+    import os
+
+    mdl, water = m
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_tabulate.npz"))
+    base = mdl.SeAConfig()
+    cfg = {"small": dataclasses.replace(base, neuron=(2, 4, 8), stride0=0.1, stride1=1.0),
+           "bench_one_side": base,
+           "bench_pair": dataclasses.replace(base, type_one_side=False)}[tag]
+    params = mdl.init_params(cfg, int(g[f"{tag}_seed"]))
+    tabs, infos = mdl.build_tables(params, g[f"{tag}_davg"], g[f"{tag}_dstd"],
+                                   float(g[f"{tag}_rmin"]), cfg)
+    names = [str(x) for x in g[f"{tag}_nets"]]
+    nt = cfg.ntypes
+    for k, name in enumerate(names):
+        # the reference's table k: filter_-1_net_{tj} (one side) or
+        # filter_{ti}_net_{tj}; ours are indexed tj (one side) or tj * nt + ti
+        if cfg.type_one_side:
+            ours = int(name.split("_")[-1])
+        else:
+            ti, tj = int(name.split("_")[1]), int(name.split("_")[3])
+            ours = tj * nt + ti
+        t, info = tabs[ours], infos[ours]
+        assert info[0] == g[f"{tag}_{k}_lower"] and info[1] == g[f"{tag}_{k}_upper"]
+        assert t.shape[0] == int(g[f"{tag}_{k}_nspline"])
+        if f"{tag}_{k}_table" in g:
+            ref = g[f"{tag}_{k}_table"]
+            rows = np.arange(t.shape[0])
+        else:
+            rows = g[f"{tag}_{k}_rows"]
+            ref = g[f"{tag}_{k}_sample"]
+            t = t[rows]
+        a, b = t.reshape(len(rows), -1, 6), ref.reshape(len(rows), -1, 6)
+        # value, slope and curvature at the row's first node
+        scale = np.abs(b).max(axis=(0, 1))
+        for c in range(3):
+            assert np.abs(a[..., c] - b[..., c]).max() <= 1e-13 * scale[c], (name, c)
+        # the interpolant and its slope inside each interval (the higher
+        # coefficients carry the nodes' rounding amplified by 1 / stride^n in
+        # any evaluation order; their effect on the polynomial is what counts)
+        n0 = int((info[1] - info[0]) / cfg.stride0)
+        tt = np.where(rows < n0, cfg.stride0, cfg.stride1)[:, None]
+        vmax, dmax = np.abs(b[..., 0]).max(), np.abs(b[..., 1]).max()
+        for f in (0.25, 0.5, 0.75, 1.0):
+            u = f * tt
+            pa = sum(a[..., c] * u ** c for c in range(6))
+            pb = sum(b[..., c] * u ** c for c in range(6))
+            da = sum(c * a[..., c] * u ** (c - 1) for c in range(1, 6))
+            db = sum(c * b[..., c] * u ** (c - 1) for c in range(1, 6))
+            assert np.abs(pa - pb).max() <= 1e-13 * vmax, (name, f)
+            assert np.abs(da - db).max() <= 1e-11 * dmax, (name, f)
+        colsum = np.abs(tabs[ours]).reshape(tabs[ours].shape[0], -1, 6).sum(axis=(0, 1))
+        np.testing.assert_allclose(colsum[:3], g[f"{tag}_{k}_colsum"][:3], rtol=1e-13)

@@ -81,14 +81,22 @@ def _frame():
     return water.water_frame(N_SIDE, BOX, SEED)
 
 
-def _ragged_frames(rank: int = 0):
-    """The 512 ragged frames of one rank (rank 0: the single-GPU workload;
-    rank r > 0 draws its own frames from the same distribution)."""
+def _ragged_frames(rank: int = 0, world: int = 1):
+    """The frames of one rank and their global indices.  One GPU: the 512
+    ragged frames.  N GPUs (weak scaling): the job holds N x 512 frames of
+    the same distribution, partitioned across the ranks by atoms."""
     import importlib
 
     _pkg()
     water = importlib.import_module("dpmd_public_gb300.water")
-    return water.ragged_frames(N_FRAMES, seed=SEED + 7919 * rank, lo=MOL_LO, hi=MOL_HI)
+    if world == 1:
+        return water.ragged_frames(N_FRAMES, seed=SEED, lo=MOL_LO, hi=MOL_HI), \
+            list(range(N_FRAMES))
+    R = importlib.import_module("dpmd_public_gb300.replicas")
+    n = N_FRAMES * world
+    counts = water.ragged_counts(n, SEED, MOL_LO, MOL_HI)
+    ids = R.frames_of_rank(3 * counts, world, rank)
+    return water.ragged_frames(n, seed=SEED, lo=MOL_LO, hi=MOL_HI, which=ids), ids
 
 
 def _stat_frames():
@@ -309,7 +317,7 @@ def reference_arm(args):
         frames, idx, workload = [_frame()], [0], WORKLOAD_12K
         sample = "full 12288-atom frame per step"
     else:
-        frames = _ragged_frames(0)
+        frames = _ragged_frames(0)[0]
         idx, workload = _cpu_sample(frames, 32), WORKLOAD_RAGGED
         sample = (f"{len(idx)} of the 512 frames per step (every 16th in size order), "
                   f"frame by frame")
@@ -494,14 +502,13 @@ def ragged_main(args):
     torch.backends.cudnn.allow_tf32 = False
     se_a, cfg, m64, model, plain = _setup_models(dev, args.fit_mode)
     L = importlib.import_module("dpmd_public_gb300._lib")
-    frames = _ragged_frames(rank)
+    frames, frame_ids = _ragged_frames(rank, ws)
     if args.profile:
         frames = frames[:args.profile_frames]
     nat = sum(len(f[1]) for f in frames)
     batch = model.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
     host_coord = np.concatenate([f[0] for f in frames]).astype(np.float32)
-    step = se_a.CapturedStep(model, batch)
-    step.coord.copy_(torch.from_numpy(host_coord))
+    step = se_a.CapturedStep(model, batch, coord=host_coord)
     step.replay()
     torch.cuda.synchronize()
     if batch.status() != 0:
@@ -578,7 +585,7 @@ def ragged_main(args):
                       "form": "fused compressed, all frames packed in one CUDA graph, "
                               "deterministic (fixed-point) sums",
                       "fitting_gemm": args.fit_mode, "l2": L2Flush.DESC,
-                      "parallelism": f"replicas x{ws} (each rank its own 512 frames)",
+                      "parallelism": f"replicas x{ws} (N x 512 frames partitioned by atoms)",
                       "wall_s": wall},
            "e2e": e2e,
            "gpu_launches": None if launches is None else launches["ours"] * args.steps,
@@ -623,6 +630,18 @@ def ragged_main(args):
                          "over the size order (smallest and largest included)"}
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline_ragged(frames, np_model)
+    if ws > 1:
+        # the per-frame results of every rank, in the job's frame order
+        R = importlib.import_module("dpmd_public_gb300.replicas")
+        offs = batch.plan.atom_off
+        Fh = F_dev.cpu().numpy()
+        Eg, Vg, Fg = R.gather_frame_results(
+            frame_ids, E_dev.cpu().numpy(), V_dev.cpu().numpy(),
+            [Fh[int(offs[k]):int(offs[k]) + len(f[1])] for k, f in enumerate(frames)],
+            N_FRAMES * ws)
+        out["replicas"] = {"frames_gathered": len(Fg), "atoms_gathered": int(sum(len(f) for f in Fg)),
+                           "partition": "N x 512 frames, balanced by atoms (replicas.py)",
+                           "energy_sum_eV": float(np.sum(Eg))}
     if not args.no_12k:
         del step
         out["water12k"] = water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, flush,
@@ -649,8 +668,7 @@ def type_one_side_false(se_a, cfg, frames, dev, args, flush):
     m = se_a.SeAModel(cfg2, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), dev,
                       torch.float32, m64.tables_np, m64.infos_np, fit_mode=args.fit_mode)
     b = m.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
-    step = se_a.CapturedStep(m, b)
-    step.coord.copy_(torch.from_numpy(np.concatenate([f[0] for f in frames]).astype(np.float32)))
+    step = se_a.CapturedStep(m, b, coord=np.concatenate([f[0] for f in frames]).astype(np.float32))
     ms, _ = time_captured(step, flush, max(3, min(args.steps, 10)), 3, 1)
     k = _by_size(frames, 2)[-1]
     c, t, bx = frames[k]
@@ -694,8 +712,7 @@ def water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, flush, full:
     c, t, b = _frame()
     nat = len(t)
     batch = model.batch([t], b[None])
-    step = se_a.CapturedStep(model, batch)
-    step.coord.copy_(torch.tensor(c, dtype=torch.float32))
+    step = se_a.CapturedStep(model, batch, coord=c.astype(np.float32))
     step.replay()
     torch.cuda.synchronize()
     if batch.status() != 0:
@@ -737,8 +754,7 @@ def water12k_leg(args, se_a, cfg, m64, model, dev, ws, rank, local, flush, full:
     Fp = None
     if full:
         # the same step with floating-point atomic sums
-        s2 = se_a.CapturedStep(model, batch, deterministic=False)
-        s2.coord.copy_(step.coord)
+        s2 = se_a.CapturedStep(model, batch, coord=step.coord, deterministic=False)
         det_ms, _ = time_captured(s2, flush, reps, 3, 1)
         del s2
         out["atomic_sums"] = {"value": ws * nat / (det_ms * 1e-3), "ms_per_step": det_ms,

@@ -18,6 +18,7 @@ _F = ctypes.c_float
 _Z = ctypes.c_size_t
 
 GBDP_OK = 0
+GBDP_STATUS_CAND_OVERFLOW = 1
 GBDP_STATUS = {
     1: "candidate overflow (raise max_cand)",
     2: "extended-atom overflow",

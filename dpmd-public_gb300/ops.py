@@ -209,6 +209,25 @@ class NeighborPlan:
     def frame(self, f: int):
         return self.frames_host[f]
 
+    # the candidate buffer lives in shared memory: 4 warps x max_cand x 9 B
+    # per CTA, at most 4096 candidates a centre (within 200 KiB)
+    MAX_CAND_LIMIT = 4096
+
+    @property
+    def max_cand(self) -> int:
+        return int(self.plan.max_cand)
+
+    def grow_candidates(self) -> bool:
+        """Double the per-centre candidate capacity after a candidate
+        overflow (as the reference doubles its neighbour capacity and
+        retries, source/op/tf/prod_env_mat_multi_device.cc:1583-1605).  The
+        workspace does not depend on it; a graph captured with the old
+        capacity must be captured again.  False when the limit is reached."""
+        if self.plan.max_cand >= self.MAX_CAND_LIMIT:
+            return False
+        self.plan.max_cand = min(2 * self.plan.max_cand, self.MAX_CAND_LIMIT)
+        return True
+
 
 class EnvMatResult:
     __slots__ = ("em", "em_deriv", "rij", "nlist", "nlist_ext", "ext_coord", "ext_type",
@@ -240,17 +259,25 @@ def env_mat_packed(plan: NeighborPlan, coord, atype, avg, std, rcut_smth, sel,
         r.ext_nall = torch.empty((plan.nframes,), dtype=torch.int32, device=dev)
     selc = (ctypes.c_int * len(sel))(*[int(s) for s in sel])
     fn = getattr(L.load(), f"gbdp_prod_env_mat_a_{L.sfx(dt)}")
-    L.check(fn(_ptr(r.em), _ptr(r.em_deriv), _ptr(r.rij), _ptr(r.nlist), _ptr(r.nlist_ext),
-               _ptr(r.ext_coord), _ptr(r.ext_type), _ptr(r.ext_map), _ptr(r.ext_nall),
-               _ptr(coord), _ptr(atype), _ptr(avg), _ptr(std), ctypes.byref(plan.plan),
-               _ptr(plan.frames_dev), ctypes.c_float(rcut_smth), selc, len(sel),
-               _ptr(plan.workspace), ctypes.c_size_t(plan.ws_bytes), _stream()),
-            "prod_env_mat_a")
-    if check_status:
+    while True:
+        L.check(fn(_ptr(r.em), _ptr(r.em_deriv), _ptr(r.rij), _ptr(r.nlist), _ptr(r.nlist_ext),
+                   _ptr(r.ext_coord), _ptr(r.ext_type), _ptr(r.ext_map), _ptr(r.ext_nall),
+                   _ptr(coord), _ptr(atype), _ptr(avg), _ptr(std), ctypes.byref(plan.plan),
+                   _ptr(plan.frames_dev), ctypes.c_float(rcut_smth), selc, len(sel),
+                   _ptr(plan.workspace), ctypes.c_size_t(plan.ws_bytes), _stream()),
+                "prod_env_mat_a")
+        if not check_status:
+            return r
         st = L.load().gbdp_env_status(_ptr(plan.workspace), _stream())
+        # a centre with more candidates than the capacity: double it and run
+        # again (the outputs of the failed run are overwritten)
+        if st == L.GBDP_STATUS_CAND_OVERFLOW and plan.grow_candidates():
+            continue
         if st != 0:
-            raise L.GbdpError(f"prod_env_mat_a device status {st}: {L.GBDP_STATUS.get(st, '?')}")
-    return r
+            raise L.GbdpError(f"prod_env_mat_a device status {st}: {L.GBDP_STATUS.get(st, '?')}"
+                              + (f" at max_cand {plan.max_cand}"
+                                 if st == L.GBDP_STATUS_CAND_OVERFLOW else ""))
+        return r
 
 
 # ---------------------------------------------------- TF-contract ops --

@@ -844,10 +844,30 @@ class CapturedStep:
     next call.  The graph reads and writes fixed buffers, so the batch and
     the model must outlive this object."""
 
-    def __init__(self, model: SeAModel, b: "Batch", warmup: int = 3, deterministic=None):
+    def __init__(self, model: SeAModel, b: "Batch", coord=None, warmup: int = 3,
+                 deterministic=None):
+        """coord: the coordinates the warm-up steps run on (host array or
+        tensor, [nloc_total, 3]); later calls bring their own."""
         self.model, self.batch = model, b
+        self.deterministic = deterministic
         dev = model.device
         self.coord = torch.zeros((b.nloc, 3), dtype=model.dtype, device=dev)
+        if coord is not None:
+            if not isinstance(coord, torch.Tensor):
+                coord = torch.from_numpy(np.ascontiguousarray(coord))
+            self.coord.copy_(coord.reshape(-1, 3))
+        self._capture(warmup)
+        self.h_coord = torch.empty((b.nloc, 3), dtype=model.dtype).pin_memory()
+        self.h_out = torch.empty(b.out.numel(), dtype=torch.uint8).pin_memory()
+        nf = b.nframes
+        esz = 8
+        self.h_energy = self.h_out[:nf * esz].view(torch.float64)
+        self.h_vir = self.h_out[nf * esz:nf * 10 * esz].view(torch.float64).view(nf, 9)
+        self.h_force = self.h_out[nf * 10 * esz:].view(model.dtype).view(b.nloc, 3)
+
+    def _capture(self, warmup: int):
+        model, b, deterministic = self.model, self.batch, self.deterministic
+        dev = model.device
         side = torch.cuda.Stream(device=dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -866,13 +886,6 @@ class CapturedStep:
                 self.graph.instantiate()
             except RuntimeError:
                 pass
-        self.h_coord = torch.empty((b.nloc, 3), dtype=model.dtype).pin_memory()
-        self.h_out = torch.empty(b.out.numel(), dtype=torch.uint8).pin_memory()
-        nf = b.nframes
-        esz = 8
-        self.h_energy = self.h_out[:nf * esz].view(torch.float64)
-        self.h_vir = self.h_out[nf * esz:nf * 10 * esz].view(torch.float64).view(nf, 9)
-        self.h_force = self.h_out[nf * 10 * esz:].view(model.dtype).view(b.nloc, 3)
 
     def replay(self):
         self.graph.replay()
@@ -890,11 +903,23 @@ class CapturedStep:
         self.h_out.copy_(self.batch.out, non_blocking=True)
 
     def __call__(self, host_coord, sync: bool = True):
+        """One step on host coordinates.  With ``sync`` the device status is
+        read as well: a candidate overflow doubles the capacity, captures the
+        step again and repeats it (other statuses raise)."""
         self.h2d(host_coord)
         self.graph.replay()
         self.d2h()
         if sync:
             torch.cuda.current_stream(self.model.device).synchronize()
+            st = self.batch.status()
+            while st == L.GBDP_STATUS_CAND_OVERFLOW and self.batch.plan.grow_candidates():
+                self._capture(1)
+                self.graph.replay()
+                self.d2h()
+                torch.cuda.current_stream(self.model.device).synchronize()
+                st = self.batch.status()
+            if st != 0:
+                raise L.GbdpError(f"fused step device status {st}: {L.GBDP_STATUS.get(st, '?')}")
         return self.h_energy, self.h_force, self.h_vir
 
     def status(self) -> int:

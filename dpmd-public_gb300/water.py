@@ -89,14 +89,20 @@ def water_box_for(n_mol: int) -> float:
     return (n_mol * VOL_PER_MOLECULE) ** (1.0 / 3.0)
 
 
-def ragged_frames(n_frames: int, seed: int, lo: int = 8, hi: int = 512):
+def ragged_counts(n_frames: int, seed: int, lo: int = 8, hi: int = 512) -> np.ndarray:
+    """Molecule counts ~ U[lo, hi] of the frames of ``ragged_frames``."""
+    return np.random.default_rng(seed).integers(lo, hi + 1, n_frames)
+
+
+def ragged_frames(n_frames: int, seed: int, lo: int = 8, hi: int = 512, which=None):
     """Independent frames with molecule counts ~ U[lo, hi], each in its own
-    1.0 g/cm^3 cubic box on an n = ceil(N^(1/3)) lattice."""
-    rng = np.random.default_rng(seed)
-    counts = rng.integers(lo, hi + 1, n_frames)
+    1.0 g/cm^3 cubic box on an n = ceil(N^(1/3)) lattice.  ``which``: build
+    only these frame indices (in that order); each frame has its own seed, so
+    a subset equals the same frames of the whole set."""
+    counts = ragged_counts(n_frames, seed, lo, hi)
     frames = []
-    for k, n in enumerate(counts):
-        n = int(n)
+    for k in (range(n_frames) if which is None else which):
+        n = int(counts[k])
         side = math.ceil(n ** (1.0 / 3.0) - 1e-9)
         frames.append(water_frame(side, water_box_for(n), seed * 100003 + k, n_mol=n))
     return frames

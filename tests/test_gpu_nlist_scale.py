@@ -144,3 +144,53 @@ def test_ragged_512_frames_sampled_bit_exact(gb, oracle):
                              f"ragged frame {k}")
     assert max(sizes[pick]) == 1536
     print(f"[nlist] ragged sample: {len(pick)} frames, {ties} ties")
+
+
+def test_candidate_overflow_doubles_capacity_and_retries(gb, oracle):
+    """A 1 A lattice has about 900 candidates within rc per centre, above
+    the default capacity of 512: the env-mat call doubles the capacity,
+    runs again and returns the reference's list (truncated to sel)."""
+    frame = _lattice(10, 1.0, seed=5)
+    avg, std = _stats()
+    plan, r = _gpu_env(gb, [frame], torch.float64, avg, std)
+    assert plan.max_cand == 1024
+    _check_frame(oracle, r, plan, 0, frame, torch.float64, avg, std, "lattice 10^3 a=1.0 retry")
+
+
+def test_candidate_overflow_at_the_limit_raises(gb):
+    """At the capacity limit the overflow is reported, not truncated."""
+    frame = _lattice(10, 1.0, seed=5)
+    avg, std = _stats()
+    plan = gb.NeighborPlan([1000], frame[2][None], 6.0, DEV, torch.float64, max_cand=512)
+    plan.MAX_CAND_LIMIT = 512
+    c = torch.tensor(frame[0], device=DEV)
+    t = torch.tensor(frame[1], dtype=torch.int32, device=DEV)
+    with pytest.raises(RuntimeError, match="candidate overflow"):
+        gb.env_mat_packed(plan, c, t, torch.tensor(avg, device=DEV), torch.tensor(std, device=DEV),
+                          0.5, SEL)
+
+
+def test_captured_step_retries_after_overflow(gb):
+    """The captured fused step on the dense lattice: the first call
+    overflows, the step is captured again with twice the capacity, and its
+    forces equal an eager step's with that capacity."""
+    import importlib
+
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    cfg = mdl.SeAConfig()
+    m64 = se_a.build_model(cfg, 7, [water.water_frame(4, 12.42, 1000)], DEV, torch.float64)
+    m = se_a.SeAModel(cfg, m64.params_np, m64.davg.cpu().numpy(), m64.dstd.cpu().numpy(), DEV,
+                      torch.float32, m64.tables_np, m64.infos_np)
+    c, t, b = _lattice(10, 1.0, seed=5)
+    # move the lattice off its exact sites so that forces are not all zero
+    c = c + np.random.default_rng(1).normal(0, 0.05, c.shape)
+    bt = m.batch([t], b[None])
+    step = se_a.CapturedStep(m, bt, coord=c.astype(np.float32))
+    E, F, V = step(c.astype(np.float32))
+    assert bt.plan.max_cand == 1024 and bt.status() == 0
+    b2 = m.batch([t], b[None], max_cand=1024)
+    E2, F2, V2 = m.step_fused(b2, torch.tensor(c, dtype=torch.float32, device=DEV))
+    torch.cuda.synchronize()
+    assert torch.equal(F, F2.cpu())

@@ -63,6 +63,7 @@ class NbrPlan(ctypes.Structure):
 _SIGS = {
     "gbdp_last_error": (ctypes.c_char_p, []),
     "gbdp_version": (_I, []),
+    "gbdp_selftest_wait_timeout": (_I, [_P, _P, ctypes.c_longlong, _P]),
     "gbdp_nbr_plan_make": (_I, [_P, _P, _I, _P, _P, _F, _I]),
     "gbdp_env_workspace_bytes": (_Z, [_P, _I]),
     "gbdp_env_status": (_I, [_P, _P]),

@@ -51,6 +51,19 @@ GBDP_API const char* gbdp_last_error(void);
 /* Library version, major * 10000 + minor * 100 + patch. */
 GBDP_API int gbdp_version(void);
 
+/* Self-test of the bounded device waits (no counterpart in the reference).
+ * The tensor-core kernels wait on mbarriers for at most a fixed number of
+ * polls; a wait that gives up raises GBDP_STATUS_TIMEOUT in the launch's
+ * status word and the kernel returns instead of hanging.  This launches one
+ * warp that completes a barrier phase with a 16-byte bulk copy of
+ * result[0..3] (16-byte aligned device ints), then waits `limit` polls on
+ * the next phase, which nothing completes.  Afterwards, in stream order:
+ * result[0] = the copied result[0] + 1 (the satisfied wait saw the data),
+ * result[1] = 0 (the second wait gave up), and *status (a device int the
+ * caller zeroes) = GBDP_STATUS_TIMEOUT.  The GPU context stays usable. */
+GBDP_API int gbdp_selftest_wait_timeout(int* status, int* result, long long limit,
+                                        gbdp_stream stream);
+
 /* ------------------------------------------------------------------------
  * Tabulated embedding + G^T.R contraction (compressed se_e2_a).
  * Replaces deepmd::tabulate_fusion_se_a_gpu / _grad_gpu / _grad_grad_gpu

@@ -82,6 +82,7 @@ _SIGS = {
     "gbdp_table_to_planar_f64": (_I, [_P, _P, _I, _I, _P]),
     "gbdp_se_a_descriptor_fwd_split_f32": (_I, [_P] * 9 + [_I, _P, _I, _I, _I, _I, _P]),
     "gbdp_fitting_tc_workspace_bytes": (_Z, [_I]),
+    "gbdp_fitting_tc_set_persistent_min_tiles": (None, [_I]),
     "gbdp_fitting_tc_f32": (_I, [_P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P]),
     "gbdp_fitting_tc_status": (_I, [_P, _I, _P]),
     "gbdp_set_autotune": (None, [_I]),

@@ -41,6 +41,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -613,7 +614,8 @@ __global__ void __launch_bounds__(128, 1)
 
 // Persistent form of k_fit_tc for a layer with one main accumulator, used for
 // B1 (20 N tiles of 80 per row block: about 12 tiles per SM on the
-// 12,288-row step; the K-240 layers have about two and run faster as two
+// 12,288-row step) and for the K-240 layers once they have many tiles per
+// SM (on the 12,288-row step they have about two and run faster as two
 // per-tile CTAs per SM): one CTA per SM walks the layer's tiles, the N tiles
 // of a row block consecutively so that they run at the same time on
 // neighbouring SMs and share A through L2.  Warp 0 issues the TMA loads,
@@ -794,7 +796,12 @@ __global__ void __launch_bounds__(192, 1)
       tile_at(tile, row0, n0, nt, t);
       const int yrow = row0 + q * 32;
       float esum = 0.f;
-      const ColP cp{ep.cscale[t] + n0, nullptr, nullptr, nullptr, nullptr};  // B1: scales only
+      // the tile's per-column parameters, read from global memory (the
+      // kinds that read one have it set; every pointer is 16-byte aligned
+      // and n0 a multiple of 16 columns)
+      auto col = [n0](const float* p) { return p ? p + n0 : nullptr; };
+      const ColP cp{ep.cscale[t] + n0, col(ep.bias[t]), col(ep.idt[t]), col(ep.idt2[t]),
+                    col(ep.wout[t])};
       const bool ok = epi_tile<PERS_TBN>(maps, ep, t, yrow, n0, lane, wsm, ib,
                                          tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(j * 256),
                                          1, 0u, 128u, cp, es, esum);
@@ -929,6 +936,15 @@ TcWs carve_tc(void* base, long rows) {
 
 using namespace gbdp;
 
+namespace {
+// tiles per SM from which the K-240 layers run on the persistent kernel
+std::atomic<int> g_short_pers_min_tiles{8};
+}  // namespace
+
+extern "C" void gbdp_fitting_tc_set_persistent_min_tiles(int tiles_per_sm) {
+  g_short_pers_min_tiles.store(tiles_per_sm < 1 ? 1 : tiles_per_sm);
+}
+
 extern "C" size_t gbdp_fitting_tc_workspace_bytes(int rows) {
   return carve_tc(nullptr, rows).bytes + 256;
 }
@@ -996,6 +1012,10 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
                  "fit_tc: idt not 16-byte aligned");
   }
   enum { LONGK = 0, SHORTK, PERSIST };
+  // the K-240 layers go to the persistent kernel from this many tiles per SM
+  const long short_tiles = (rows / TBM) * (FIT_W / CfgShortK::TBN);
+  const int short_cfg =
+      short_tiles >= (long)g_short_pers_min_tiles.load() * nsm ? PERSIST : SHORTK;
   // act: index into act_scale of the split output (-1: none)
   struct Step {
     int kind;
@@ -1014,13 +1034,13 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
       {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}, 0,
        LONGK},
       {EPI_F2, ws.h1h, ws.h1l, FIT_W, FIT_W, 1, true, {ws.t1, nullptr}, {ws.t2, ws.h2h, ws.h2l},
-       1, SHORTK},
+       1, short_cfg},
       {EPI_F3, ws.h2h, ws.h2l, FIT_W, FIT_W, 2, true, {ws.t1, ws.t2},
-       {nullptr, ws.gz3h, ws.gz3l}, 2, SHORTK},
+       {nullptr, ws.gz3h, ws.gz3l}, 2, short_cfg},
       {EPI_B3, ws.gz3h, ws.gz3l, FIT_W, FIT_W, 2, false, {ws.t2, nullptr},
-       {ws.g2, ws.gz2h, ws.gz2l}, 3, SHORTK},
+       {ws.g2, ws.gz2h, ws.gz2l}, 3, short_cfg},
       {EPI_B2, ws.gz2h, ws.gz2l, FIT_W, FIT_W, 1, false, {ws.t1, ws.g2},
-       {nullptr, ws.gz1h, ws.gz1l}, 4, SHORTK},
+       {nullptr, ws.gz1h, ws.gz1l}, 4, short_cfg},
       {EPI_B1, ws.gz1h, ws.gz1l, FIT_W, FIT_D, 0, false, {nullptr, nullptr},
        {dE_dD, nullptr, nullptr}, -1, PERSIST}};
   for (const Step& sp : steps) {

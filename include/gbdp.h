@@ -472,6 +472,13 @@ GBDP_API int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, const
  * run on this workspace (GBDP_OK or GBDP_STATUS_TIMEOUT). */
 GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream stream);
 
+/* Launch-shape control of the tensor-core fitting (no counterpart in the
+ * reference): the four K-240 layers (F2, F3, B3, B2) run as one CTA per
+ * 128 x 80 tile, two per SM, while a layer has fewer than `tiles_per_sm`
+ * tiles per SM (default 8), and on the persistent kernel (one CTA per SM,
+ * double-buffered accumulators) from there on.  Process-wide. */
+GBDP_API void gbdp_fitting_tc_set_persistent_min_tiles(int tiles_per_sm);
+
 /* ---- launch-shape autotuning ----------------------------------------------
  * The fused descriptor kernels (the gbdp_se_a_descriptor_ fwd and bwd entry
  * points) run 1, 2 or 4 centre atoms per CTA, and the FP32 backward 1 or 2

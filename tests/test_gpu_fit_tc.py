@@ -70,3 +70,29 @@ def test_tc_fused_step_vs_fp64(setup):
     assert np.abs(F.cpu().numpy().astype(np.float64) - Fr).max() <= 1e-5
     assert abs(float(E[0]) - Er) / len(frame[1]) <= 1e-6
     assert np.abs(V[0].cpu().numpy() - Vr).max() <= 1e-3
+
+
+def test_persistent_short_k_layers_equal_per_tile(setup):
+    """The K-240 layers on the persistent kernel (forced with a threshold of
+    one tile per SM) give the same bits as one CTA per tile: the same MMAs
+    into the same accumulators and the same epilogue, on a ragged batch of
+    two type blocks."""
+    se_a, cfg, m64, mk, water = setup
+    tc = mk("tc-f16x3")
+    frames = water.ragged_frames(12, seed=31, lo=40, hi=300)
+    b = tc.batch([f[1] for f in frames], np.stack([f[2] for f in frames]))
+    coord = torch.tensor(np.concatenate([f[0] for f in frames]), dtype=torch.float32, device=DEV)
+    lib = tc._lib
+    out = []
+    try:
+        for thr in (1 << 20, 1):
+            lib.gbdp_fitting_tc_set_persistent_min_tiles(thr)
+            E, F, V = tc.step_fused(b, coord)
+            torch.cuda.synchronize()
+            assert lib.gbdp_fitting_tc_status(b.tc_ws.data_ptr(), b.nrows_total,
+                                              torch.cuda.current_stream().cuda_stream) == 0
+            out.append((b.ae.clone(), b.dD.clone(), F.clone(), V.clone()))
+    finally:
+        lib.gbdp_fitting_tc_set_persistent_min_tiles(8)
+    for x, y in zip(out[0], out[1]):
+        assert torch.equal(x, y)

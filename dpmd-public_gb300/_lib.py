@@ -113,6 +113,8 @@ for _s in ("f32", "f64"):
         f"gbdp_tabulate_fusion_se_a_grad_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
         f"gbdp_tabulate_fusion_se_a_grad_grad_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
         f"gbdp_prod_env_mat_a_{_s}": (_I, [_P] * 13 + [_P, _P, _F, _P, _I, _P, _Z, _P]),
+        f"gbdp_prod_env_mat_a_skin_{_s}": (_I, [_P] * 15 + [_F, _F, _P, _I, _I, _P, _P, _I, _P, _P,
+                                                          _P, _Z, _P]),
         f"gbdp_prod_force_a_{_s}": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _Z, _P]),
         f"gbdp_prod_virial_a_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _Z, _P]),
         f"gbdp_prod_force_grad_a_{_s}": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),

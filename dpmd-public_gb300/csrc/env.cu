@@ -543,7 +543,24 @@ __device__ __forceinline__ void warp_bitonic128(uint64_t* v, int lane) {
   }
 }
 
-template <typename T>
+// Verlet list of a skin build: per centre up to `cap` frame-local extended
+// indices (every extended atom within rcut + skin at the last rebuild, in
+// stencil order), their count, and the extended types.
+struct VList {
+  int* idx;    // [nloc_total, cap]
+  int* cnt;    // [nloc_total]
+  int cap;
+  const int* ext_type;
+};
+
+// Modes of k_nlist_env:
+//   kEnvCells  candidates from the cell stencil, formatted list + env rows
+//   kEnvList   candidates from the Verlet list, formatted list + env rows
+//   kEnvBuild  candidates from the cell stencil (rc2f = (rcut + skin)^2)
+//              written to the Verlet list; nothing else
+enum { kEnvCells = 0, kEnvList = 1, kEnvBuild = 2 };
+
+template <typename T, int MODE>
 __global__ void __launch_bounds__(kEnvWarps * 32)
     k_nlist_env(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
                 const int* __restrict__ atom_frame, const int* __restrict__ atom_cell,
@@ -553,7 +570,7 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
                 const T* __restrict__ avg, const T* __restrict__ stdv, SecInfo si, float rc2f,
                 T rmin, T rmax, int max_cand, T* __restrict__ em, T* __restrict__ em_deriv,
                 T* __restrict__ rij, int* __restrict__ nlist, int* __restrict__ nlist_ext,
-                int* __restrict__ status) {
+                int* __restrict__ status, VList vl) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kEnvWarps + warp;
@@ -571,7 +588,8 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   const T xi = ext_coord[3 * (eoff + il)], yi = ext_coord[3 * (eoff + il) + 1],
           zi = ext_coord[3 * (eoff + il) + 2];
   const int ti = atype[i];
-  const int c = atom_cell[i] - g.cell_off;
+  // (the list mode reads no cell data: its launches pass no cell arrays)
+  const int c = MODE == kEnvList ? 0 : atom_cell[i] - g.cell_off;
   const int c0 = c / (g.ncell[1] * g.ncell[2]);
   const int c1 = (c / g.ncell[2]) % g.ncell[1];
   const int c2 = c % g.ncell[2];
@@ -583,8 +601,38 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   //      tests 32 candidates across cell boundaries (the owning cell found by
   //      a binary search over the scan with shuffles)
   int ncand = 0;
+  if (MODE == kEnvList) {
+    // ---- the Verlet list's entries, 32 per pass, with the current
+    //      coordinates (refreshed from the local atoms since the rebuild)
+    const int* L = vl.idx + (size_t)i * vl.cap;
+    const int nl_i = min(vl.cnt[i], vl.cap);
+    for (int base = 0; base < nl_i; base += 32) {
+      const int f = base + lane;
+      bool ok = false;
+      uint64_t key = 0;
+      int t = 0;
+      if (f < nl_i) {
+        const int idx = L[f];
+        const size_t ej = eoff + idx;
+        t = vl.ext_type[ej];
+        const auto r = make_xs(ext_coord[3 * ej], ext_coord[3 * ej + 1], ext_coord[3 * ej + 2],
+                               pack_idx_type(idx, t));
+        float k2;
+        ok = cand_test<T>(r, xi, yi, zi, rc2f, k2) && idx != il && t >= 0 && t < si.ntypes;
+        key = ((uint64_t)__float_as_uint(k2) << 32) | (uint32_t)idx;
+      }
+      const unsigned m = __ballot_sync(kFull, ok);
+      const int pos = ncand + __popc(m & ((1u << lane) - 1u));
+      if (ok && pos < max_cand) {
+        keys[pos] = key;
+        ctype[pos] = (unsigned char)t;
+      }
+      ncand += __popc(m);
+    }
+  }
   const int sy = 2 * g.stencil[1] + 1, sz = 2 * g.stencil[2] + 1;
-  const int nst = (2 * g.stencil[0] + 1) * sy * sz;
+  const int nst = MODE == kEnvList ? 0 : (2 * g.stencil[0] + 1) * sy * sz;
+  int* vrow = MODE == kEnvBuild ? vl.idx + (size_t)i * vl.cap : nullptr;
   for (int cg = 0; cg < nst; cg += 32) {
     const int q = cg + lane;
     int st = 0, cnt = 0;
@@ -629,12 +677,21 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
       }
       const unsigned m = __ballot_sync(kFull, ok);
       const int pos = ncand + __popc(m & ((1u << lane) - 1u));
-      if (ok && pos < max_cand) {
+      if (MODE == kEnvBuild) {
+        if (ok && pos < vl.cap) vrow[pos] = (int)(uint32_t)(key & 0xffffffffu);
+      } else if (ok && pos < max_cand) {
         keys[pos] = key;
         ctype[pos] = (unsigned char)t;
       }
       ncand += __popc(m);
     }
+  }
+  if (MODE == kEnvBuild) {
+    if (lane == 0) {
+      vl.cnt[i] = ncand;
+      if (ncand > vl.cap) raise_status(status, GBDP_STATUS_CAND_OVERFLOW);
+    }
+    return;
   }
   if (ncand > max_cand) {
     if (lane == 0) raise_status(status, GBDP_STATUS_CAND_OVERFLOW);
@@ -896,23 +953,13 @@ int env_check_args(const T* em, const T* em_deriv, const int* nlist, const T* ex
   return GBDP_OK;
 }
 
+// The cell build and ghost images of the periodic pipeline (k_localize ..
+// k_ghost_fill); clears the status word and the cell counters first.
 template <typename T>
-int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
-               int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
-               const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
-               const gbdp_nbr_frame* frames, float rcut_smth, const int* sel, int ntypes,
-               void* workspace, size_t ws_bytes, cudaStream_t stream) {
-  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a: null plan/frames/workspace");
-  SecInfo si;
-  const int chk = env_check_args<T>(em, em_deriv, nlist, ext_coord, ext_type, ext_map, ext_nall,
-                                    coord, atype, avg, stdv, plan, sel, ntypes, &si);
-  if (chk) return chk;
-  const int fp64 = sizeof(T) == 8;
-  EnvWs w = carve(*plan, workspace, fp64);
-  GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_env_mat_a: workspace %zu < %zu bytes", ws_bytes,
-               w.bytes);
+void env_ghosts(const EnvWs& w, T* ext_coord, int* ext_type, int* ext_map, int* ext_nall,
+                const T* coord, const int* atype, const gbdp_nbr_plan* plan,
+                const gbdp_nbr_frame* frames, cudaStream_t stream) {
   const int nl = plan->nloc_total;
-  if (nl == 0) return GBDP_OK;
   cudaMemsetAsync(w.status, 0, w.zero_bytes, stream);
   const int tb = 256;
   k_localize<T><<<(nl + tb - 1) / tb, tb, 0, stream>>>(frames, plan->nframes, nl, coord, atype,
@@ -931,17 +978,146 @@ int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_co
       frames, plan->nframes, nec, w.cell_start, w.cell_count, w.cell_atoms, w.ext_start,
       w.ghost_start, ext_coord, ext_type, ext_map,
       static_cast<typename XsOf<T>::type*>(w.xs));
+}
+
+// One launch of k_nlist_env in the given mode (candidates within rc).
+template <typename T, int MODE>
+void nlist_env_mode(const EnvWs& w, const gbdp_nbr_plan* plan, const gbdp_nbr_frame* frames,
+                    const SecInfo& si, float rc, float rcut_smth, float rmax, T* em, T* em_deriv,
+                    T* rij, int* nlist, int* nlist_ext, const T* ext_coord, const int* ext_map,
+                    const int* atype, const T* avg, const T* stdv, const VList& vl,
+                    cudaStream_t stream) {
+  const int nl = plan->nloc_total;
   const int mc = plan->max_cand;
-  const size_t smem = nlist_env_smem(mc, si.nnei);
-  auto kern = k_nlist_env<T>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-  const float rc = plan->rcut;
+  const size_t smem = MODE == kEnvBuild ? 0 : nlist_env_smem(mc, si.nnei);
+  auto kern = k_nlist_env<T, MODE>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const bool cells = MODE != kEnvList;
   kern<<<(nl + kEnvWarps - 1) / kEnvWarps, kEnvWarps * 32, smem, stream>>>(
-      nl, frames, w.atom_frame, w.atom_cell, w.ext_start, w.ext_cnt,
-      static_cast<const typename XsOf<T>::type*>(w.xs), ext_coord, ext_map, atype, avg, stdv, si,
-      rc * rc, (T)rcut_smth, (T)rc, mc, em, em_deriv, rij, nlist, nlist_ext, w.status);
+      nl, frames, w.atom_frame, cells ? w.atom_cell : nullptr, cells ? w.ext_start : nullptr,
+      cells ? w.ext_cnt : nullptr,
+      cells ? static_cast<const typename XsOf<T>::type*>(w.xs) : nullptr, ext_coord, ext_map,
+      atype, avg, stdv, si, rc * rc, (T)rcut_smth, (T)rmax, mc, em, em_deriv, rij, nlist,
+      nlist_ext, w.status, vl);
+}
+
+template <typename T>
+int env_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
+               int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
+               const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
+               const gbdp_nbr_frame* frames, float rcut_smth, const int* sel, int ntypes,
+               void* workspace, size_t ws_bytes, cudaStream_t stream) {
+  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a: null plan/frames/workspace");
+  SecInfo si;
+  const int chk = env_check_args<T>(em, em_deriv, nlist, ext_coord, ext_type, ext_map, ext_nall,
+                                    coord, atype, avg, stdv, plan, sel, ntypes, &si);
+  if (chk) return chk;
+  const int fp64 = sizeof(T) == 8;
+  EnvWs w = carve(*plan, workspace, fp64);
+  GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_env_mat_a: workspace %zu < %zu bytes", ws_bytes,
+               w.bytes);
+  if (plan->nloc_total == 0) return GBDP_OK;
+  env_ghosts<T>(w, ext_coord, ext_type, ext_map, ext_nall, coord, atype, plan, frames, stream);
+  nlist_env_mode<T, kEnvCells>(w, plan, frames, si, plan->rcut, rcut_smth, plan->rcut, em,
+                               em_deriv, rij, nlist, nlist_ext, ext_coord, ext_map, atype, avg,
+                               stdv, VList{nullptr, nullptr, 0, nullptr}, stream);
   GBDP_CHECK_LAUNCH("prod_env_mat_a");
+  return GBDP_OK;
+}
+
+// ------------------------------------------------------- Verlet (skin) list --
+__device__ __forceinline__ int find_frame_ext(const gbdp_nbr_frame* fr, int nframes, int e) {
+  int lo = 0, hi = nframes - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].ext_off <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// At a rebuild: the source local atom (packed index) of every filled
+// extended slot, and the shift from that atom's input coordinate to the
+// slot's coordinate (the wrap into the box, plus the image vector of a
+// ghost); unfilled slots get source -1.
+template <typename T>
+__global__ void k_ext_shift(const gbdp_nbr_frame* __restrict__ fr, int nframes, int ext_total,
+                            const int* __restrict__ ext_nall, const int* __restrict__ ext_map,
+                            const T* __restrict__ coord, const T* __restrict__ ext_coord,
+                            T* __restrict__ shift, int* __restrict__ src) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ext_total) return;
+  const int f = find_frame_ext(fr, nframes, e);
+  const gbdp_nbr_frame& g = fr[f];
+  const int el = e - g.ext_off;
+  if (el >= ext_nall[f] || el >= g.ext_cap) {
+    src[e] = -1;
+    return;
+  }
+  const int a = g.atom_off + ext_map[e];
+  src[e] = a;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) shift[3 * (size_t)e + d] = ext_coord[3 * (size_t)e + d] - coord[3 * (size_t)a + d];
+}
+
+// Between rebuilds: every filled extended slot follows its source atom.
+template <typename T>
+__global__ void k_ext_refresh(int ext_total, const int* __restrict__ src,
+                              const T* __restrict__ shift, const T* __restrict__ coord,
+                              T* __restrict__ ext_coord) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ext_total) return;
+  const int a = src[e];
+  if (a < 0) return;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    ext_coord[3 * (size_t)e + d] = coord[3 * (size_t)a + d] + shift[3 * (size_t)e + d];
+}
+
+template <typename T>
+int env_skin_launch(T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord,
+                    int* ext_type, int* ext_map, int* ext_nall, const T* coord, const int* atype,
+                    const T* avg, const T* stdv, const gbdp_nbr_plan* plan,
+                    const gbdp_nbr_frame* frames, float rcut, float rcut_smth, const int* sel,
+                    int ntypes, int rebuild, int* vlist, int* vcnt, int vcap, T* ext_shift,
+                    int* ext_src, void* workspace, size_t ws_bytes, cudaStream_t stream) {
+  GBDP_REQUIRE(plan && frames && workspace, "prod_env_mat_a_skin: null plan/frames/workspace");
+  SecInfo si;
+  const int chk = env_check_args<T>(em, em_deriv, nlist, ext_coord, ext_type, ext_map, ext_nall,
+                                    coord, atype, avg, stdv, plan, sel, ntypes, &si);
+  if (chk) return chk;
+  GBDP_REQUIRE(vlist && vcnt && ext_shift && ext_src && vcap >= 1,
+               "prod_env_mat_a_skin: null Verlet-list buffer or capacity < 1");
+  GBDP_REQUIRE(rcut > 0.f && rcut <= plan->rcut,
+               "prod_env_mat_a_skin: rcut %g must be positive and at most the plan's %g", rcut,
+               plan->rcut);
+  const int fp64 = sizeof(T) == 8;
+  EnvWs w = carve(*plan, workspace, fp64);
+  GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_env_mat_a_skin: workspace %zu < %zu bytes", ws_bytes,
+               w.bytes);
+  const int nl = plan->nloc_total;
+  if (nl == 0) return GBDP_OK;
+  const VList vl{vlist, vcnt, vcap, ext_type};
+  const int ne = plan->ext_total;
+  if (rebuild) {
+    env_ghosts<T>(w, ext_coord, ext_type, ext_map, ext_nall, coord, atype, plan, frames, stream);
+    k_ext_shift<T><<<(ne + 255) / 256, 256, 0, stream>>>(frames, plan->nframes, ne, ext_nall,
+                                                         ext_map, coord, ext_coord, ext_shift,
+                                                         ext_src);
+    nlist_env_mode<T, kEnvBuild>(w, plan, frames, si, plan->rcut, rcut_smth, rcut, em, em_deriv,
+                                 rij, nlist, nlist_ext, ext_coord, ext_map, atype, avg, stdv, vl,
+                                 stream);
+  } else {
+    cudaMemsetAsync(w.status, 0, sizeof(int), stream);
+    k_ext_refresh<T><<<(ne + 255) / 256, 256, 0, stream>>>(ne, ext_src, ext_shift, coord,
+                                                           ext_coord);
+  }
+  nlist_env_mode<T, kEnvList>(w, plan, frames, si, rcut, rcut_smth, rcut, em, em_deriv, rij,
+                              nlist, nlist_ext, ext_coord, ext_map, atype, avg, stdv, vl, stream);
+  GBDP_CHECK_LAUNCH("prod_env_mat_a_skin");
   return GBDP_OK;
 }
 
@@ -1130,6 +1306,22 @@ extern "C" int gbdp_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij
                             ext_nall, coord, atype, avg, std, plan, frames_dev, rcut_smth, sel,
                             ntypes, workspace, workspace_bytes, (cudaStream_t)stream);
 }
+
+#define GBDP_ENV_SKIN_ENTRY(T, SFX)                                                             \
+  extern "C" int gbdp_prod_env_mat_a_skin_##SFX(                                                \
+      T* em, T* em_deriv, T* rij, int* nlist, int* nlist_ext, T* ext_coord, int* ext_type,       \
+      int* ext_map, int* ext_nall, const T* coord, const int* atype, const T* avg, const T* std, \
+      const gbdp_nbr_plan* plan, const gbdp_nbr_frame* frames_dev, float rcut, float rcut_smth, \
+      const int* sel, int ntypes, int rebuild, int* vlist, int* vcnt, int vcap, T* ext_shift,    \
+      int* ext_src, void* workspace, size_t workspace_bytes, gbdp_stream stream) {              \
+    return env_skin_launch<T>(em, em_deriv, rij, nlist, nlist_ext, ext_coord, ext_type, ext_map, \
+                              ext_nall, coord, atype, avg, std, plan, frames_dev, rcut,          \
+                              rcut_smth, sel, ntypes, rebuild, vlist, vcnt, vcap, ext_shift,     \
+                              ext_src, workspace, workspace_bytes, (cudaStream_t)stream);        \
+  }
+GBDP_ENV_SKIN_ENTRY(float, f32)
+GBDP_ENV_SKIN_ENTRY(double, f64)
+#undef GBDP_ENV_SKIN_ENTRY
 
 #define GBDP_ENV_NLIST_ENTRY(T, SFX)                                                           \
   extern "C" int gbdp_prod_env_mat_a_nlist_##SFX(                                              \

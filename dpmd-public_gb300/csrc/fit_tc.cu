@@ -938,7 +938,10 @@ using namespace gbdp;
 
 namespace {
 // tiles per SM from which the K-240 layers run on the persistent kernel
-std::atomic<int> g_short_pers_min_tiles{8};
+// (measured on the ragged water batches: per-tile and persistent within 1 %
+// from 4 to 60 tiles per SM; the layers are bound by their activation
+// traffic, not by launches)
+std::atomic<int> g_short_pers_min_tiles{32};
 }  // namespace
 
 extern "C" void gbdp_fitting_tc_set_persistent_min_tiles(int tiles_per_sm) {

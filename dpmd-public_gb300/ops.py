@@ -280,6 +280,48 @@ def env_mat_packed(plan: NeighborPlan, coord, atype, avg, std, rcut_smth, sel,
         return r
 
 
+class VerletList:
+    """Buffers of the skin form of the env pipeline (kept between calls):
+    per centre up to ``cap`` extended indices within rcut + skin of the last
+    rebuild, their count, and each extended slot's source atom and shift."""
+
+    def __init__(self, plan: NeighborPlan, cap: int = 0):
+        dev, dt = plan.device, plan.dtype
+        self.cap = int(cap) if cap > 0 else plan.max_cand
+        n, ne = plan.nloc_total, plan.ext_total
+        self.idx = torch.empty((n, self.cap), dtype=torch.int32, device=dev)
+        self.cnt = torch.zeros((n,), dtype=torch.int32, device=dev)
+        self.shift = torch.empty((ne, 3), dtype=dt, device=dev)
+        self.src = torch.full((ne,), -1, dtype=torch.int32, device=dev)
+
+
+def env_mat_skin(plan: NeighborPlan, vl: VerletList, coord, atype, avg, std, rcut: float,
+                 rcut_smth, sel, rebuild: bool, out: EnvMatResult,
+                 check_status: bool = False) -> EnvMatResult:
+    """The env pipeline on a Verlet list: ``plan`` made with rcut + skin;
+    ``rebuild`` rebuilds ghosts and the list, otherwise the ghosts follow
+    the local atoms and the list of the last rebuild is formatted at rcut.
+    Outputs go to ``out`` (no allocation)."""
+    _need_cuda(coord, atype, avg, std)
+    dt = plan.dtype
+    selc = (ctypes.c_int * len(sel))(*[int(s) for s in sel])
+    fn = getattr(L.load(), f"gbdp_prod_env_mat_a_skin_{L.sfx(dt)}")
+    r = out
+    L.check(fn(_ptr(r.em), _ptr(r.em_deriv), _ptr(r.rij), _ptr(r.nlist), _ptr(r.nlist_ext),
+               _ptr(r.ext_coord), _ptr(r.ext_type), _ptr(r.ext_map), _ptr(r.ext_nall),
+               _ptr(coord), _ptr(atype), _ptr(avg), _ptr(std), ctypes.byref(plan.plan),
+               _ptr(plan.frames_dev), ctypes.c_float(rcut), ctypes.c_float(rcut_smth), selc,
+               len(sel), int(bool(rebuild)), _ptr(vl.idx), _ptr(vl.cnt), vl.cap, _ptr(vl.shift),
+               _ptr(vl.src), _ptr(plan.workspace), ctypes.c_size_t(plan.ws_bytes), _stream()),
+            "prod_env_mat_a_skin")
+    if check_status:
+        st = L.load().gbdp_env_status(_ptr(plan.workspace), _stream())
+        if st != 0:
+            raise L.GbdpError(f"prod_env_mat_a_skin device status {st}: "
+                              f"{L.GBDP_STATUS.get(st, '?')}")
+    return r
+
+
 # ---------------------------------------------------- TF-contract ops --
 _PLAN_CACHE: dict = {}
 

@@ -31,7 +31,8 @@ import torch
 
 from . import _lib as L
 from . import model as mdl
-from .ops import EnvMatResult, NeighborPlan, env_mat_packed, prod_force_se_a_impl, prod_virial_se_a_impl
+from .ops import (EnvMatResult, NeighborPlan, VerletList, env_mat_packed, env_mat_skin,
+                  prod_force_se_a_impl, prod_virial_se_a_impl)
 
 _P = ctypes.c_void_p
 
@@ -236,8 +237,8 @@ class SeAModel:
         return dst
 
     # ------------------------------------------------------------- batches --
-    def batch(self, atype_per_frame, boxes, max_cand: int = 0) -> "Batch":
-        return Batch(self, atype_per_frame, boxes, max_cand)
+    def batch(self, atype_per_frame, boxes, max_cand: int = 0, skin: float = 0.0) -> "Batch":
+        return Batch(self, atype_per_frame, boxes, max_cand, skin)
 
     # ------------------------------------------------------------ fitting --
     def _mm(self, a: torch.Tensor, w: torch.Tensor, out=None):
@@ -304,14 +305,19 @@ class SeAModel:
         return torch.addmm(bf, h, wf)[:, 0] + self.bias_atom_e[t]
 
     # ------------------------------------------------------- chosen form --
-    def step_fused(self, b: "Batch", coord: torch.Tensor, deterministic: bool | None = None):
+    def step_fused(self, b: "Batch", coord: torch.Tensor, deterministic: bool | None = None,
+                   rebuild: bool = True):
         """E [nframes] f64, F [nloc_total, 3], virial [nframes, 9] f64.
         deterministic: forces, virials and energies summed in 64-bit fixed
         point, the same bits on every run (floating-point atomics otherwise).
         Default: on for FP32 models (its 2^-32 eV/A grid is far below FP32
         rounding, and the integer sums measured faster than the FP64
         atomics of the frame virial), off for FP64 models (whose rounding is
-        finer than the 2^-40 grid)."""
+        finer than the 2^-40 grid).
+        rebuild: for a batch made with a skin, rebuild the Verlet list (and
+        ghosts) at this step; otherwise the list of the last rebuild is
+        reused with the ghosts following their atoms.  A batch without a
+        skin rebuilds at every step."""
         if deterministic is None:
             deterministic = self.dtype == torch.float32
         cfg = self.cfg
@@ -319,8 +325,12 @@ class SeAModel:
             raise RuntimeError("the fused form needs the compression tables")
         M, A = cfg.neuron[-1], cfg.axis_neuron
         n = b.nloc
-        env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth, list(cfg.sel),
-                       check_status=False, out=b.env)
+        if b.skin > 0:
+            env_mat_skin(b.plan, b.vl, coord, b.atype, self.davg, self.dstd, cfg.rcut,
+                         cfg.rcut_smth, list(cfg.sel), rebuild, out=b.env)
+        else:
+            env_mat_packed(b.plan, coord, b.atype, self.davg, self.dstd, cfg.rcut_smth,
+                           list(cfg.sel), check_status=False, out=b.env)
         lib = self._lib
         if self._tc_nets is not None:
             L.check(lib.gbdp_se_a_descriptor_fwd_split_f32(
@@ -693,14 +703,20 @@ class Batch:
     buffer the fused step writes (fixed addresses, so the step can be
     captured in a CUDA graph)."""
 
-    def __init__(self, model: SeAModel, atype_per_frame, boxes, max_cand: int = 0):
+    def __init__(self, model: SeAModel, atype_per_frame, boxes, max_cand: int = 0,
+                 skin: float = 0.0):
+        """skin > 0: the neighbour search covers rcut + skin and keeps a
+        Verlet list, which steps reuse between rebuilds (step_fused's
+        ``rebuild``)."""
         cfg = model.cfg
         dev = model.device
         dt = model.dtype
         at = [np.asarray(a, np.int32).reshape(-1) for a in atype_per_frame]
         self.nframes = len(at)
+        self.skin = float(skin)
         self.plan = NeighborPlan([len(a) for a in at], np.asarray(boxes, np.float64).reshape(-1, 9),
-                                 cfg.rcut, dev, dt, max_cand=max_cand)
+                                 cfg.rcut + self.skin, dev, dt, max_cand=max_cand)
+        self.vl = VerletList(self.plan) if self.skin > 0 else None
         self.nloc = int(self.plan.nloc_total)
         flat = np.concatenate(at)
         self.atype = torch.tensor(flat, dtype=torch.int32, device=dev)

@@ -224,6 +224,45 @@ GBDP_API int gbdp_prod_env_mat_a_nlist_f64(double* em, double* em_deriv, double*
                                            float rcut_smth, const int* sel, int ntypes,
                                            gbdp_stream stream);
 
+/* Verlet-list (skin) form of gbdp_prod_env_mat_a_*, for MD steps that
+ * rebuild the neighbour list every few steps, as the reference's LAMMPS
+ * path reuses an rcut + skin list between rebuilds
+ * (source/api_cc/src/DeepPotPT.cc:311-330, list formatted by
+ * deepmd/pt/model/model/make_model.py:541-598 and sorted as se_a asks,
+ * deepmd/pt/model/descriptor/se_a.py:872-883).  No single reference
+ * function: it combines the periodic build with the formatting of a stored
+ * list.  The plan is made with the cutoff rcut + skin (its cells and ghost
+ * images cover that range); `rcut` is the model cutoff (<= plan->rcut).
+ *   rebuild != 0  the ghost images and cells are built as by
+ *                 gbdp_prod_env_mat_a_*, ext_src / ext_shift record each
+ *                 filled extended slot's local source atom (packed index)
+ *                 and its offset from that atom's coordinate, and vlist
+ *                 [nloc_total, vcap] / vcnt [nloc_total] receive every
+ *                 extended atom within plan->rcut of each centre;
+ *   rebuild == 0  ext_coord is refreshed as coord[ext_src] + ext_shift and
+ *                 nothing else is rebuilt.
+ * Either way the outputs are formed from the stored candidates within
+ * rcut of the current coordinates, in the canonical order (type, float
+ * r^2, extended index; indices of the last rebuild).  A centre with more
+ * than vcap candidates raises GBDP_STATUS_CAND_OVERFLOW (rebuild again with
+ * a larger vcap).  The caller keeps vlist, vcnt, ext_shift [ext_total, 3],
+ * ext_src [ext_total], the outputs and the workspace between calls and
+ * rebuilds before the atoms have moved by more than half the skin. */
+GBDP_API int gbdp_prod_env_mat_a_skin_f32(
+    float* em, float* em_deriv, float* rij, int* nlist, int* nlist_ext, float* ext_coord,
+    int* ext_type, int* ext_map, int* ext_nall, const float* coord, const int* atype,
+    const float* avg, const float* std, const gbdp_nbr_plan* plan,
+    const gbdp_nbr_frame* frames_dev, float rcut, float rcut_smth, const int* sel, int ntypes,
+    int rebuild, int* vlist, int* vcnt, int vcap, float* ext_shift, int* ext_src,
+    void* workspace, size_t workspace_bytes, gbdp_stream stream);
+GBDP_API int gbdp_prod_env_mat_a_skin_f64(
+    double* em, double* em_deriv, double* rij, int* nlist, int* nlist_ext, double* ext_coord,
+    int* ext_type, int* ext_map, int* ext_nall, const double* coord, const int* atype,
+    const double* avg, const double* std, const gbdp_nbr_plan* plan,
+    const gbdp_nbr_frame* frames_dev, float rcut, float rcut_smth, const int* sel, int ntypes,
+    int rebuild, int* vlist, int* vcnt, int vcap, double* ext_shift, int* ext_src,
+    void* workspace, size_t workspace_bytes, gbdp_stream stream);
+
 /* Allocation-free variant of gbdp_prod_env_mat_a_f32 (float only).  It has
  * no counterpart in the reference.  It is for callers that cannot allocate
  * device memory at the point of the call: a host MD engine that owns all
@@ -475,7 +514,7 @@ GBDP_API int gbdp_fitting_tc_status(const void* workspace, int rows, gbdp_stream
 /* Launch-shape control of the tensor-core fitting (no counterpart in the
  * reference): the four K-240 layers (F2, F3, B3, B2) run as one CTA per
  * 128 x 80 tile, two per SM, while a layer has fewer than `tiles_per_sm`
- * tiles per SM (default 8), and on the persistent kernel (one CTA per SM,
+ * tiles per SM (default 32), and on the persistent kernel (one CTA per SM,
  * double-buffered accumulators) from there on.  Process-wide. */
 GBDP_API void gbdp_fitting_tc_set_persistent_min_tiles(int tiles_per_sm);
 

@@ -93,6 +93,6 @@ def test_persistent_short_k_layers_equal_per_tile(setup):
                                               torch.cuda.current_stream().cuda_stream) == 0
             out.append((b.ae.clone(), b.dD.clone(), F.clone(), V.clone()))
     finally:
-        lib.gbdp_fitting_tc_set_persistent_min_tiles(8)
+        lib.gbdp_fitting_tc_set_persistent_min_tiles(32)
     for x, y in zip(out[0], out[1]):
         assert torch.equal(x, y)

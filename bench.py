@@ -893,7 +893,9 @@ def train_workload(args):
 def md_workload(args):
     """262,144 H2O (786,432 atoms) in a 198.7 A box (64-molecule cell
     replicated 16^3, jittered), 330 K Maxwell-Boltzmann, velocity-Verlet
-    NVE, dt 0.5 fs, the whole step captured in a CUDA graph."""
+    NVE, dt 0.5 fs, the whole step captured in a CUDA graph; a 2 A skin
+    with the Verlet list rebuilt every 10 steps (--md-skin 0: rebuilt every
+    step)."""
     import importlib
 
     import torch
@@ -914,8 +916,8 @@ def md_workload(args):
     md = importlib.import_module("dpmd_public_gb300.md")
     c, t, b = water.replicated_frame(4, 12.42, 16, SEED)
     v = md.maxwell_boltzmann(t, 330.0, SEED)
-    batch = model.batch([t], b[None])
-    nve = md.NVE(model, batch, c, v, t, dt=0.5)
+    batch = model.batch([t], b[None], skin=args.md_skin)
+    nve = md.NVE(model, batch, c, v, t, dt=0.5, rebuild_every=args.md_rebuild)
     nve.capture()
     e0 = nve.total_energy()
     torch.cuda.synchronize()
@@ -941,7 +943,9 @@ def md_workload(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic", "config": {
                "workload": "262144 H2O (786432 atoms), 198.7 A box, NVE velocity-Verlet dt 0.5 fs, "
-                           "330 K, whole step in one CUDA graph, nlist rebuilt every step",
+                           "330 K, whole step in a CUDA graph, " + (
+                               f"{args.md_skin:g} A skin, list rebuilt every {args.md_rebuild} steps"
+                               if args.md_skin > 0 else "nlist rebuilt every step"),
                "atoms": nat, "fitting_gemm": args.fit_mode,
                "model": f"random weights, fitting output layer x {args.md_out_scale}"},
            "energy_drift_eV_per_atom_per_ps": drift,

@@ -1,13 +1,18 @@
 """The Verlet-list (skin) form of the env pipeline and of the MD step.
 
 After a rebuild at rcut + skin, the atoms move by up to 0.6 A (less than
-half the 2 A skin) and the list is reused: the neighbour list (mapped to
-local atoms) equals a fresh build's at the new coordinates element by
-element, and the env rows agree within the env tolerances (fp64 1e-12,
-fp32 5e-6: the refreshed ghost coordinates round once more than freshly
-built ones).  The fused step on a reused list gives the energy, forces and
-virial of a fresh step; NVE with a rebuild every 10 steps follows the
-trajectory that rebuilds at every step."""
+half the 2 A skin) and the list is reused: the formatted list equals, bit
+for bit, the reference's formatting (oracle format_nlist: build_nlist_cpu +
+format_nlist_cpu) of the extended coordinates the step used, the ghosts
+refreshed from their atoms.  In fp64 it also equals a fresh build's at the
+new coordinates element by element, with the env rows within 1e-12 (values)
+and 1e-10 (derivative rows: a refreshed ghost coordinate, coord + shift,
+rounds differently from a freshly built one, coord - image vector, and the
+derivative rows amplify that).  In fp32 that rounding difference is large
+enough to swap neighbours whose float r^2 are within an ulp, so the fp32
+check is the oracle's formatting alone.  The fused step on a reused list
+gives the energy, forces and virial of a fresh step; NVE with a rebuild
+every 10 steps follows the trajectory that rebuilds at every step."""
 
 import importlib
 
@@ -52,7 +57,7 @@ def _displace(c, seed, amp=0.6):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_reused_list_matches_fresh_build(gb, mods, dtype):
+def test_reused_list_matches_fresh_build(gb, oracle, mods, dtype):
     se_a, mdl, water, ops = mods
     frames = _frames(water)
     avg_n, std_n = _stats()
@@ -78,16 +83,30 @@ def test_reused_list_matches_fresh_build(gb, mods, dtype):
     tol = dict(atol=1e-12, rtol=1e-12) if dtype == torch.float64 else dict(atol=5e-6, rtol=5e-6)
     dtol = dict(atol=1e-10, rtol=1e-10) if dtype == torch.float64 else dict(atol=2e-5, rtol=2e-5)
     plan = gb.NeighborPlan(nl, boxes, 6.0, DEV, dtype)
+    npd = np.float64 if dtype == torch.float64 else np.float32
     for step, c in enumerate([c0, _displace(c0, 1), _displace(c0, 2)]):
         ct = torch.tensor(c, dtype=dtype, device=DEV)
         ops.env_mat_skin(skin_plan, vl, ct, t, avg, std, 6.0, 0.5, SEL, rebuild=(step == 0),
                          out=out, check_status=True)
-        fresh = gb.env_mat_packed(plan, ct, t, avg, std, 0.5, SEL)
         torch.cuda.synchronize()
-        assert torch.equal(out.nlist, fresh.nlist), step
-        torch.testing.assert_close(out.em, fresh.em, **tol)
-        torch.testing.assert_close(out.em_deriv, fresh.em_deriv, **dtol)
-        torch.testing.assert_close(out.rij, fresh.rij, **tol)
+        # the reference's formatting of the extended coordinates the step
+        # used (ghosts refreshed from their atoms): bit-exact
+        for f in range(len(frames)):
+            a0, n_f = int(skin_plan.atom_off[f]), nl[f]
+            e0, ne = int(skin_plan.ext_off[f]), int(out.ext_nall[f])
+            ec = out.ext_coord[e0:e0 + ne].cpu().numpy().astype(npd)
+            et = out.ext_type[e0:e0 + ne].cpu().numpy()
+            ref = oracle.format_nlist(ec, et, n_f, 6.0, SEL)
+            np.testing.assert_array_equal(out.nlist_ext[a0:a0 + n_f].cpu().numpy(), ref)
+        if dtype == torch.float64:
+            # and a fresh build at the same coordinates (its ghosts round the
+            # same within 1e-15 A: no near-tie can swap)
+            fresh = gb.env_mat_packed(plan, ct, t, avg, std, 0.5, SEL)
+            torch.cuda.synchronize()
+            assert torch.equal(out.nlist, fresh.nlist), step
+            torch.testing.assert_close(out.em, fresh.em, **tol)
+            torch.testing.assert_close(out.em_deriv, fresh.em_deriv, **dtol)
+            torch.testing.assert_close(out.rij, fresh.rij, **tol)
 
 
 def test_fused_step_on_reused_list(gb, mods):

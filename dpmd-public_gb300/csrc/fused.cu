@@ -497,9 +497,22 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
   V4<T>* dy4 = reinterpret_cast<V4<T>*>(wbase);
   V4<T>* xT = dy4 + MP;  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k)
   T* xTs = reinterpret_cast<T*>(xT);
-  for (int u = lane; u < 4 * M; u += 32) {
-    const int m = u / M, k = u - m * M;
-    xTs[4 * k + m] = ld_stream(X + (size_t)i * 4 * M + u);
+  // all of X's loads issued before the first is stored (no dependent chain)
+  {
+    T xv[4 * NQ];
+#pragma unroll
+    for (int q = 0; q < 4 * NQ; ++q) {
+      const int u = q * 32 + lane;
+      xv[q] = u < 4 * M ? ld_stream(X + (size_t)i * 4 * M + u) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 4 * NQ; ++q) {
+      const int u = q * 32 + lane;
+      if (u < 4 * M) {
+        const int m = u / M, k = u - m * M;
+        xTs[4 * k + m] = xv[q];
+      }
+    }
   }
   __syncwarp();
   const size_t drow_i = drow ? (size_t)drow[i] : (size_t)i;
@@ -536,17 +549,31 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
     }
   }
   __syncwarp();
-  // ---- ... + dD^T X for the first A columns: two half-warps split kk
+  // ---- ... + dD^T X for the first A columns: two half-warps split kk;
+  //      the loads of kDtxBatch rows are issued before they are used, so
+  //      the pass waits for one memory round trip per batch, not per row
   {
+    constexpr int kDtxBatch = 10;
     const int h = lane >> 4, kc = lane & 15;
     T s[4] = {T(0), T(0), T(0), T(0)};
-    for (int kk = h; kk < M; kk += 2) {
-      const T g = ld_first(g_i + kk * kAxis + kc);
-      const V4<T> x4 = xT[kk];
-      s[0] += g * x4.x;
-      s[1] += g * x4.y;
-      s[2] += g * x4.z;
-      s[3] += g * x4.w;
+    for (int kk0 = h; kk0 < M; kk0 += 2 * kDtxBatch) {
+      T gv[kDtxBatch];
+#pragma unroll
+      for (int u = 0; u < kDtxBatch; ++u) {
+        const int kk = kk0 + 2 * u;
+        gv[u] = kk < M ? ld_first(g_i + kk * kAxis + kc) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kDtxBatch; ++u) {
+        const int kk = kk0 + 2 * u;
+        if (kk < M) {
+          const V4<T> x4 = xT[kk];
+          s[0] += gv[u] * x4.x;
+          s[1] += gv[u] * x4.y;
+          s[2] += gv[u] * x4.z;
+          s[3] += gv[u] * x4.w;
+        }
+      }
     }
 #pragma unroll
     for (int m = 0; m < 4; ++m) s[m] += __shfl_xor_sync(kFull, s[m], 16);

@@ -34,6 +34,21 @@ Two sources, both read only here (the fixtures travel; the reference does not):
    settings stored as lower / upper / nspline, per-column sums and a sample
    of rows.
 
+6. ``ref_descriptor_pt.npz``: the reference's own PyTorch descriptor
+   (``DescrptSeA`` of ``deepmd/pt/model/descriptor/se_a.py``, compressed,
+   FP64) run on CPU from a copy of the reference package with its own
+   ``torch.ops.deepmd.tabulate_fusion_se_a`` compiled from
+   ``source/op/pt/tabulate_multi_device.cc``: seeded weights and statistics,
+   a seeded 192-atom water frame extended and listed by the reference's own
+   ``extend_input_and_build_neighbor_list``; the descriptor, the gradient of
+   a seeded linear function of it wrt the extended coordinates, and the
+   ``tabulate_fusion_se_a`` calls the module made (inputs, outputs and
+   input gradients for a seeded output gradient, first 24 atoms).  The
+   package copy, the import stand-ins for packages this image lacks (yaml,
+   dargs, h5py, wcmatch, mendeleev, lmdb, e3nn: never used on this path;
+   array_api_compat: numpy / torch namespaces) and the compiled op live in
+   a temporary directory only.
+
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
         (or DPMD_REFERENCE=/path/to/reference python tests/golden/make_golden.py)
 """
@@ -372,6 +387,182 @@ def reference_tabulate_fixture(path_out: str) -> None:
     np.savez_compressed(path_out, **data)
 
 
+def _reference_pt_package(tmp: str):
+    """A copy of the reference Python package in ``tmp`` with the metadata
+    files its build would write, its PyTorch op library compiled from the
+    reference sources, and import stand-ins for the packages this image
+    lacks.  Returns the imported descriptor module and the nlist module."""
+    import shutil
+    import subprocess
+    import types
+
+    import torch
+    import torch.utils.cpp_extension as ce
+
+    shutil.copytree(os.path.join(REF, "deepmd"), os.path.join(tmp, "deepmd"))
+    with open(os.path.join(tmp, "deepmd", "__about__.py"), "w") as fh:
+        fh.write('__version__ = "0.0.0"\n')
+    os.makedirs(os.path.join(tmp, "deepmd", "lib"), exist_ok=True)
+    open(os.path.join(tmp, "deepmd", "lib", "__init__.py"), "w").close()
+    tmpl = open(os.path.join(REF, "source", "config", "run_config.ini")).read()
+    with open(os.path.join(tmp, "deepmd", "lib", "run_config.ini"), "w") as fh:
+        fh.write(re.sub(r"@[^@]*@", "", tmpl))
+    srcs = [os.path.join(REF, "source", "op", "pt", f)
+            for f in ("tabulate_multi_device.cc", "print_summary.cc")]
+    srcs += [os.path.join(REF, "source", "lib", "src", f) for f in ("tabulate.cc", "errors.cc")
+             if os.path.exists(os.path.join(REF, "source", "lib", "src", f))]
+    lib = ce.library_paths()[0]
+    cmd = (["g++", "-O2", "-shared", "-fPIC", "-std=c++17",
+            f"-D_GLIBCXX_USE_CXX11_ABI={int(torch._C._GLIBCXX_USE_CXX11_ABI)}",
+            "-I" + os.path.join(REF, "source", "lib", "include")]
+           + [f"-I{p}" for p in ce.include_paths()] + srcs
+           + [f"-L{lib}", f"-Wl,-rpath,{lib}", "-ltorch", "-ltorch_cpu", "-lc10", "-o",
+              os.path.join(tmp, "deepmd", "lib", "libdeepmd_op_pt.so")])
+    subprocess.run(cmd, check=True)
+
+    class _Absent(types.ModuleType):
+        def __getattr__(self, name):
+            if name.startswith("__"):
+                raise AttributeError(name)
+            return type(name, (), {"__init__": lambda s_, *a, **k: None,
+                                   "__call__": lambda s_, *a, **k: None})
+
+    for m in ("yaml", "dargs", "h5py", "wcmatch", "wcmatch.glob", "mendeleev", "lmdb", "e3nn",
+              "e3nn.o3"):
+        sys.modules.setdefault(m, _Absent(m))
+
+    class _TorchNS:
+        def __getattr__(self, n):
+            return getattr(torch, n)
+
+        def astype(self, x, dtype, copy=True):
+            return x.to(dtype)
+
+        def asarray(self, x, dtype=None, device=None, copy=None):
+            return torch.as_tensor(x, dtype=dtype, device=device)
+
+        def concat(self, xs, axis=0):
+            return torch.cat(xs, dim=axis)
+
+        def permute_dims(self, x, axes):
+            return x.permute(*axes)
+
+        def expand_dims(self, x, axis):
+            return x.unsqueeze(axis)
+
+        def sum(self, x, axis=None, keepdims=False):
+            return x.sum() if axis is None else x.sum(dim=axis, keepdim=keepdims)
+
+        def reshape(self, x, shape):
+            return x.reshape(shape)
+
+    tns = _TorchNS()
+    aac = types.ModuleType("array_api_compat")
+    aac.array_namespace = lambda *xs: tns if any(isinstance(x, torch.Tensor) for x in xs) else np
+    aac.device = lambda x: getattr(x, "device", "cpu")
+    aac.is_torch_array = lambda x: isinstance(x, torch.Tensor)
+    aac.is_numpy_array = lambda x: isinstance(x, np.ndarray)
+    aac.is_array_api_obj = lambda x: isinstance(x, (np.ndarray, torch.Tensor))
+    aac.to_device = lambda x, d: x
+    aac.size = lambda x: x.size if isinstance(x, np.ndarray) else x.numel()
+    sys.modules["array_api_compat"] = aac
+    sys.path.insert(0, tmp)
+    import deepmd.pt.model.descriptor.se_a as S  # noqa: E402
+    import deepmd.pt.utils.nlist as NL  # noqa: E402
+
+    return S, NL
+
+
+def reference_descriptor_fixture(path_out: str) -> None:
+    import tempfile
+
+    import torch
+
+    sys.path.insert(0, ROOT)
+    from __graft_entry__ import load_package  # noqa: E402
+
+    load_package()
+    import dpmd_public_gb300.model as mdl  # noqa: E402
+    import dpmd_public_gb300.water as W  # noqa: E402
+
+    torch.set_default_dtype(torch.float64)
+    with tempfile.TemporaryDirectory() as tmp:
+        S, NL = _reference_pt_package(tmp)
+        cfg = mdl.SeAConfig()
+        seed = 2026
+        params = mdl.init_params(cfg, seed)
+        rng = np.random.default_rng(seed + 1)
+        nn = cfg.nnei
+        davg = np.zeros((cfg.ntypes, nn, 4))
+        davg[:, :, 0] = rng.uniform(0.03, 0.08, (cfg.ntypes, 1))
+        dstd = np.ones((cfg.ntypes, nn, 4))
+        dstd[:, :, 0] = rng.uniform(0.11, 0.15, (cfg.ntypes, 1))
+        dstd[:, :, 1:] = rng.uniform(0.07, 0.09, (cfg.ntypes, 1, 1))
+        rmin = 0.78
+        d = S.DescrptSeA(rcut=cfg.rcut, rcut_smth=cfg.rcut_smth, sel=list(cfg.sel),
+                         neuron=list(cfg.neuron), axis_neuron=cfg.axis_neuron,
+                         type_one_side=True, precision="float64", resnet_dt=False)
+        ser = d.serialize()
+        for k, net in enumerate(ser["embeddings"]["networks"]):
+            for l, layer in enumerate(net["layers"]):
+                layer["@variables"]["w"] = np.asarray(params["emb"][k][l]["w"], np.float64)
+                layer["@variables"]["b"] = np.asarray(params["emb"][k][l]["b"], np.float64)
+        ser["@variables"]["davg"] = davg
+        ser["@variables"]["dstd"] = dstd
+        d = S.DescrptSeA.deserialize(ser)
+        d.enable_compression(rmin, 5, 0.01, 0.1)
+        calls = []
+        real = torch.ops.deepmd.tabulate_fusion_se_a
+
+        def record(table, info, em_x, em, last):
+            out = real(table, info, em_x, em, last)
+            calls.append((info.detach().clone(), em_x.detach().clone(), em.detach().clone(),
+                          out[0].detach().clone(), int(last)))
+            return out
+
+        torch.ops.deepmd.tabulate_fusion_se_a = record
+        c, t, b = W.water_frame(4, 12.42, 2027)
+        coord = torch.tensor(c[None])
+        atype = torch.tensor(t[None], dtype=torch.int64)
+        box = torch.tensor(b[None])
+        ext, etype, mapping, nlist = NL.extend_input_and_build_neighbor_list(
+            coord, atype, cfg.rcut, list(cfg.sel), mixed_types=False, box=box)
+        ext = ext.detach().clone().requires_grad_(True)
+        desc = d(ext.reshape(1, -1), etype, nlist, mapping)[0]
+        wts = torch.tensor(np.random.default_rng(seed + 2).normal(0, 1, desc.shape))
+        (grad,) = torch.autograd.grad((desc * wts).sum(), ext)
+        torch.ops.deepmd.tabulate_fusion_se_a = real
+        keep = 24
+        data = {"seed": seed, "davg": davg.reshape(cfg.ntypes, -1), "dstd": dstd.reshape(cfg.ntypes, -1),
+                "rmin": rmin, "coord": c, "atype": t, "box": b,
+                "ext_coord": ext.detach().numpy()[0], "ext_atype": etype.numpy()[0].astype(np.int32),
+                "mapping": mapping.numpy()[0].astype(np.int32),
+                "nlist": nlist.numpy()[0].astype(np.int32),
+                "desc_head": desc.detach().numpy()[0, :keep],
+                "desc_norm": np.linalg.norm(desc.detach().numpy()[0], axis=1),
+                "grad_ext": grad.numpy()[0],
+                "ncalls": len(calls)}
+        for q, (info, em_x, em, out, last) in enumerate(calls):
+            nsel = em.shape[1]
+            data[f"call{q}_info"] = info.numpy()
+            data[f"call{q}_last"] = last
+            data[f"call{q}_em"] = em.numpy()[:keep]
+            data[f"call{q}_em_x"] = em_x.numpy()[: keep * nsel]
+            data[f"call{q}_out"] = out.numpy()[:keep]
+            dy = torch.tensor(np.random.default_rng(seed + 10 + q).normal(0, 1, (keep, 4, last)))
+            ex = em_x[: keep * nsel].clone().requires_grad_(True)
+            ee = em[:keep].clone().requires_grad_(True)
+            tab = d.sea.compress_data[q].detach()
+            data[f"call{q}_table_rows"] = tab.shape[0]
+            data[f"call{q}_table_abs_sum"] = float(tab.abs().sum())
+            o = real(tab, info, ex, ee, last)[0]
+            gx, gm = torch.autograd.grad(o, (ex, ee), dy)
+            data[f"call{q}_dy"] = dy.numpy()
+            data[f"call{q}_gx"] = gx.numpy()
+            data[f"call{q}_gm"] = gm.numpy()
+    np.savez_compressed(path_out, **data)
+
+
 def main() -> None:
     lib = {}
     for f in LIB_TESTS:
@@ -386,6 +577,7 @@ def main() -> None:
     reference_format_nlist_fixture(os.path.join(HERE, "pt_format_nlist.npz"))
     reference_model_fixture(os.path.join(HERE, "ref_deeppot_sea.npz"))
     reference_tabulate_fixture(os.path.join(HERE, "ref_tabulate.npz"))
+    reference_descriptor_fixture(os.path.join(HERE, "ref_descriptor_pt.npz"))
     print("fixtures:", sorted(os.listdir(HERE)))
 
 

@@ -1219,6 +1219,10 @@ def op_kernel_times(model, batch, coord, flush, peaks, reps: int = 5):
                                 n * nn * (16 + 48 + 4) + nall * 12),
         "prod_virial_se_a": (lambda: ops.prod_virial_se_a_impl(net, ed, rij, nl, natoms, nn, 0),
                              n * nn * (16 + 48 + 12 + 4) + nall * 36 + 36),
+        # both outputs from one pass over the shared inputs
+        "prod_force_virial_se_a": (
+            lambda: ops.prod_force_virial_se_a_impl(net, ed, rij, nl, natoms, nn, 0),
+            n * nn * (16 + 48 + 12 + 4) + nall * (12 + 36) + 36),
         "tabulate_fusion_se_a": (lambda: [ops.tabulate_forward(t_, i_, x_, e_, M)
                                           for t_, i_, x_, e_, _ in tab],
                                  sum(x_.numel() * f * 5 + n * 4 * M * f for _, _, x_, _, _ in tab)),

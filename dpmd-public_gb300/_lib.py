@@ -117,6 +117,7 @@ for _s in ("f32", "f64"):
                                                           _P, _Z, _P]),
         f"gbdp_prod_force_a_{_s}": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _Z, _P]),
         f"gbdp_prod_virial_a_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _Z, _P]),
+        f"gbdp_prod_force_virial_a_{_s}": (_I, [_P] * 7 + [_I, _I, _I, _I, _I, _P, _Z, _P]),
         f"gbdp_prod_force_grad_a_{_s}": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
         f"gbdp_prod_virial_grad_a_{_s}": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _P]),
         f"gbdp_se_a_descriptor_fwd_{_s}": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I, _P]),

@@ -767,6 +767,15 @@ int prod_virial_impl(T* virial, T* atom_virial, const T* net, const T* dR, const
                                nall, nnei, nframes, deterministic, workspace, workspace_bytes, \
                                (cudaStream_t)stream);                                          \
   }                                                                                             \
+  extern "C" int gbdp_prod_force_virial_a_##SFX(                                                \
+      T* force, T* virial, T* atom_virial, const T* net_deriv, const T* env_deriv, const T* rij, \
+      const int* nlist, int nloc, int nall, int nnei, int nframes, int deterministic,          \
+      void* workspace, size_t workspace_bytes, gbdp_stream stream) {                           \
+    GBDP_REQUIRE(force && virial && atom_virial, "prod_force_virial_a: null output");           \
+    return prod_launch<T>(force, virial, atom_virial, net_deriv, env_deriv, rij, nlist, nloc,  \
+                          nall, nnei, nframes, deterministic, workspace, workspace_bytes,      \
+                          (cudaStream_t)stream);                                               \
+  }                                                                                             \
   extern "C" int gbdp_prod_force_grad_a_##SFX(T* grad_net, const T* grad, const T* env_deriv,   \
                                               const int* nlist, int nloc, int nnei,            \
                                               int nframes, gbdp_stream stream) {               \

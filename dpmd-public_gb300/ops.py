@@ -456,6 +456,34 @@ def prod_virial_se_a_impl(net_deriv, in_deriv, rij, nlist, natoms, n_a_sel: int,
     return virial, atom_virial
 
 
+def prod_force_virial_se_a_impl(net_deriv, in_deriv, rij, nlist, natoms, n_a_sel: int,
+                                n_r_sel: int, deterministic: bool = False):
+    """prod_force_se_a and prod_virial_se_a in one pass over their shared
+    inputs: (force [nf, nall*3], virial [nf, 9], atom_virial [nf, nall*9])."""
+    _need_cuda(net_deriv, in_deriv, rij, nlist)
+    nat = [int(v) for v in natoms.reshape(-1).tolist()]
+    nloc, nall = nat[0], nat[1]
+    nf = net_deriv.shape[0]
+    nnei = int(n_a_sel) + int(n_r_sel)
+    dt = net_deriv.dtype
+    dev = net_deriv.device
+    force = torch.empty((nf, nall * 3), dtype=dt, device=dev)
+    virial = torch.empty((nf, 9), dtype=dt, device=dev)
+    atom_virial = torch.empty((nf, nall * 9), dtype=dt, device=dev)
+    lib = L.load()
+    wsb = int(lib.gbdp_prod_workspace_bytes(nf, nloc, nall, nnei, int(deterministic)))
+    ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+    fn = getattr(lib, f"gbdp_prod_force_virial_a_{L.sfx(dt)}")
+    net_deriv = net_deriv.contiguous()
+    in_deriv = in_deriv.to(dt).contiguous()
+    rij = rij.to(dt).contiguous()
+    nlist = nlist.to(torch.int32).contiguous()
+    L.check(fn(_ptr(force), _ptr(virial), _ptr(atom_virial), _ptr(net_deriv), _ptr(in_deriv),
+               _ptr(rij), _ptr(nlist), nloc, nall, nnei, nf, int(deterministic), _ptr(ws),
+               ctypes.c_size_t(wsb), _stream()), "prod_force_virial_se_a")
+    return force, virial, atom_virial
+
+
 def prod_force_grad_impl(grad, in_deriv, nlist, nloc, nnei, nf):
     dt = grad.dtype
     out = torch.empty((nf, nloc * nnei * 4), dtype=dt, device=grad.device)

@@ -32,7 +32,7 @@ import torch
 from . import _lib as L
 from . import model as mdl
 from .ops import (EnvMatResult, NeighborPlan, VerletList, env_mat_packed, env_mat_skin,
-                  prod_force_se_a_impl, prod_virial_se_a_impl)
+                  prod_force_se_a_impl, prod_force_virial_se_a_impl, prod_virial_se_a_impl)
 
 _P = ctypes.c_void_p
 
@@ -443,9 +443,9 @@ class SeAModel:
             nd = net[a0:a0 + nl].reshape(1, -1)
             ed = env.em_deriv[a0:a0 + nl].reshape(1, -1)
             nlst = env.nlist[a0:a0 + nl].reshape(1, -1)
-            forces.append(prod_force_se_a_impl(nd, ed, nlst, natoms, nnei, 0).reshape(nl, 3))
-            v, _ = prod_virial_se_a_impl(nd, ed, env.rij[a0:a0 + nl].reshape(1, -1), nlst, natoms,
-                                         nnei, 0)
+            f_, v, _ = prod_force_virial_se_a_impl(nd, ed, env.rij[a0:a0 + nl].reshape(1, -1),
+                                                   nlst, natoms, nnei, 0)
+            forces.append(f_.reshape(nl, 3))
             virs.append(v.reshape(9))
         L.check(getattr(self._lib, f"gbdp_frame_energy_{self._sfx}")(
             _ptr(b.energy), _ptr(b.ae), _ptr(b.frame_of_row), b.ae.numel(), b.nframes, 0,
@@ -510,9 +510,9 @@ class SeAModel:
             nd = net[a0:a1].reshape(1, -1)
             ed = env.em_deriv[a0:a1].reshape(1, -1)
             nlst = env.nlist[a0:a1].reshape(1, -1)
-            forces.append(prod_force_se_a_impl(nd, ed, nlst, natoms, nnei, 0, deterministic).reshape(nl, 3))
-            v, _ = prod_virial_se_a_impl(nd, ed, env.rij[a0:a1].reshape(1, -1), nlst, natoms, nnei, 0,
-                                         deterministic)
+            f_, v, _ = prod_force_virial_se_a_impl(nd, ed, env.rij[a0:a1].reshape(1, -1), nlst,
+                                                   natoms, nnei, 0, deterministic)
+            forces.append(f_.reshape(nl, 3))
             virs.append(v.reshape(9))
         E = torch.zeros(b.nframes, dtype=torch.float64, device=self.device)
         E.index_add_(0, b.frame_of_atom, E_atom.detach().to(torch.float64))

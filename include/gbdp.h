@@ -332,6 +332,25 @@ GBDP_API int gbdp_prod_virial_a_f64(double* virial, double* atom_virial, const d
                            int nloc, int nall, int nnei, int nframes, int deterministic,
                            void* workspace, size_t workspace_bytes, gbdp_stream stream);
 
+/* Force and virial in one pass over net_deriv / env_deriv / nlist (no
+ * counterpart in the reference, which runs ProdForceSeA and ProdVirialSeA
+ * as two ops reading the same inputs): the outputs of gbdp_prod_force_a_*
+ * and gbdp_prod_virial_a_* with the same arguments, the 80 B a slot of
+ * net_deriv, env_deriv, nlist (and 12 B of rij) read once instead of twice.
+ * Same workspace (gbdp_prod_workspace_bytes), modes and alignment rules. */
+GBDP_API int gbdp_prod_force_virial_a_f32(float* force, float* virial, float* atom_virial,
+                                          const float* net_deriv, const float* env_deriv,
+                                          const float* rij, const int* nlist, int nloc, int nall,
+                                          int nnei, int nframes, int deterministic,
+                                          void* workspace, size_t workspace_bytes,
+                                          gbdp_stream stream);
+GBDP_API int gbdp_prod_force_virial_a_f64(double* force, double* virial, double* atom_virial,
+                                          const double* net_deriv, const double* env_deriv,
+                                          const double* rij, const int* nlist, int nloc, int nall,
+                                          int nnei, int nframes, int deterministic,
+                                          void* workspace, size_t workspace_bytes,
+                                          gbdp_stream stream);
+
 /* Backward of the two ops wrt net_deriv (second order of the env-mat
  * derivative).  Replace deepmd::prod_force_grad_a_gpu
  * (source/lib/include/prod_force_grad.h, source/lib/src/gpu/

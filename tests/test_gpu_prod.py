@@ -141,3 +141,42 @@ def test_many_frames_virial(gb, oracle, det):
         np.testing.assert_allclose(v[k].cpu().numpy(), np.reshape(vo, -1), atol=1e-9, rtol=1e-10)
         np.testing.assert_allclose(av[k].cpu().numpy(), np.reshape(avo, -1), atol=1e-10, rtol=1e-10)
         np.testing.assert_allclose(f[k].cpu().numpy(), np.reshape(fo, -1), atol=1e-10, rtol=1e-10)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("det", [0, 1])
+def test_force_virial_in_one_pass(gb, oracle, dtype, det):
+    """gbdp_prod_force_virial_a_* equals the two separate ops: bit for bit in
+    the deterministic mode, within floating-point atomics order otherwise."""
+    import importlib
+
+    ops = importlib.import_module("dpmd_public_gb300.ops")
+    water = importlib.import_module("dpmd_public_gb300.water")
+    frames = [water.water_frame(4, 12.42, 81), water.water_frame(4, 12.42, 82)]
+    nnei = 138
+    npd = np.float64 if dtype == torch.float64 else np.float32
+    avg = np.zeros((2, nnei * 4))
+    std = np.ones((2, nnei * 4))
+    ems, emds, rijs, nls = [], [], [], []
+    for c, t, b in frames:
+        em, emd, rij, nl = oracle.prod_env_mat_a_pbc(c.astype(npd), t, b.astype(npd),
+                                                     avg.astype(npd), std.astype(npd), 6.0, 0.5,
+                                                     [46, 92])
+        ems.append(em), emds.append(emd), rijs.append(rij), nls.append(nl)
+    n = len(frames[0][1])
+    rng = np.random.default_rng(83)
+    net = torch.tensor(rng.normal(0, 1, (2, n * nnei * 4)), dtype=dtype, device="cuda")
+    ed = torch.tensor(np.stack(emds), dtype=dtype, device="cuda")
+    rij = torch.tensor(np.stack(rijs), dtype=dtype, device="cuda")
+    nl = torch.tensor(np.stack(nls), dtype=torch.int32, device="cuda")
+    natoms = torch.tensor([n, n, 0, 0], dtype=torch.int32)
+    f1 = ops.prod_force_se_a_impl(net, ed, nl, natoms, nnei, 0, bool(det))
+    v1, av1 = ops.prod_virial_se_a_impl(net, ed, rij, nl, natoms, nnei, 0, bool(det))
+    f2, v2, av2 = ops.prod_force_virial_se_a_impl(net, ed, rij, nl, natoms, nnei, 0, bool(det))
+    torch.cuda.synchronize()
+    if det:
+        assert torch.equal(f1, f2) and torch.equal(v1, v2) and torch.equal(av1, av2)
+    else:
+        tol = 1e-12 if dtype == torch.float64 else 2e-5
+        for a, b in ((f1, f2), (v1, v2), (av1, av2)):
+            assert float((a - b).abs().max()) <= tol * max(1.0, float(a.abs().max()))

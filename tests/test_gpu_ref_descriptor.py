@@ -9,7 +9,7 @@ extended and listed, with seeded weights and statistics (made by
 tests/golden/make_golden.py).  On the GPU:
 
 * the tables this library builds for those weights have the reference's
-  range, row count and magnitude;
+  range and row count, and its coefficient magnitude to 1e-6;
 * every tabulate_fusion_se_a call the reference module made, replayed
   through torch.ops.deepmd.tabulate_fusion_se_a on CUDA: outputs and the
   input gradients for the recorded output gradient within 1e-10;
@@ -48,8 +48,11 @@ def test_tables_match_the_reference_modules(ref):
     for q in range(int(g["ncalls"])):
         np.testing.assert_array_equal(infos[q], g[f"call{q}_info"])
         assert tabs[q].shape[0] == int(g[f"call{q}_table_rows"])
+        # the sum is dominated by the a3..a5 columns, which carry the nodes'
+        # rounding amplified by 1 / stride^n in any evaluation order (the
+        # interpolants themselves agree to 1e-13: test_host_model.py)
         np.testing.assert_allclose(np.abs(tabs[q]).sum(), float(g[f"call{q}_table_abs_sum"]),
-                                   rtol=1e-9)
+                                   rtol=1e-6)
 
 
 def test_replayed_tabulate_calls(ref):

@@ -42,7 +42,7 @@ class NbrFrame(ctypes.Structure):
         ("ext_cell_off", ctypes.c_int),
         ("ext_off", ctypes.c_int),
         ("ext_cap", ctypes.c_int),
-        ("pad0", ctypes.c_int),
+        ("subcell", ctypes.c_int),
     ]
 
 

@@ -131,7 +131,8 @@ __global__ void k_localize(const gbdp_nbr_frame* __restrict__ fr, int nframes, i
                            const T* __restrict__ coord, const int* __restrict__ atype,
                            T* __restrict__ ext_coord, int* __restrict__ ext_type,
                            int* __restrict__ ext_map, int* __restrict__ atom_frame,
-                           int* __restrict__ atom_cell, int* __restrict__ cell_count) {
+                           int* __restrict__ atom_cell, int* __restrict__ cell_count,
+                           int* __restrict__ sub_count, int* __restrict__ atom_sub) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nloc_total) return;
   const int f = find_frame_atom(fr, nframes, i);
@@ -162,7 +163,7 @@ __global__ void k_localize(const gbdp_nbr_frame* __restrict__ fr, int nframes, i
   ext_map[e] = il;
   // cell from the wrapped coordinate, in double (SimulationRegion<double>)
   double pd[3] = {(double)q[0], (double)q[1], (double)q[2]};
-  int ci[3];
+  int ci[3], sub = 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     double in = __dadd_rn(__dadd_rn(__dmul_rn(pd[0], g.rec[d * 3 + 0]),
@@ -173,11 +174,18 @@ __global__ void k_localize(const gbdp_nbr_frame* __restrict__ fr, int nframes, i
     if (in < 0.) --k;
     k = max(0, min(k, g.ncell[d] - 1));
     ci[d] = k;
+    // the half of the cell along d (searched as its own cell when split)
+    if ((g.subcell >> d) & 1) {
+      const double u = in / cs - (double)k;
+      if (u >= 0.5) sub |= 1 << d;
+    }
   }
   const int c = g.cell_off + (ci[0] * g.ncell[1] + ci[1]) * g.ncell[2] + ci[2];
   atom_frame[i] = f;
   atom_cell[i] = c;
+  atom_sub[i] = sub;
   atomicAdd(&cell_count[c], 1);
+  atomicAdd(&sub_count[(size_t)c * 8 + sub], 1);
 }
 
 // Block-wide exclusive scan (blockDim.x multiple of 32, <= 1024).
@@ -232,7 +240,8 @@ __global__ void k_cell_scan(const gbdp_nbr_frame* __restrict__ fr,
                             const int* __restrict__ cell_count, int* __restrict__ cell_start,
                             int* __restrict__ ext_start, int* __restrict__ ext_cnt,
                             int* __restrict__ ghost_start, int* __restrict__ ext_nall,
-                            int* __restrict__ status) {
+                            int* __restrict__ status, const int* __restrict__ sub_count,
+                            int* __restrict__ ext_sub) {
   __shared__ int warp_tot[32];
   const gbdp_nbr_frame& g = fr[blockIdx.x];
   const int ncl = g.ncell[0] * g.ncell[1] * g.ncell[2];
@@ -250,9 +259,9 @@ __global__ void k_cell_scan(const gbdp_nbr_frame* __restrict__ fr,
   int carry_all = 0, carry_ghost = 0;
   for (int base = 0; base < ne; base += blockDim.x) {
     int e = base + threadIdx.x;
-    int cnt = 0, gcnt = 0;
+    int cnt = 0, gcnt = 0, src = 0;
     if (e < ne) {
-      int ii[3], sh[3], src;
+      int ii[3], sh[3];
       bool local;
       ext_cell_source(g, e, ii, sh, src, local);
       cnt = cell_count[src];
@@ -262,9 +271,20 @@ __global__ void k_cell_scan(const gbdp_nbr_frame* __restrict__ fr,
     int ex_all = block_excl_scan(cnt, warp_tot, tot_all);
     int ex_ghost = block_excl_scan(gcnt, warp_tot, tot_ghost);
     if (e < ne) {
-      ext_start[g.ext_cell_off + e] = g.ext_off + carry_all + ex_all;
+      const int st = g.ext_off + carry_all + ex_all;
+      ext_start[g.ext_cell_off + e] = st;
       ext_cnt[g.ext_cell_off + e] = cnt;
       ghost_start[g.ext_cell_off + e] = g.nloc + carry_ghost + ex_ghost;
+      // xs start of each half cell (the source cell's atoms in half-cell
+      // order), then the cell's end
+      int* es = ext_sub + 9 * (size_t)(g.ext_cell_off + e);
+      int acc = st;
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        es[h] = acc;
+        acc += sub_count[8 * (size_t)src + h];
+      }
+      es[8] = acc;
     }
     carry_all += tot_all;
     carry_ghost += tot_ghost;
@@ -290,20 +310,31 @@ __global__ void k_cell_bucket(int nloc_total, const gbdp_nbr_frame* __restrict__
 }
 
 // Ascending local index inside each cell: the order build_clist pushes them.
+// The atom's position in its cell's candidate copy (xs): ordered by half
+// cell, then by local index.
 __global__ void k_cell_rank(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
                             const int* __restrict__ atom_frame,
                             const int* __restrict__ atom_cell,
                             const int* __restrict__ cell_start,
                             const int* __restrict__ cell_count, const int* __restrict__ bucket,
-                            int* __restrict__ cell_atoms) {
+                            int* __restrict__ cell_atoms, const int* __restrict__ atom_sub,
+                            int* __restrict__ atom_xpos) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nloc_total) return;
   const int c = atom_cell[i];
-  const int il = i - fr[atom_frame[i]].atom_off;
+  const int aoff = fr[atom_frame[i]].atom_off;
+  const int il = i - aoff;
+  const int hs = atom_sub[i];
   const int s = cell_start[c], n = cell_count[c];
-  int rank = 0;
-  for (int k = 0; k < n; ++k) rank += bucket[s + k] < il;
+  int rank = 0, xpos = 0;
+  for (int k = 0; k < n; ++k) {
+    const int o = bucket[s + k];
+    const int ho = atom_sub[aoff + o];
+    rank += o < il;
+    xpos += ho < hs || (ho == hs && o < il);
+  }
   cell_atoms[s + rank] = il;
+  atom_xpos[i] = xpos;
 }
 
 // --------------------------------------------------------- k_ghost_fill --
@@ -318,7 +349,8 @@ __global__ void k_ghost_fill(const gbdp_nbr_frame* __restrict__ fr, int nframes,
                              const int* __restrict__ ext_start,
                              const int* __restrict__ ghost_start, T* __restrict__ ext_coord,
                              int* __restrict__ ext_type, int* __restrict__ ext_map,
-                             typename XsOf<T>::type* __restrict__ xs) {
+                             typename XsOf<T>::type* __restrict__ xs,
+                             const int* __restrict__ atom_xpos) {
   const int ew = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (ew >= next_cell_total) return;
@@ -358,7 +390,10 @@ __global__ void k_ghost_fill(const gbdp_nbr_frame* __restrict__ fr, int nframes,
       ext_type[eg] = t;
       ext_map[eg] = p;
     }
-    xs[xs0 + k] = make_xs(x, y, z, pack_idx_type(idx, t));
+    // the candidate copy is ordered by half cell (extended indices keep
+    // copy_coord's order)
+    const int xp = atom_xpos[(size_t)g.atom_off + p];
+    if (xs0 + xp < xs_end) xs[xs0 + xp] = make_xs(x, y, z, pack_idx_type(idx, t));
   }
 }
 
@@ -564,7 +599,7 @@ template <typename T, int MODE>
 __global__ void __launch_bounds__(kEnvWarps * 32)
     k_nlist_env(int nloc_total, const gbdp_nbr_frame* __restrict__ fr,
                 const int* __restrict__ atom_frame, const int* __restrict__ atom_cell,
-                const int* __restrict__ ext_start, const int* __restrict__ ext_cnt,
+                const int* __restrict__ atom_sub, const int* __restrict__ ext_sub,
                 const typename XsOf<T>::type* __restrict__ xs, const T* __restrict__ ext_coord,
                 const int* __restrict__ ext_map, const int* __restrict__ atype,
                 const T* __restrict__ avg, const T* __restrict__ stdv, SecInfo si, float rc2f,
@@ -630,20 +665,39 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
       ncand += __popc(m);
     }
   }
-  const int sy = 2 * g.stencil[1] + 1, sz = 2 * g.stencil[2] + 1;
-  const int nst = MODE == kEnvList ? 0 : (2 * g.stencil[0] + 1) * sy * sz;
+  // the search grid: along a split dimension d the extended cells are
+  // halved (fine index F = 2 cell + half) and the stencil reaches two half
+  // cells either way; otherwise it is the extended cells themselves
+  int fs[3], hw[3], F[3];
+  {
+    const int cc[3] = {c0, c1, c2};
+    const int hs = MODE == kEnvList ? 0 : atom_sub[i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const bool split = (g.subcell >> d) & 1;
+      fs[d] = split ? 2 : 1;
+      hw[d] = split ? 2 : g.stencil[d];
+      F[d] = fs[d] * (cc[d] + g.ngcell[d]) + (split ? (hs >> d) & 1 : 0);
+    }
+  }
+  const int sy = 2 * hw[1] + 1, sz = 2 * hw[2] + 1;
+  const int nst = MODE == kEnvList ? 0 : (2 * hw[0] + 1) * sy * sz;
   int* vrow = MODE == kEnvBuild ? vl.idx + (size_t)i * vl.cap : nullptr;
   for (int cg = 0; cg < nst; cg += 32) {
     const int q = cg + lane;
     int st = 0, cnt = 0;
     if (q < nst) {
-      const int d0 = q / (sy * sz) - g.stencil[0];
-      const int d1 = (q / sz) % sy - g.stencil[1];
-      const int d2 = q % sz - g.stencil[2];
-      const int e = g.ext_cell_off + ((c0 + g.ngcell[0] + d0) * n1 + (c1 + g.ngcell[1] + d1)) * n2 +
-                    (c2 + g.ngcell[2] + d2);
-      st = ext_start[e];
-      cnt = ext_cnt[e];
+      const int o[3] = {q / (sy * sz) - hw[0], (q / sz) % sy - hw[1], q % sz - hw[2]};
+      int E[3], h = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int fp = F[d] + o[d];  // >= 0: the ghost layers cover the stencil
+        E[d] = fs[d] == 2 ? fp >> 1 : fp;
+        if (fs[d] == 2) h |= (fp & 1) << d;
+      }
+      const int* es = ext_sub + 9 * (size_t)(g.ext_cell_off + (E[0] * n1 + E[1]) * n2 + E[2]);
+      st = es[h];
+      cnt = es[h + 1] - st;
     }
     int incl = cnt;
 #pragma unroll
@@ -886,8 +940,12 @@ struct EnvWs {
   int* ext_start;
   int* ext_cnt;
   int* ghost_start;
+  int* sub_count;  // [ncell_total][8] atoms per half cell of each local cell
+  int* atom_sub;   // [nloc_total] half cell of each local atom (bit d: upper half)
+  int* atom_xpos;  // [nloc_total] position of the atom in its cell's xs range
+  int* ext_sub;    // [next_cell_total][9] xs start of each half cell, then the end
   void* xs;
-  size_t zero_bytes;  // status .. cell_fill: zeroed before every build
+  size_t zero_bytes;  // status .. sub_count: zeroed before every build
   size_t bytes;
 };
 
@@ -900,11 +958,16 @@ EnvWs carve(const gbdp_nbr_plan& p, void* base, int fp64) {
     off += align256(n);
     return r;
   };
-  // status, cell_count and cell_fill first and adjacent: one zero fill
+  // status, cell_count, cell_fill and sub_count first and adjacent: one
+  // zero fill
   w.status = reinterpret_cast<int*>(take(256));
   w.cell_count = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
   w.cell_fill = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
+  w.sub_count = reinterpret_cast<int*>(take(sizeof(int) * 8 * (size_t)p.ncell_total));
   w.zero_bytes = off;
+  w.atom_sub = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.atom_xpos = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
+  w.ext_sub = reinterpret_cast<int*>(take(sizeof(int) * 9 * (size_t)p.next_cell_total));
   w.atom_frame = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
   w.atom_cell = reinterpret_cast<int*>(take(sizeof(int) * p.nloc_total));
   w.cell_start = reinterpret_cast<int*>(take(sizeof(int) * p.ncell_total));
@@ -964,20 +1027,21 @@ void env_ghosts(const EnvWs& w, T* ext_coord, int* ext_type, int* ext_map, int* 
   const int tb = 256;
   k_localize<T><<<(nl + tb - 1) / tb, tb, 0, stream>>>(frames, plan->nframes, nl, coord, atype,
                                                        ext_coord, ext_type, ext_map,
-                                                       w.atom_frame, w.atom_cell, w.cell_count);
+                                                       w.atom_frame, w.atom_cell, w.cell_count,
+                                                       w.sub_count, w.atom_sub);
   k_cell_scan<<<plan->nframes, 1024, 0, stream>>>(frames, w.cell_count, w.cell_start,
                                                   w.ext_start, w.ext_cnt, w.ghost_start,
-                                                  ext_nall, w.status);
+                                                  ext_nall, w.status, w.sub_count, w.ext_sub);
   k_cell_bucket<<<(nl + tb - 1) / tb, tb, 0, stream>>>(nl, frames, w.atom_frame, w.atom_cell,
                                                        w.cell_start, w.cell_fill, w.bucket);
   k_cell_rank<<<(nl + tb - 1) / tb, tb, 0, stream>>>(nl, frames, w.atom_frame, w.atom_cell,
                                                      w.cell_start, w.cell_count, w.bucket,
-                                                     w.cell_atoms);
+                                                     w.cell_atoms, w.atom_sub, w.atom_xpos);
   const int nec = plan->next_cell_total;
   k_ghost_fill<T><<<(nec * 32 + tb - 1) / tb, tb, 0, stream>>>(
       frames, plan->nframes, nec, w.cell_start, w.cell_count, w.cell_atoms, w.ext_start,
       w.ghost_start, ext_coord, ext_type, ext_map,
-      static_cast<typename XsOf<T>::type*>(w.xs));
+      static_cast<typename XsOf<T>::type*>(w.xs), w.atom_xpos);
 }
 
 // One launch of k_nlist_env in the given mode (candidates within rc).
@@ -995,8 +1059,8 @@ void nlist_env_mode(const EnvWs& w, const gbdp_nbr_plan* plan, const gbdp_nbr_fr
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const bool cells = MODE != kEnvList;
   kern<<<(nl + kEnvWarps - 1) / kEnvWarps, kEnvWarps * 32, smem, stream>>>(
-      nl, frames, w.atom_frame, cells ? w.atom_cell : nullptr, cells ? w.ext_start : nullptr,
-      cells ? w.ext_cnt : nullptr,
+      nl, frames, w.atom_frame, cells ? w.atom_cell : nullptr, cells ? w.atom_sub : nullptr,
+      cells ? w.ext_sub : nullptr,
       cells ? static_cast<const typename XsOf<T>::type*>(w.xs) : nullptr, ext_coord, ext_map,
       atype, avg, stdv, si, rc * rc, (T)rcut_smth, (T)rmax, mc, em, em_deriv, rij, nlist,
       nlist_ext, w.status, vl);
@@ -1231,6 +1295,10 @@ extern "C" int gbdp_nbr_plan_make(gbdp_nbr_plan* plan, gbdp_nbr_frame* frames, i
       double cs = face / nc;
       g.ncell[d] = nc;
       g.ngcell[d] = (int)((double)rcut / cs) + 1;
+      // cells at least 0.1 % wider than rcut are searched in halves: a pair
+      // within rcut is then at most two half cells apart along d (with a
+      // margin far above the coordinates' rounding)
+      if (g.ngcell[d] == 1 && (double)rcut <= 0.999 * cs) g.subcell |= 1 << d;
       // every extended atom within rcut of a local atom lies within ngcell
       // cells of it (cell >= rcut, or ngcell covers rcut / cell)
       g.stencil[d] = g.ngcell[d];

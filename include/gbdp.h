@@ -133,7 +133,7 @@ typedef struct gbdp_nbr_frame {
   int ext_cell_off;/* first extended cell                                */
   int ext_off;     /* first extended-atom slot                           */
   int ext_cap;     /* extended-atom slots reserved (upper bound of nall) */
-  int pad0;
+  int subcell;     /* bit d: the neighbour search scans half cells along d */
 } gbdp_nbr_frame;
 
 typedef struct gbdp_nbr_plan {

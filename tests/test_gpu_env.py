@@ -145,14 +145,18 @@ def test_tf_contract_op_multi_frame(gb, oracle):
         np.testing.assert_allclose(out[2][k].cpu().numpy(), rij, atol=1e-12)
 
 
-def test_candidate_overflow_is_reported(gb):
+def test_candidate_overflow_is_reported_and_retried(gb, oracle):
     """A max_cand smaller than the real neighbour count raises the device
-    status word (no fault, no hang) and the host wrapper reports it."""
+    status word (no fault, no hang); the host wrapper doubles the capacity
+    until every centre's candidates fit (16 -> 128 for water, about 90
+    within rc) and returns the reference's list."""
     water = __import__("dpmd_public_gb300.water", fromlist=["x"])
     c, t, b = water.water_frame(4, 12.42, 2)
     avg, std = _stats(torch.float64, 2)
-    with pytest.raises(RuntimeError, match="candidate overflow"):
-        _run(gb, [c], [t], [b], avg, std, torch.float64, max_cand=16)
+    plan, r = _run(gb, [c], [t], [b], avg, std, torch.float64, max_cand=16)
+    assert plan.max_cand == 128
+    em, emd, rij, nl = oracle.prod_env_mat_a_pbc(c, t, b, avg, std, 6.0, 0.5, SEL)
+    np.testing.assert_array_equal(r.nlist.cpu().numpy().reshape(-1), nl)
 
 
 def test_sel_overflow_keeps_nearest(gb, oracle):

@@ -125,6 +125,61 @@ __device__ __forceinline__ void load_coef6_kp(T* a, const T* __restrict__ row, i
   a[5] = w.y;
 }
 
+// Phase-1 sums of the FP32 backward for one neighbour per 16-lane group:
+// the lane's outputs k and k + 16 share the Horner sweeps (value and slope
+// of the quintic) as the two halves of packed FP32x2 FMAs (sm_100 and
+// later), each half rounding as a scalar fmaf does; the sums then take
+// output k and k + 16 in the scalar loop's order, so the results equal the
+// scalar loop's bit for bit.  The row load for k + 16 is unconditional
+// while q + 1 < NK: a plane holds kp_pitch(M) / 2 = 16 ceil(M / 16) >=
+// 16 NK coefficient pairs, so k + 16 < 16 NK stays inside it (pairs past M
+// are padding whose sums are not taken), and the loads issue without a
+// branch.  p[0..3] += v_k dy[k][0..3], p[4] += v'_k (em . dy[k]).
+template <int NK>
+__device__ __forceinline__ void bwd_tab_grad_pairs(float* p, const float* __restrict__ row, int ps,
+                                                   float x, const float4& e,
+                                                   const float (&dr)[NK][4], int t16, int M) {
+  const float2 X2 = make_float2(x, x);
+#pragma unroll
+  for (int q = 0; q < NK; q += 2) {
+    const int k = t16 + 16 * q;
+    if (k >= M) break;
+    float a1[6], a2[6];
+    load_coef6_kp<float>(a1, row, ps, k);
+    if (q + 1 < NK) {
+      load_coef6_kp<float>(a2, row, ps, k + 16);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) a2[c] = 0.f;
+    }
+    float2 A[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) A[c] = make_float2(a1[c], a2[c]);
+    float2 V = A[5], DV = A[5];
+    V = __ffma2_rn(V, X2, A[4]);
+    DV = __ffma2_rn(DV, X2, V);
+    V = __ffma2_rn(V, X2, A[3]);
+    DV = __ffma2_rn(DV, X2, V);
+    V = __ffma2_rn(V, X2, A[2]);
+    DV = __ffma2_rn(DV, X2, V);
+    V = __ffma2_rn(V, X2, A[1]);
+    DV = __ffma2_rn(DV, X2, V);
+    V = __ffma2_rn(V, X2, A[0]);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int qh = q + h;
+      if (h == 1 && (qh >= NK || k + 16 >= M)) break;
+      const float* d = dr[qh < NK ? qh : q];
+      const float v = h ? V.y : V.x, dv = h ? DV.y : DV.x;
+      p[0] += v * d[0];
+      p[1] += v * d[1];
+      p[2] += v * d[2];
+      p[3] += v * d[3];
+      p[4] += dv * (e.x * d[0] + e.y * d[1] + e.z * d[2] + e.w * d[3]);
+    }
+  }
+}
+
 // one row of 4 values (16-byte aligned), not allocated in L1
 __device__ __forceinline__ float4 ld_stream4(const float* p) {
   float4 v;
@@ -661,33 +716,37 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
 #pragma unroll
           for (int c = 0; c < 5; ++c) p[u][c] = T(0);
         }
+        if constexpr (sizeof(T) == 4 && U == 1) {
+          bwd_tab_grad_pairs<NK>(p[0], row[0], ts.ps, x[0], e[0], dr, t16, M);
+        } else {
 #pragma unroll
-        for (int q = 0; q < NK; ++q) {
-          const int k = t16 + 16 * q;
-          if (k >= M) break;
-          T a[U][6];
+          for (int q = 0; q < NK; ++q) {
+            const int k = t16 + 16 * q;
+            if (k >= M) break;
+            T a[U][6];
 #pragma unroll
-          for (int u = 0; u < U; ++u) load_coef6_kp<T>(a[u], row[u], ts.ps, k);
-          const T d[4] = {dr[q][0], dr[q][1], dr[q][2], dr[q][3]};
+            for (int u = 0; u < U; ++u) load_coef6_kp<T>(a[u], row[u], ts.ps, k);
+            const T d[4] = {dr[q][0], dr[q][1], dr[q][2], dr[q][3]};
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            // value and slope by one Horner sweep (9 FMA)
-            const T xu = x[u];
-            T v = a[u][5], dv = a[u][5];
-            v = v * xu + a[u][4];
-            dv = dv * xu + v;
-            v = v * xu + a[u][3];
-            dv = dv * xu + v;
-            v = v * xu + a[u][2];
-            dv = dv * xu + v;
-            v = v * xu + a[u][1];
-            dv = dv * xu + v;
-            v = v * xu + a[u][0];
-            p[u][0] += v * d[0];
-            p[u][1] += v * d[1];
-            p[u][2] += v * d[2];
-            p[u][3] += v * d[3];
-            p[u][4] += dv * (e[u].x * d[0] + e[u].y * d[1] + e[u].z * d[2] + e[u].w * d[3]);
+            for (int u = 0; u < U; ++u) {
+              // value and slope by one Horner sweep (9 FMA)
+              const T xu = x[u];
+              T v = a[u][5], dv = a[u][5];
+              v = v * xu + a[u][4];
+              dv = dv * xu + v;
+              v = v * xu + a[u][3];
+              dv = dv * xu + v;
+              v = v * xu + a[u][2];
+              dv = dv * xu + v;
+              v = v * xu + a[u][1];
+              dv = dv * xu + v;
+              v = v * xu + a[u][0];
+              p[u][0] += v * d[0];
+              p[u][1] += v * d[1];
+              p[u][2] += v * d[2];
+              p[u][3] += v * d[3];
+              p[u][4] += dv * (e[u].x * d[0] + e[u].y * d[1] + e[u].z * d[2] + e[u].w * d[3]);
+            }
           }
         }
 #pragma unroll

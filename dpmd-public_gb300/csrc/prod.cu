@@ -152,7 +152,21 @@ struct ScatterU<double> {
 
 constexpr int kScatterWarps = 4;
 
-template <typename T, int U, bool WV>
+// F4: force rows padded to 4 floats (16-byte aligned), so that each F_j is
+// one red.global.add.v4.f32 instead of a v2 and a scalar reduction: the
+// reductions of a warp go to 32 distinct rows, and their cost in the
+// load/store unit scales with the instructions, not the bytes (measured: the
+// two-instruction form spends about a quarter of the force call on them).
+template <typename T, bool F4>
+__device__ __forceinline__ void scatter_force(T* __restrict__ force, size_t row, const T* v) {
+  if constexpr (F4) {
+    red4(reinterpret_cast<float*>(force) + row * 4, v[0], v[1], v[2], 0.f);
+  } else {
+    scatter3(force + row * 3, v);
+  }
+}
+
+template <typename T, int U, bool WV, bool F4>
 __global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
     T* __restrict__ force, T* __restrict__ atom_virial, double* __restrict__ vir_acc,
     const T* __restrict__ net, const T* __restrict__ dR, const T* __restrict__ rij,
@@ -223,7 +237,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
       ci[2] += v[2];
       const int j = cur.j[u];
       if (j < 0 || j >= nall) continue;
-      if (force) scatter3(force + ((size_t)f * nall + j) * 3, v);
+      if (force) scatter_force<T, F4>(force, (size_t)f * nall + j, v);
       if (WV) {
         T t[9];
 #pragma unroll
@@ -243,7 +257,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
         if (lane == 0) {
           const int i = (int)(row - (long)f * nloc);
           const T m[3] = {-ci[0], -ci[1], -ci[2]};
-          scatter3(force + ((size_t)f * nall + i) * 3, m);
+          scatter_force<T, F4>(force, (size_t)f * nall + i, m);
         }
       }
       ci[0] = ci[1] = ci[2] = T(0);
@@ -257,6 +271,17 @@ __global__ void __launch_bounds__(kScatterWarps * 32) k_scatter_atomic(
     fold();
     flush();
   }
+}
+
+// padded FP32 force rows [n][4] -> the output's [n][3]
+__global__ void k_force4_compact(float* __restrict__ force, const float4* __restrict__ f4,
+                                 size_t n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float4 v = f4[t];
+  force[3 * t] = v.x;
+  force[3 * t + 1] = v.y;
+  force[3 * t + 2] = v.z;
 }
 
 template <typename T>
@@ -551,6 +576,7 @@ size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct ProdWs {
   double* vir_acc;
+  float4* force4;    // atomic mode, FP32: padded force rows [nframes * nall]
   double* vir_part;  // deterministic frame-virial partials [nframes, nchunk, 9]
   int* cnt;
   int* start;
@@ -571,6 +597,7 @@ ProdWs carve_prod(void* base, int nframes, int nloc, int nall, int nnei, int det
     return r;
   };
   w.vir_acc = reinterpret_cast<double*>(take(sizeof(double) * 9 * (size_t)nframes));
+  if (!det) w.force4 = reinterpret_cast<float4*>(take(sizeof(float4) * (size_t)nframes * nall));
   if (det) {
     const size_t nchunk = (size_t)(nall + kVirChunk - 1) / kVirChunk;
     w.vir_part = reinterpret_cast<double*>(take(sizeof(double) * 9 * (size_t)nframes * nchunk));
@@ -614,8 +641,8 @@ int scatter_cap() {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_atomic<T, ScatterU<T>::U, WV>,
-                                                kScatterWarps * 32, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, k_scatter_atomic<T, ScatterU<T>::U, WV, sizeof(T) == 4>, kScatterWarps * 32, 0);
   return std::max(1, sms * std::max(1, per_sm));
 }
 
@@ -627,18 +654,29 @@ unsigned scatter_grid(size_t rows) {
 }
 
 template <typename T>
-void launch_atomic(T* force, T* atom_virial, double* vir_acc, const T* net, const T* dR,
-                   const T* rij, const int* nlist, int nloc, int nall, int nnei, int nframes,
-                   cudaStream_t st) {
+void launch_atomic(T* force, float4* force4, T* atom_virial, double* vir_acc, const T* net,
+                   const T* dR, const T* rij, const int* nlist, int nloc, int nall, int nnei,
+                   int nframes, cudaStream_t st) {
   const size_t rows = (size_t)nframes * nloc;
+  // FP32: forces accumulate in the padded rows of the workspace (zeroed by
+  // the caller), then compacted into the output
+  constexpr bool F4 = sizeof(T) == 4;
+  T* fdst = F4 && force ? reinterpret_cast<T*>(force4) : force;
   if (atom_virial)
-    k_scatter_atomic<T, ScatterU<T>::U, true><<<scatter_grid<T, true>(rows), kScatterWarps * 32,
-                                                0, st>>>(force, atom_virial, vir_acc, net, dR,
-                                                         rij, nlist, nloc, nall, nnei, nframes);
+    k_scatter_atomic<T, ScatterU<T>::U, true, F4><<<scatter_grid<T, true>(rows),
+                                                    kScatterWarps * 32, 0, st>>>(
+        fdst, atom_virial, vir_acc, net, dR, rij, nlist, nloc, nall, nnei, nframes);
   else
-    k_scatter_atomic<T, ScatterU<T>::U, false><<<scatter_grid<T, false>(rows),
-                                                 kScatterWarps * 32, 0, st>>>(
-        force, nullptr, nullptr, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+    k_scatter_atomic<T, ScatterU<T>::U, false, F4><<<scatter_grid<T, false>(rows),
+                                                     kScatterWarps * 32, 0, st>>>(
+        fdst, nullptr, nullptr, net, dR, rij, nlist, nloc, nall, nnei, nframes);
+  if constexpr (F4) {
+    if (force) {
+      const size_t n = (size_t)nframes * nall;
+      k_force4_compact<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+          reinterpret_cast<float*>(force), force4, n);
+    }
+  }
 }
 
 template <typename T>
@@ -668,9 +706,13 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
   ProdWs w = carve_prod(ws, nframes, nloc, nall, nnei, det);
   GBDP_REQUIRE(ws != nullptr || w.bytes == 0, "prod_force/virial: null workspace");
   GBDP_REQUIRE(ws_bytes >= w.bytes, "prod_force/virial: workspace %zu < %zu", ws_bytes, w.bytes);
-  if (force) cudaMemsetAsync(force, 0, sizeof(T) * (size_t)nframes * nall * 3, st);
+  // the FP32 atomic mode writes every force word from its padded rows
+  const bool f4 = !det && sizeof(T) == 4 && force;
+  const bool empty = nframes == 0 || nloc == 0 || nnei == 0;
+  if (force && (!f4 || empty))
+    cudaMemsetAsync(force, 0, sizeof(T) * (size_t)nframes * nall * 3, st);
   if (atom_virial) cudaMemsetAsync(atom_virial, 0, sizeof(T) * (size_t)nframes * nall * 9, st);
-  if (nframes == 0 || nloc == 0 || nnei == 0) {
+  if (empty) {
     if (virial) cudaMemsetAsync(virial, 0, sizeof(T) * (size_t)nframes * 9, st);
     GBDP_CHECK_LAUNCH("prod_force/virial");
     return GBDP_OK;
@@ -684,8 +726,9 @@ int prod_launch(T* force, T* virial, T* atom_virial, const T* net, const T* dR, 
   // atomic mode only where a virial is asked for
   if (!det) {
     if (atom_virial) cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
-    launch_atomic<T>(force, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
-                     nframes, st);
+    if (f4) cudaMemsetAsync(w.force4, 0, sizeof(float4) * (size_t)nframes * nall, st);
+    launch_atomic<T>(force, w.force4, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall,
+                     nnei, nframes, st);
     if (virial) k_vir_finish<T><<<(unsigned)((9 * nframes + 255) / 256), 256, 0, st>>>(
         virial, w.vir_acc, 9 * nframes);
   } else {
@@ -732,8 +775,8 @@ int prod_virial_impl(T* virial, T* atom_virial, const T* net, const T* dR, const
                "prod_virial_a: net_deriv and env_deriv must be 16-byte aligned");
   if (!det) {
     cudaMemsetAsync(w.vir_acc, 0, sizeof(double) * 9 * nframes, st);
-    launch_atomic<T>(nullptr, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall, nnei,
-                     nframes, st);
+    launch_atomic<T>(nullptr, nullptr, atom_virial, w.vir_acc, net, dR, rij, nlist, nloc, nall,
+                     nnei, nframes, st);
     k_vir_finish<T><<<(unsigned)((9 * nframes + 255) / 256), 256, 0, st>>>(virial, w.vir_acc,
                                                                              9 * nframes);
   } else {

@@ -356,17 +356,30 @@ __global__ void __launch_bounds__(W * 32)
     for (int t = 0; t < ts.ntypes; ++t) {
       const int s0 = ts.sec[t], cnt = sl.cnt[t];
       const T* tab = ts.table[tab_index(ts, t, ti)];
+      // the section's slots are in ascending distance, so neighbours that
+      // look up the same table row are consecutive (about a third of them
+      // on water, most in the outer shell where s(r) flattens): their
+      // coefficients stay in registers instead of being read again
+      T a[NQF > 0 ? NQF : 1][6];
+      int prev = -1;
       for (int j = 0; j < cnt; ++j) {
         const V4<T> e = sl.em[s0 + j];
         const T x = sl.xr[s0 + j];
-        const T* row = tab + (size_t)sl.idx[s0 + j] * rs;
+        const int idx = sl.idx[s0 + j];
+        if (idx != prev) {  // uniform over the warp
+          prev = idx;
+          const T* row = tab + (size_t)idx * rs;
+#pragma unroll
+          for (int q = 0; q < NQF; ++q) {
+            const int k = q * 32 + lane;
+            if (k < M) load_coef6_kp<T>(a[q], row, ts.ps, k);
+          }
+        }
 #pragma unroll
         for (int q = 0; q < NQF; ++q) {
           const int k = q * 32 + lane;
           if (k < M) {
-            T a[6];
-            load_coef6_kp<T>(a, row, ts.ps, k);
-            const T v = poly5(a, x);
+            const T v = poly5(a[q], x);
             acc[q][0] += v * e.x;
             acc[q][1] += v * e.y;
             acc[q][2] += v * e.z;

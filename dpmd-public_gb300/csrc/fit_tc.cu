@@ -338,6 +338,10 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
   unsigned char* outb = wsm + EPI_IN_BYTES;    // [2 buf][o0 | hi | lo]
   const int nin = ep.nin;
   constexpr int NCH = TBN / 16;
+  // a layer's last tile may be partial (columns past ep.ncols skipped); the
+  // chunk counter advances by the chunks done, so that the staging buffers'
+  // barrier phases stay in step across the tiles of a persistent CTA
+  const int nch = min(NCH, (ep.ncols - n0 + 15) / 16);
   // F1: the inverse scale of this thread's D row; the split output's scale
   const float rsc = ep.kind == EPI_F1 ? __ldg(ep.rscale + yrow + lane) : 1.f;
   const float osc = ep.oscale[t];
@@ -354,10 +358,9 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
     ++es.in_issued;
   }
 #pragma unroll 1
-  for (int ci = 0; ci < NCH; ++ci) {
+  for (int ci = 0; ci < nch; ++ci) {
     const int c0 = ci * 16, g = es.gci + ci, buf = g & 1;
-    if (n0 + c0 >= ep.ncols) break;  // a last tile's columns past the layer (no inputs issued)
-    if (ci + 1 < NCH && n0 + c0 + 16 < ep.ncols && nin > 0) {
+    if (ci + 1 < nch && nin > 0) {
       // the other input buffer was last read by the previous chunk
       fence_proxy_async_smem();
       __syncwarp();
@@ -458,7 +461,7 @@ __device__ __forceinline__ bool epi_tile(const TcMaps& maps, const TcEpi& ep, in
       bulk_commit();
     }
   }
-  es.gci += NCH;
+  es.gci += nch;
   return true;
 }
 
@@ -621,7 +624,7 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // Persistent form of k_fit_tc for a layer with one main accumulator, used for
-// B1 (20 N tiles of 80 per row block: about 12 tiles per SM on the
+// B1 (13 N tiles of 128 per row block: about 8 tiles per SM on the
 // 12,288-row step) and for the K-240 layers once they have many tiles per
 // SM (on the 12,288-row step they have about two and run faster as two
 // per-tile CTAs per SM): one CTA per SM walks the layer's tiles, the N tiles
@@ -630,8 +633,10 @@ __global__ void __launch_bounds__(128, 1)
 // warp 1 the MMAs, warps 2-5 run the epilogue (warp w reads TMEM lanes
 // 32 (w % 4) ..).  Two tensor-memory buffers of (main, cross) accumulators
 // let the MMAs of the next tile run while the epilogue drains the last one.
-constexpr int PERS_TBN = 80, PERS_STAGES = 3;
-constexpr int PERS_STAGE = 2 * A_TILE + 2 * PERS_TBN * TBK * 2;  // 52 KiB
+// 128-wide tiles (the last one of a layer partial: 240 = 128 + 112, 1600 =
+// 12 x 128 + 64, its padding columns skipped by the epilogue), two stages.
+constexpr int PERS_TBN = 128, PERS_STAGES = 2;
+constexpr int PERS_STAGE = 2 * A_TILE + 2 * PERS_TBN * TBK * 2;  // 64 KiB
 constexpr int PERS_SMEM = PERS_STAGES * PERS_STAGE + 4 * EPI_WARP_BYTES + 1024 + 256;
 static_assert(PERS_SMEM <= 227 * 1024, "persistent fitting kernel shared memory");
 
@@ -1012,7 +1017,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
   base.ntypes = ntypes;
   for (int t = 0; t <= ntypes; ++t) base.row_off[t] = row_off[t];
   base.status = status;
-  base.ntile_n = FIT_W / PERS_TBN;  // F3's N tiles
+  // (base.ntile_n, F3's N tiles, is set below with the K-240 layers' kernel)
   for (int t = 0; t < ntypes; ++t) {
     base.wout[t] = nets[t].w_out;
     base.idt2[t] = nets[t].idt[1];
@@ -1027,6 +1032,8 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
   const long short_tiles = (rows / TBM) * (FIT_W / CfgShortK::TBN);
   const int short_cfg =
       short_tiles >= (long)g_short_pers_min_tiles.load() * nsm ? PERSIST : SHORTK;
+  // F3's partial energies: one per N tile of the kernel that runs it
+  base.ntile_n = short_cfg == PERSIST ? (FIT_W + PERS_TBN - 1) / PERS_TBN : FIT_W / CfgShortK::TBN;
   // act: index into act_scale of the split output (-1: none)
   struct Step {
     int kind;
@@ -1038,8 +1045,8 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
     int act;
     int cfg;
   };
-  static_assert(FIT_W % CfgShortK::TBN == 0 && FIT_D % PERS_TBN == 0 &&
-                    CfgShortK::TBN == PERS_TBN && CfgLongK::TBN % 16 == 0,
+  static_assert(FIT_W % CfgShortK::TBN == 0 && PERS_TBN % 16 == 0 && CfgLongK::TBN % 16 == 0 &&
+                    FIT_W / CfgShortK::TBN <= 3 && (FIT_W + PERS_TBN - 1) / PERS_TBN <= 3,
                 "tile widths must divide the layer widths (F1's last tile may be partial)");
   const Step steps[6] = {
       {EPI_F1, D_hi, D_lo, FIT_D, FIT_W, 0, true, {nullptr, nullptr}, {ws.t1, ws.h1h, ws.h1l}, 0,
@@ -1116,7 +1123,7 @@ extern "C" int gbdp_fitting_tc_f32(float* e, float* dE_dD, const void* D_hi, con
       le = cudaLaunchKernelEx(&lc, k_fit_tc<CfgShortK>, maps, ep, sp.K);
     } else {
       // one CTA per SM walking the layer's tiles
-      const int ntn = sp.N / PERS_TBN, ntiles = ntn * (int)(rows / TBM);
+      const int ntn = (sp.N + PERS_TBN - 1) / PERS_TBN, ntiles = ntn * (int)(rows / TBM);
       lc.gridDim = dim3((unsigned)(ntiles < nsm ? ntiles : nsm));
       lc.blockDim = dim3(192);
       lc.dynamicSmemBytes = PERS_SMEM;

@@ -74,9 +74,11 @@ def test_tc_fused_step_vs_fp64(setup):
 
 def test_persistent_short_k_layers_equal_per_tile(setup):
     """The K-240 layers on the persistent kernel (forced with a threshold of
-    one tile per SM) give the same bits as one CTA per tile: the same MMAs
-    into the same accumulators and the same epilogue, on a ragged batch of
-    two type blocks."""
+    one tile per SM, 128-wide tiles) give the same bits as one CTA per tile
+    (80-wide tiles): the same MMAs into the same accumulators and the same
+    epilogue per column, on a ragged batch of two type blocks.  The atom
+    energies sum F3's per-tile partials, two of them against three, so they
+    agree to rounding only."""
     se_a, cfg, m64, mk, water = setup
     tc = mk("tc-f16x3")
     frames = water.ragged_frames(12, seed=31, lo=40, hi=300)
@@ -94,5 +96,6 @@ def test_persistent_short_k_layers_equal_per_tile(setup):
             out.append((b.ae.clone(), b.dD.clone(), F.clone(), V.clone()))
     finally:
         lib.gbdp_fitting_tc_set_persistent_min_tiles(32)
-    for x, y in zip(out[0], out[1]):
+    torch.testing.assert_close(out[0][0], out[1][0], rtol=1e-6, atol=1e-6)
+    for x, y in zip(out[0][1:], out[1][1:]):
         assert torch.equal(x, y)

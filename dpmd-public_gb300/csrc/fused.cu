@@ -180,6 +180,11 @@ __device__ __forceinline__ void bwd_tab_grad_pairs(float* p, const float* __rest
   }
 }
 
+// a non-binding prefetch of the 128-byte line holding p into L2
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // one row of 4 values (16-byte aligned), not allocated in L1
 __device__ __forceinline__ float4 ld_stream4(const float* p) {
   float4 v;
@@ -553,12 +558,29 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
                const int* __restrict__ nlist_ext, const T* __restrict__ ext_coord,
                const int* __restrict__ ext_map, const int* __restrict__ atype,
                const T* __restrict__ inv_std, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
-               int nnei, int M) {
+               int nnei, int M, int pf_dist) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   constexpr int MP = NQ * 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * W + warp;
   if (i >= nloc) return;
+  {
+    // the atom pf_dist ahead (about one wave of resident warps later):
+    // its dE/dD row, X and env rows prefetched into L2, so that the warp
+    // that takes it finds its first loads in L2 rather than in DRAM
+    const int ip = i + pf_dist;
+    if (pf_dist > 0 && ip < nloc) {
+      const size_t rp = drow ? (size_t)drow[ip] : (size_t)ip;
+      const char* pd = reinterpret_cast<const char*>(dD + rp * M * kAxis);
+      const char* px = reinterpret_cast<const char*>(X + (size_t)ip * 4 * M);
+      const char* pe = reinterpret_cast<const char*>(em + (size_t)ip * nnei * 4);
+      const int ld = (int)((sizeof(T) * M * kAxis + 127) / 128),
+                lx = (int)((sizeof(T) * 4 * M + 127) / 128),
+                le = (int)((sizeof(T) * 4 * nnei + 127) / 128);
+      for (int l = lane; l < ld + lx + le; l += 32)
+        prefetch_l2(l < ld ? pd + 128 * l : l < ld + lx ? px + 128 * (l - ld) : pe + 128 * (l - ld - lx));
+    }
+  }
   const int ti = atype[i];
   if (ti < 0) return;
   unsigned char* wbase = smem_raw + (size_t)warp * bwd_warp_bytes<T>(nnei, MP);
@@ -1175,9 +1197,15 @@ void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, l
   const int per_sm = ((U == 1 ? 28 : 24) / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
+  // prefetch distance: the warps resident on the device at once
+  int dev = 0, sms = 0, ctas = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, W * 32, smem);
+  const int pf_dist = sms * ctas * W;
   kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(
       force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, inv_std,
-      geo, ts, rmin, rmax, nloc, nnei, M);
+      geo, ts, rmin, rmax, nloc, nnei, M, pf_dist);
 }
 
 template <typename T, int W, int U>

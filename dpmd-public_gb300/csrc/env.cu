@@ -536,7 +536,7 @@ __device__ __forceinline__ void env_row_store(const T* xj, T xi, T yi, T zi, int
   }
 }
 
-// Ascending bitonic sort of 128 64-bit keys held by a warp, element
+// Ascending bitonic sort of 32 E 64-bit keys held by a warp, element
 // e * 32 + lane in v[e]: partners closer than 32 are in other lanes
 // (shuffles), farther ones in the same lane (register swaps).
 __device__ __forceinline__ uint64_t shfl_xor64(uint64_t x, int m) {
@@ -545,15 +545,16 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t x, int m) {
   return ((uint64_t)hi << 32) | lo;
 }
 
-__device__ __forceinline__ void warp_bitonic128(uint64_t* v, int lane) {
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint64_t* v, int lane) {
 #pragma unroll
-  for (int k = 2; k <= 128; k <<= 1) {
+  for (int k = 2; k <= 32 * E; k <<= 1) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
       if (j >= 32) {
         const int je = j >> 5;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
+        for (int e = 0; e < E; ++e) {
           if (e & je) continue;
           const int i = e * 32 + lane;
           const bool asc = (i & k) == 0;
@@ -565,7 +566,7 @@ __device__ __forceinline__ void warp_bitonic128(uint64_t* v, int lane) {
         }
       } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
+        for (int e = 0; e < E; ++e) {
           const int i = e * 32 + lane;
           const bool asc = (i & k) == 0;
           const bool lower = (lane & j) == 0;
@@ -575,6 +576,25 @@ __device__ __forceinline__ void warp_bitonic128(uint64_t* v, int lane) {
         }
       }
     }
+  }
+}
+
+// One type's candidates (n <= 32 E keys (r^2, index) at stage[0, n)) sorted
+// by a warp and the first sel of them placed at their ranks in row[].
+template <int E>
+__device__ __forceinline__ void sort_type_rows(const uint64_t* stage, int n, int sel, int* row,
+                                               int lane) {
+  uint64_t v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int c = e * 32 + lane;
+    v[e] = c < n ? stage[c] : ~0ull;
+  }
+  warp_bitonic<E>(v, lane);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int pos = e * 32 + lane;
+    if (pos < n && pos < sel) row[pos] = (int)(uint32_t)(v[e] & 0xffffffffu);
   }
 }
 
@@ -753,7 +773,36 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   }
   for (int s = lane; s < nnei; s += 32) row[s] = -1;
   __syncwarp();
-  if (ncand <= 128) {
+  if (ncand <= 128 && max_cand >= 256) {
+    // ---- up to 128 candidates: each type's (r^2, index) keys compacted
+    //      into a staging area past them (keys[128, 256)) and sorted on
+    //      their own by the smallest bitonic network that holds them (32,
+    //      64 or 128 keys): about half the compare-exchange steps of one
+    //      128-key sort over all types on water (~30 O and ~60 H)
+    uint64_t* stage = keys + 128;
+    for (int t = 0; t < si.ntypes; ++t) {
+      int n = 0;
+      for (int c0 = 0; c0 < ncand; c0 += 32) {
+        const int cc = c0 + lane;
+        const bool is_t = cc < ncand && (int)ctype[cc] == t;
+        const unsigned m = __ballot_sync(kFull, is_t);
+        if (is_t) stage[n + __popc(m & ((1u << lane) - 1u))] = keys[cc];
+        n += __popc(m);
+      }
+      __syncwarp();
+      const int sel_t = si.sec[t + 1] - si.sec[t];
+      int* rt = row + si.sec[t];
+      if (n > 0 && sel_t > 0) {
+        if (n <= 32)
+          sort_type_rows<1>(stage, n, sel_t, rt, lane);
+        else if (n <= 64)
+          sort_type_rows<2>(stage, n, sel_t, rt, lane);
+        else
+          sort_type_rows<4>(stage, n, sel_t, rt, lane);
+      }
+      __syncwarp();  // the staging area is read before the next type refills it
+    }
+  } else if (ncand <= 128) {
     // ---- up to 128 candidates: a bitonic sort of (type, r^2, index) keys
     //      in registers; a candidate's rank in its type is its sorted
     //      position minus the number of candidates of lower types.
@@ -765,7 +814,7 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
                              (keys[c] & 0xffffffull)
                        : ~0ull;
     }
-    warp_bitonic128(v, lane);
+    warp_bitonic<4>(v, lane);
     int below = 0;  // candidates of types lower than the current one
     for (int t = 0; t < si.ntypes; ++t) {
       int cnt = 0;

@@ -784,23 +784,25 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
             }
           }
         }
-#pragma unroll
-        for (int o = 8; o >= 1; o >>= 1)
-#pragma unroll
-          for (int u = 0; u < U; ++u)
-#pragma unroll
-            for (int c = 0; c < 5; ++c) p[u][c] += __shfl_xor_sync(kFull, p[u][c], o);
+        // dE/d em[j, :] = (p0 + p4, p1, p2, p3) summed over the 16-lane
+        // group (em_x is em[:, 0]) by a reduce-scatter: the halves of the
+        // group exchange half of the four sums (xor 8), then half of the
+        // rest (xor 4), and the last two levels add one value each, so lane
+        // t16 ends with component (t16 >> 2) & 3 (5 shuffles instead of the
+        // 20 of four full butterflies over five sums)
 #pragma unroll
         for (int u = 0; u < U; ++u) {
+          const bool h8 = (t16 & 8) != 0, h4 = (t16 & 4) != 0;
+          const T q0 = p[u][0] + p[u][4];
+          const T r0 = __shfl_xor_sync(kFull, h8 ? q0 : p[u][2], 8);
+          const T r1 = __shfl_xor_sync(kFull, h8 ? p[u][1] : p[u][3], 8);
+          const T a0 = (h8 ? p[u][2] : q0) + r0;
+          const T a1 = (h8 ? p[u][3] : p[u][1]) + r1;
+          T b = (h4 ? a1 : a0) + __shfl_xor_sync(kFull, h4 ? a0 : a1, 4);
+          b += __shfl_xor_sync(kFull, b, 2);
+          b += __shfl_xor_sync(kFull, b, 1);
           const int j = j0 + n + 2 * u;
-          if (t16 == 0 && j < nv) {
-            V4<T> net;  // dE/d em[j, :]; em_x is em[:, 0]
-            net.x = p[u][0] + p[u][4];
-            net.y = p[u][1];
-            net.z = p[u][2];
-            net.w = p[u][3];
-            sl.em[s0 + j] = net;
-          }
+          if ((t16 & 3) == 0 && j < nv) reinterpret_cast<T*>(&sl.em[s0 + j])[t16 >> 2] = b;
         }
       }
     }

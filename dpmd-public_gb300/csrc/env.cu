@@ -702,12 +702,19 @@ __global__ void __launch_bounds__(kEnvWarps * 32)
   }
   const int sy = 2 * hw[1] + 1, sz = 2 * hw[2] + 1;
   const int nst = MODE == kEnvList ? 0 : (2 * hw[0] + 1) * sy * sz;
+  // stencil offsets from the flat index by reciprocal multiplies instead of
+  // integer divisions: floor((q + 1/2) / d) from FP32 is exact while
+  // q + 1/2 < 2^22 (the product's relative error, 2^-23, stays below the
+  // 1/(2d) gap to the nearest integer), and nst is a few hundred
+  const float inv_z = 1.f / (float)sz, inv_yz = 1.f / (float)(sy * sz);
   int* vrow = MODE == kEnvBuild ? vl.idx + (size_t)i * vl.cap : nullptr;
   for (int cg = 0; cg < nst; cg += 32) {
     const int q = cg + lane;
     int st = 0, cnt = 0;
     if (q < nst) {
-      const int o[3] = {q / (sy * sz) - hw[0], (q / sz) % sy - hw[1], q % sz - hw[2]};
+      const int q0 = (int)(((float)q + 0.5f) * inv_yz), rq = q - q0 * sy * sz;
+      const int q1 = (int)(((float)rq + 0.5f) * inv_z), q2 = rq - q1 * sz;
+      const int o[3] = {q0 - hw[0], q1 - hw[1], q2 - hw[2]};
       int E[3], h = 0;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {

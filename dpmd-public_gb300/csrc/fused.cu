@@ -538,11 +538,13 @@ __device__ __forceinline__ int filled_prefix(const int* __restrict__ nl, int ns)
 }
 
 template <typename T>
-__host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int mp) {
-  // dy4 [mp] and X^T [mp] while dX is formed, then the slot arrays over them
+__host__ __device__ constexpr size_t bwd_warp_bytes(int nnei, int m) {
+  // dy4 [M] and X^T [M] while dX is formed, then the slot arrays over them
   // (dy is in registers by then): the smaller the footprint, the more L1 is
-  // left for table rows
-  return max_sz(slots_bytes<T>(nnei), (size_t)2 * mp * sizeof(V4<T>));
+  // left for table rows (M = 100, nnei = 138: 3,328 B a warp, so that the
+  // 28 resident warps fit the 100 KB shared-memory carveout and leave
+  // 156 KB of L1)
+  return max_sz(slots_bytes<T>(nnei), (size_t)2 * m * sizeof(V4<T>));
 }
 
 // Phase 1 runs 16 lanes per neighbour.
@@ -583,9 +585,9 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
   }
   const int ti = atype[i];
   if (ti < 0) return;
-  unsigned char* wbase = smem_raw + (size_t)warp * bwd_warp_bytes<T>(nnei, MP);
+  unsigned char* wbase = smem_raw + (size_t)warp * bwd_warp_bytes<T>(nnei, M);
   V4<T>* dy4 = reinterpret_cast<V4<T>*>(wbase);
-  V4<T>* xT = dy4 + MP;  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k)
+  V4<T>* xT = dy4 + M;  // X^T: xT[k] = (X_0k, X_1k, X_2k, X_3k), k < M
   T* xTs = reinterpret_cast<T*>(xT);
   // all of X's loads issued before the first is stored (no dependent chain)
   {
@@ -1271,8 +1273,7 @@ int desc_bwd(T* force, double* vir_acc, const T* X, const T* dD, const int* drow
                    ((uintptr_t)inv_std & 15) == 0,
                "se_a descriptor bwd: em / dE_dD / inv_std must be 16-byte aligned");
   BwdGeom geo{atom_frame, frame_aoff, frame_eoff};
-  const int nq = (M + 31) / 32;
-  const size_t wb = bwd_warp_bytes<T>(nnei, nq * 32);
+  const size_t wb = bwd_warp_bytes<T>(nnei, M);
   GBDP_REQUIRE((size_t)kBWarps * wb <= 200 * 1024,
                "se_a descriptor bwd: nnei %d needs %zu bytes of shared memory", nnei,
                (size_t)kBWarps * wb);

@@ -180,3 +180,21 @@ def test_force_virial_in_one_pass(gb, oracle, dtype, det):
         tol = 1e-12 if dtype == torch.float64 else 2e-5
         for a, b in ((f1, f2), (v1, v2), (av1, av2)):
             assert float((a - b).abs().max()) <= tol * max(1.0, float(a.abs().max()))
+
+
+def test_many_frames_force_fp32(gb, oracle):
+    """FP32 atomic force over 40 frames in one call: the forces accumulate
+    in padded 16-byte rows of the workspace (frame f, atom j at row
+    f * nall + j) and are compacted into [nframes, nall * 3]; every frame
+    against the oracle, nothing left at a zero fill."""
+    ops = __import__("dpmd_public_gb300.ops", fromlist=["x"])
+    nloc, nnei, net, emd, rij, nl = _water_case(gb, oracle, torch.float32, n=2, L=6.2, seed=29)
+    nf = 40
+    nets = np.random.default_rng(8).normal(0, 1, (nf, net.size)).astype(np.float32)
+    natoms = torch.tensor([nloc, nloc, 0, 0], dtype=torch.int32)
+    rep = lambda a: torch.tensor(np.tile(a.reshape(1, -1), (nf, 1)), device=DEV)
+    f = ops.prod_force_se_a_impl(torch.tensor(nets, device=DEV), rep(emd), rep(nl), natoms, nnei, 0)
+    assert f.shape == (nf, nloc * 3)
+    for k in range(nf):
+        fo = oracle.prod_force_a(nets[k], emd, nl, nloc, nloc, nnei)
+        np.testing.assert_allclose(f[k].cpu().numpy(), np.reshape(fo, -1), atol=2e-3, rtol=1e-4)

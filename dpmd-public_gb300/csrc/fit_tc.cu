@@ -53,7 +53,7 @@ namespace {
 constexpr int TBM = 128, TBK = 64;     // a k-block: 64 FP16 = one 128-byte swizzle row
 constexpr int A_TILE = TBM * TBK * 2;  // 16 KiB
 
-// Tile configurations of the per-tile kernel k_fit_tc (128 x 80 tiles):
+// Tile configurations of the per-tile kernel k_fit_tc:
 //   CfgLongK   F1 (K 1600): 128 x 128 tiles (two N tiles, the second
 //              holding columns 128-239 and 16 zero-filled ones that the
 //              epilogue skips), 3 stages, 3 main accumulators, one CTA per
@@ -61,17 +61,17 @@ constexpr int A_TILE = TBM * TBK * 2;  // 16 KiB
 //              block instead of three times with 80-wide tiles, and each
 //              stage carries 1.6x the MMA work for 1.23x the bytes
 //              (the fitting 4.56 -> 4.19 ms on the 512-frame ragged batch,
-//              same bits).  The 3 accumulators keep
-//              the long chain FP32-accurate: one main accumulator measured
+//              same bits).  The 3 accumulators keep the long chain
+//              FP32-accurate: one main accumulator measured
 //              2.3x the energy error and 7x the frame-virial error, its
 //              truncation errors adding up coherently over a frame.
-//   CfgShortK  K 240 layers: 2 stages, 1 main accumulator, two CTAs per SM
+//   CfgShortK  K 240 layers: 128 x 80 tiles, 2 stages, 1 main accumulator, two CTAs per SM
 //              (105 KB shared, 256 TMEM columns each): with about two tiles
 //              per SM, a second CTA's epilogue overlapping the first's main
 //              loop measured faster than the persistent kernel (about 21 us
 //              against 25-27 us a layer).
-// B1 (1920 tiles of 128 x 80 on the 12,288-row step, about 12 per SM) runs
-// on the persistent kernel k_fit_pers (64 us -> 49 us).
+// B1 runs on the persistent kernel k_fit_pers (with 128 x 80 tiles on the
+// 12,288-row step: 64 us per tile-CTA -> 49 us persistent).
 template <int TBN_, int STAGES_, int NACC_>
 struct TcCfg {
   static constexpr int TBN = TBN_, STAGES = STAGES_, NACC = NACC_;

@@ -312,7 +312,10 @@ GBDP_API int gbdp_env_status(const void* workspace, gbdp_stream stream);
  * rij [nframes, nloc, nnei, 3], nlist [nframes, nloc, nnei] (indices in
  * [0, nall)), force [nframes, nall, 3], virial [nframes, 9], atom_virial
  * [nframes, nall, 9].  deterministic != 0 gathers through a reverse
- * neighbour list (bitwise reproducible); 0 scatters with atomics.
+ * neighbour list (bitwise reproducible); 0 scatters with atomics (FP32
+ * forces accumulate in 16-byte padded rows of the workspace, one vector
+ * reduction a pair, then are compacted into `force`; the workspace size
+ * below includes those rows).
  * ---------------------------------------------------------------------- */
 GBDP_API size_t gbdp_prod_workspace_bytes(int nframes, int nloc, int nall, int nnei, int deterministic);
 GBDP_API int gbdp_prod_force_a_f32(float* force, const float* net_deriv, const float* env_deriv,

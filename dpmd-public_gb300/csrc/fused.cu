@@ -562,7 +562,6 @@ __global__ void __launch_bounds__(W * 32, sizeof(T) == 4 ? (U == 1 ? 28 : 24) / 
                const T* __restrict__ inv_std, BwdGeom geo, TabSet<T> ts, T rmin, T rmax, int nloc,
                int nnei, int M, int pf_dist) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
-  constexpr int MP = NQ * 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * W + warp;
   if (i >= nloc) return;
@@ -1201,12 +1200,22 @@ void launch_bwd(size_t warp_bytes, cudaStream_t st, T* force, double* vir_acc, l
   const int per_sm = ((U == 1 ? 28 : 24) / W) * (int)(smem + 1024);
   cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                        per_sm >= 228 * 1024 ? 100 : (per_sm * 100 + 228 * 1024 - 1) / (228 * 1024));
-  // prefetch distance: the warps resident on the device at once
-  int dev = 0, sms = 0, ctas = 0;
+  // prefetch distance: the warps resident on the device at once (the
+  // occupancy query is repeated only when the device or the shared-memory
+  // size of this instantiation changes)
+  thread_local int c_dev = -1, c_pf = 0;
+  thread_local size_t c_smem = 0;
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, W * 32, smem);
-  const int pf_dist = sms * ctas * W;
+  if (dev != c_dev || smem != c_smem) {
+    int sms = 0, ctas = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, W * 32, smem);
+    c_dev = dev;
+    c_smem = smem;
+    c_pf = sms * ctas * W;
+  }
+  const int pf_dist = c_pf;
   kern<<<(unsigned)((nloc + W - 1) / W), W * 32, smem, st>>>(
       force, vir_acc, force_fx, X, dD, drow, em, nlist_ext, ext_coord, ext_map, atype, inv_std,
       geo, ts, rmin, rmax, nloc, nnei, M, pf_dist);

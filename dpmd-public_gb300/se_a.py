@@ -712,6 +712,12 @@ class Batch:
         dev = model.device
         dt = model.dtype
         at = [np.asarray(a, np.int32).reshape(-1) for a in atype_per_frame]
+        # every atom gets a row of D / dE/dD by its type, which the fused
+        # kernels write and read; a type outside the model has none
+        for f, a in enumerate(at):
+            if a.size and (a.min() < 0 or a.max() >= cfg.ntypes):
+                raise ValueError(f"frame {f}: atom types must lie in [0, {cfg.ntypes}) "
+                                 f"(got {int(a.min())} .. {int(a.max())})")
         self.nframes = len(at)
         self.skin = float(skin)
         self.plan = NeighborPlan([len(a) for a in at], np.asarray(boxes, np.float64).reshape(-1, 9),

@@ -390,7 +390,9 @@ GBDP_API int gbdp_prod_virial_grad_a_f64(double* grad_net, const double* grad, c
  * [n_tables * 6];
  * sel: HOST [ntypes].  em comes from gbdp_prod_env_mat_a_*.  d_row (device,
  * may be NULL for the identity) gives the row of D / dE_dD that belongs to
- * atom i, so that a caller can keep each type's rows contiguous.
+ * atom i, so that a caller can keep each type's rows contiguous; it must
+ * hold a valid row for every atom, an atom of type < 0 included (the
+ * forward writes its row, from zero sums).
  * Backward: from dE/dD, force [nloc, 3] (zeroed here, local indices, packed
  * frames) and virial_acc [nframes, 9] (double, zeroed here) get the
  * contributions of every real neighbour, the env-matrix derivative being

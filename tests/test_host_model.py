@@ -169,3 +169,24 @@ def test_tables_match_reference_dptabulate(m, tag):
             assert np.abs(da - db).max() <= 1e-11 * dmax, (name, f)
         colsum = np.abs(tabs[ours]).reshape(tabs[ours].shape[0], -1, 6).sum(axis=(0, 1))
         np.testing.assert_allclose(colsum[:3], g[f"{tag}_{k}_colsum"][:3], rtol=1e-13)
+
+
+def test_batch_rejects_atom_types_outside_the_model(gb):
+    """A fused-step batch gives every atom a row of D by its type; a type
+    outside [0, ntypes) is rejected before any device work."""
+    import importlib
+
+    import pytest
+
+    se_a = importlib.import_module("dpmd_public_gb300.se_a")
+    mdl = importlib.import_module("dpmd_public_gb300.model")
+
+    class _Model:  # only what Batch reads before the check
+        cfg = mdl.SeAConfig()
+        device = "cpu"
+        dtype = None
+
+    box = np.diag([12.0] * 3).reshape(1, 9)
+    for bad in ([0, 1, -1], [0, 2, 1]):
+        with pytest.raises(ValueError, match="atom types"):
+            se_a.Batch(_Model(), [np.array(bad, np.int32)], box)
